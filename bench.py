@@ -1,0 +1,387 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 dense LU path (PDGESV on a 1x1 grid).
+
+Workload (one "step"): plain FP64 PDGESV, N=16384, NB=256, NRHS=16, A and B iid
+uniform[-0.5,0.5] from a seeded generator -- the configuration the headline
+metric "LU solve TFLOP/s (2N^3/3)" is quoted on.
+
+  value  device-resident: inputs already in HBM; each step restores A and B
+         from pristine device copies and calls sl1x1_dgesv_dev. 2N^3/3 flops
+         per step; whole-job TFLOP/s summed over ranks (max time over ranks).
+  e2e    the same solve through the Fortran-ABI entry point pdgesv_ with A and
+         B in pinned host memory: H2D of A and B, factor, solve, D2H of the
+         factors, IPIV and X are all inside the timed region.
+  roofline  the FP64 trailing update (PDGEMM, DMMA kernel) timed live with the
+         library's phase events on its launching stream, against the FP64
+         tensor peak measured live by a register-only DMMA loop.
+  cpu_baseline  the CPU restatement of the reference (oracle/, OpenBLAS, all
+         host cores) on a bounded sample of the same workload, rank 0 only.
+
+--impl reference times that CPU implementation alone (rank 0; other ranks exit).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = ("LU solve TFLOP/s (2N³/3) plain FP64 vs mixed-IR at matched residual; "
+          "batched solve/s")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    p.add_argument("--n", type=int, default=16384)
+    p.add_argument("--nb", type=int, default=256)
+    p.add_argument("--nrhs", type=int, default=16)
+    p.add_argument("--seed", type=int, default=2024)
+    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def make_inputs(n, nrhs, seed):
+    rng = np.random.default_rng(seed)
+    A = np.asfortranarray(rng.uniform(-0.5, 0.5, size=(n, n)))
+    B = np.asfortranarray(rng.uniform(-0.5, 0.5, size=(n, nrhs)))
+    return A, B
+
+
+def flops_lu(n):
+    return 2.0 * n ** 3 / 3.0
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_solve_sample(A, B, nb, budget_s=25.0):
+    """Time the oracle's PDGESV restatement (host BLAS, all cores) on a bounded
+    sample of the workload: the full matrix when its estimated time fits the
+    budget, else the leading n x n block with n scaled down to fit."""
+    from oracle import oracle as orc
+
+    orc.lib()
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    n_full = A.shape[0]
+    n0 = min(2048, n_full)
+    a0 = np.asfortranarray(A[:n0, :n0].copy())
+    b0 = np.asfortranarray(B[:n0, :].copy())
+    t = time.perf_counter()
+    orc.solve_reference(a0, b0, nb=nb)
+    t0 = time.perf_counter() - t
+    est = t0 * (n_full / n0) ** 3
+    n = n_full if est <= budget_s else int(n0 * (budget_s / t0) ** (1 / 3)) // nb * nb
+    n = max(min(n, n_full), n0)
+    a = np.asfortranarray(A[:n, :n].copy())
+    b = np.asfortranarray(B[:n, :].copy())
+    t = time.perf_counter()
+    LU, ipiv, X, info = orc.solve_reference(a, b, nb=nb)
+    dt = time.perf_counter() - t
+    return {"value": flops_lu(n) / dt / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+            "sample": f"oracle PDGESV restatement (OpenBLAS, {cores} threads), N={n} NB={nb} "
+                      f"NRHS={B.shape[1]}, one solve of {dt:.2f} s",
+            "blas_loaded": orc.blas_loaded(), "seconds": dt, "n": n}
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist  # noqa: F811
+
+        backend = "nccl" if args.impl == "gpu" else "gloo"
+        dist.init_process_group(backend=backend)
+    return ws, rank, local, dist
+
+
+def run_reference(args):
+    ws, rank, local, dist = dist_init(args)
+    if rank != 0:
+        return 0
+    A, B = make_inputs(args.n, args.nrhs, args.seed)
+    from oracle import oracle as orc
+
+    orc.lib()
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    # bounded sample per step so that W + K steps end within a few minutes
+    per_step_budget = max(5.0, 150.0 / max(1, args.steps + args.warmup))
+    probe = cpu_solve_sample(A, B, args.nb, budget_s=per_step_budget)
+    n = probe["n"]
+    a0 = np.asfortranarray(A[:n, :n].copy())
+    b0 = np.asfortranarray(B[:n, :].copy())
+    for _ in range(args.warmup):
+        orc.solve_reference(a0, b0, nb=args.nb)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        orc.solve_reference(a0, b0, nb=args.nb)
+    dt = (time.perf_counter() - t) / args.steps
+    val = flops_lu(n) / dt / 1e12
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "TFLOP/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": f"synthetic: A, B iid U[-0.5,0.5] (numpy PCG64 seed {args.seed})",
+        "config": {"workload": f"plain FP64 PDGESV (1x1 grid) N={args.n} NB={args.nb} "
+                               f"NRHS={args.nrhs}; CPU sample N={n}", "n": args.n, "nb": args.nb,
+                   "nrhs": args.nrhs, "sample_n": n},
+        "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                         "sample": f"oracle PDGESV restatement on host BLAS (OpenBLAS, {cores} "
+                                   f"threads), N={n} NB={args.nb} NRHS={args.nrhs} per step; the "
+                                   "Fortran/MPI reference cannot be compiled here"},
+        "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    ws, rank, local, dist = dist_init(args)
+    torch.cuda.set_device(local)
+    import scalapack_gb300 as sl
+
+    L = sl.lib(build_if_missing=True)
+    if L.sl1x1_device_ok() != 1:
+        raise SystemExit("sl1x1: no usable sm_103 GPU")
+    n, nb, nrhs = args.n, args.nb, args.nrhs
+    A, B = make_inputs(n, nrhs, args.seed + rank)
+    dev = torch.device("cuda", local)
+    # column-major device copies: torch row-major (cols, rows) == Fortran (rows, cols)
+    dA0 = torch.from_numpy(A.T).to(dev)  # contiguous (n, n) holding A column-major
+    dB0 = torch.from_numpy(B.T).to(dev)
+    dA = torch.empty_like(dA0)
+    dB = torch.empty_like(dB0)
+    dpiv = torch.empty(n, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    def step():
+        dA.copy_(dA0)
+        dB.copy_(dB0)
+        info = sl.dgesv_dev(n, nrhs, dA.data_ptr(), n, dpiv.data_ptr(), dB.data_ptr(), n, nb,
+                            stream=sptr)
+        if info != 0:
+            raise RuntimeError(f"sl1x1_dgesv_dev INFO={info}")
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    peak = float(L.sl1x1_dmma_peak_tflops())
+    sl.prof_enable(True)
+    launches0 = sl.launch_count()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = sl.launch_count() - launches0
+    phases = sl.prof_read()
+    sl.prof_enable(False)
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * flops_lu(n) / (ms * 1e-3) / 1e12
+
+    # accuracy of the last device solve (tester residual, computed with torch FP64)
+    X = dB.T  # (n, nrhs) view in row-major numpy sense after .cpu()
+    Ad = dA0.T
+    R = torch.from_numpy(B).to(dev) - Ad @ X
+    anorm = Ad.abs().sum(dim=1).max()
+    eps = 2.0 ** -53
+    sresid = float((R.abs().amax(dim=0) / (X.abs().amax(dim=0) * anorm * eps * n)).max())
+
+    # roofline of the dominant kernel: the FP64 trailing update (DMMA)
+    g_launch, g_ms, g_flops, g_bytes = phases["gemm"]
+    achieved = g_flops / (g_ms * 1e-3) / 1e12 if g_ms > 0 else None
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get("dgemm_dmma_trailing", {}).get("bytes_per_launch")
+        except Exception:
+            traffic = None
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if (achieved and peak) else None, "traffic": traffic,
+                "kernel": "dgemm_dmma_kernel (PDGEMM trailing update, FP64 DMMA m16n8k4)",
+                "peak_source": "measured live: register-only DMMA loop (sl1x1_dmma_peak_tflops); "
+                               "MEASURED_PEAKS.json has no FP64 figure",
+                "launches": g_launch, "avg_launch_ms": g_ms / max(1, g_launch),
+                "algorithmic_bytes_per_launch": g_bytes / max(1, g_launch)}
+    phase_summary = {k: {"launches": v[0], "ms_per_step": v[1] / args.steps,
+                         "tflops": (v[2] / (v[1] * 1e-3) / 1e12) if v[1] > 0 and v[2] > 0 else None,
+                         "gbs": (v[3] / (v[1] * 1e-3) / 1e9) if v[1] > 0 and v[3] > 0 else None}
+                     for k, v in phases.items() if v[0] > 0}
+
+    # end to end through the Fortran-ABI entry point with pinned host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        ctxt = sl.blacs_gridinit(1, 1)
+        hA0 = torch.from_numpy(A.T).pin_memory()
+        hB0 = torch.from_numpy(B.T).pin_memory()
+        hA = torch.empty_like(hA0).pin_memory()
+        hB = torch.empty_like(hB0).pin_memory()
+        ipiv = np.zeros(n + nb, dtype=np.int32)
+        desca = np.array([1, ctxt, n, n, nb, nb, 0, 0, n], dtype=np.int32)
+        descb = np.array([1, ctxt, n, nrhs, nb, nb, 0, 0, n], dtype=np.int32)
+        an = hA.numpy().T  # Fortran-ordered view of pinned memory
+        bn = hB.numpy().T
+        tt = []
+        for it in range(args.e2e_steps + 1):
+            hA.copy_(hA0)
+            hB.copy_(hB0)
+            if dist is not None:
+                dist.barrier()
+            t = time.perf_counter()
+            info = sl.pdgesv(n, nrhs, an, 1, 1, desca, ipiv, bn, 1, 1, descb)
+            dt = time.perf_counter() - t
+            if info != 0:
+                raise RuntimeError(f"pdgesv_ INFO={info}")
+            if it > 0:
+                tt.append(dt)
+        e2e_s = float(np.mean(tt))
+        if dist is not None:
+            t = torch.tensor([e2e_s], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": ws * flops_lu(n) / e2e_s / 1e12, "unit": "TFLOP/s",
+               "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs,
+               "d2h_bytes_per_step": 8 * n * n + 4 * n + 8 * n * nrhs,
+               "ms_per_step": e2e_s * 1e3, "steps": len(tt),
+               "path": "pdgesv_ (Fortran ABI) from pinned host memory"}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_solve_sample(A, B, nb)
+        cpu.pop("n", None)
+
+    # cuBLAS DGEMM yardstick (run and timed only, never on the product path)
+    yard = None
+    try:
+        x = torch.rand(4096, 4096, dtype=torch.float64, device=dev)
+        y = torch.rand(4096, 4096, dtype=torch.float64, device=dev)
+        x @ y
+        torch.cuda.synchronize(dev)
+        f0 = torch.cuda.Event(enable_timing=True); f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(); x @ y; f1.record(); torch.cuda.synchronize(dev)
+        yard = 2 * 4096 ** 3 / (f0.elapsed_time(f1) * 1e-3) / 1e12
+    except Exception:
+        pass
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": f"synthetic: A, B iid U[-0.5,0.5] (numpy PCG64 seed {args.seed}+rank)",
+            "config": {"workload": f"plain FP64 PDGESV (1x1 grid) N={n} NB={nb} NRHS={nrhs}",
+                       "n": n, "nb": nb, "nrhs": nrhs,
+                       "parallelism": "replicas" if ws > 1 else "1 GPU",
+                       "l2": "inputs (8N^2 = %.1f GiB) larger than L2; no flush" % (8 * n * n / 2**30)},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+            "accuracy": {"sresid": sresid, "threshold": 16.0},
+            "phases": phase_summary,
+            "yardstick_cublas_dgemm_tflops": yard,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,113 @@
+/*
+ * sl1x1.h -- C ABI of libsl1x1gpu.so, a GB300 (sm_103a) implementation of
+ * ScaLAPACK's dense LU path on a 1x1 BLACS grid.
+ *
+ * The Fortran-callable entry points keep the reference's names, argument
+ * order and meaning (gfortran "Add_" mangling, all arguments by reference,
+ * 32-bit INTEGER, hidden CHARACTER lengths last), so a program linked against
+ * ScaLAPACK can link against this library instead when it runs on one process
+ * with one GPU.  Every call computes on the GPU; there is no CPU fallback.
+ *
+ * Descriptor layout (DLEN_ = 9, SRC/pdgetrf.f:137-141, TOOLS/descinit.f:177-186):
+ *   DESC = { DTYPE_=1, CTXT_, M_, N_, MB_, NB_, RSRC_, CSRC_, LLD_ }
+ *
+ * INFO conventions (as the reference, plus one class for the GPU):
+ *   INFO = 0       success
+ *   INFO = -i      the i-th scalar argument is illegal
+ *   INFO = -(i*100+j)  entry j of the i-th (array) argument is illegal
+ *   INFO = K > 0   U(K,K) is exactly zero (factorization completed)
+ *   INFO <= -10000 GPU failure: -10000 - cudaError_t for a CUDA runtime error,
+ *                  -20000 - s for a device status s (1: a bounded grid barrier
+ *                  timed out, 2: a bounded flag wait timed out), -30000 when
+ *                  the problem exceeds a documented size limit of the GPU path.
+ */
+#ifndef SL1X1_H
+#define SL1X1_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- ScaLAPACK LU driver and computational routines ---------------------- */
+
+/* Replaces PDGETRF, SRC/pdgetrf.f:1-312 (signature at :1-2). */
+void pdgetrf_(const int* M, const int* N, double* A, const int* IA, const int* JA,
+              const int* DESCA, int* IPIV, int* INFO);
+
+/* Replaces PDGETRS, SRC/pdgetrs.f:1-292 (signature at :1-2). TRANS = 'N','T','C'. */
+void pdgetrs_(const char* TRANS, const int* N, const int* NRHS, const double* A, const int* IA,
+              const int* JA, const int* DESCA, const int* IPIV, double* B, const int* IB,
+              const int* JB, const int* DESCB, int* INFO, size_t TRANS_len);
+
+/* Replaces PDGESV, SRC/pdgesv.f:1-245 (signature at :1-2). */
+void pdgesv_(const int* N, const int* NRHS, double* A, const int* IA, const int* JA,
+             const int* DESCA, int* IPIV, double* B, const int* IB, const int* JB,
+             const int* DESCB, int* INFO);
+
+/* ---- TOOLS used by callers of the LU path ------------------------------- */
+
+/* Replaces DESCINIT, TOOLS/descinit.f:1-192. */
+void descinit_(int* DESC, const int* M, const int* N, const int* MB, const int* NB,
+               const int* IRSRC, const int* ICSRC, const int* ICTXT, const int* LLD, int* INFO);
+
+/* Replaces NUMROC, TOOLS/numroc.f:1-82. */
+int numroc_(const int* N, const int* NB, const int* IPROC, const int* ISRCPROC,
+            const int* NPROCS);
+
+/* ---- 1x1 BLACS shim (replaces the BLACS/SRC entry points named) ---------- */
+/* A context is valid only for a 1x1 grid; BLACS_GRIDINFO on any other
+ * context returns NPROW = NPCOL = MYROW = MYCOL = -1, which the LU routines
+ * report as INFO = -(600+CTXT_) / -(700+CTXT_) like the reference. */
+void blacs_pinfo_(int* MYPNUM, int* NPROCS);                         /* BLACS/SRC/blacs_pinfo_.c:6 */
+void blacs_get_(const int* ICTXT, const int* WHAT, int* VAL);        /* BLACS/SRC/blacs_get_.c */
+void blacs_gridinit_(int* ICTXT, const char* ORDER, const int* NPROW, const int* NPCOL,
+                     size_t ORDER_len);                              /* BLACS/SRC/blacs_init_.c:6 */
+void blacs_gridinfo_(const int* ICTXT, int* NPROW, int* NPCOL, int* MYROW,
+                     int* MYCOL);                                    /* BLACS/SRC/blacs_info_.c:6 */
+void blacs_gridexit_(const int* ICTXT);                              /* BLACS/SRC/blacs_grid_.c */
+void blacs_exit_(const int* CONTINUE);                               /* BLACS/SRC/blacs_exit_.c */
+
+/* ---- Device-resident C entry points ------------------------------------ */
+/* Same semantics as PDGETRF/PDGETRS on a whole matrix (IA=JA=1), with the
+ * matrix already in GPU memory: dA is m x n column-major with leading
+ * dimension ldda, dipiv receives min(m,n) 1-based pivot rows (LAPACK/ScaLAPACK
+ * convention for IA=1), stream is a cudaStream_t (NULL = legacy default).
+ * Returns INFO. The call returns after the work on `stream` has finished. */
+int sl1x1_dgetrf_dev(int m, int n, double* dA, long long ldda, int* dipiv, int nb, void* stream);
+int sl1x1_dgetrs_dev(char trans, int n, int nrhs, const double* dA, long long ldda,
+                     const int* dipiv, double* dB, long long lddb, void* stream);
+int sl1x1_dgesv_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, double* dB,
+                    long long lddb, int nb, void* stream);
+
+/* ---- Library control ----------------------------------------------------- */
+/* Free every device buffer the library holds (also done by blacs_exit_). */
+void sl1x1_finalize(void);
+/* Block size NB used by the device entry points when nb <= 0 (default 256). */
+void sl1x1_set_default_nb(int nb);
+/* 1 if the library found a usable sm_103 device, else 0. */
+int sl1x1_device_ok(void);
+/* Version string. */
+const char* sl1x1_version(void);
+
+/* ---- Phase timers (the GPU counterpart of SLTIMER, TOOLS/sltimer.f:47) ---- */
+/* Phases: 0 panel (PDGETF2), 1 row interchanges (PDLASWP), 2 U12 solve
+ * (PDTRSM), 3 trailing update (PDGEMM, FP64), 4 solve (PDGETRS), 5 mixed
+ * trailing update, 6 mixed panel, 7 refinement, 8 batched solver.
+ * sl1x1_prof_enable(1) clears and starts event timing of every phase launch;
+ * sl1x1_prof_read returns launches, summed device milliseconds and the
+ * algorithmic flops and bytes of a phase (0 on success). */
+void sl1x1_prof_enable(int on);
+int sl1x1_prof_read(int phase, long long* launches, double* ms, double* flops, double* bytes);
+/* Number of kernels this library has launched since it was loaded. */
+long long sl1x1_launch_count(void);
+/* FP64 tensor (DMMA) throughput of this device from a register-only loop,
+ * TFLOP/s: the roofline denominator of the FP64 trailing update. */
+double sl1x1_dmma_peak_tflops(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SL1X1_H */

@@ -1,0 +1,215 @@
+"""scalapack_gb300 -- GB300 (sm_103a) implementation of ScaLAPACK's dense LU
+path on a 1x1 BLACS grid (PDGETRF / PDGETRS / PDGESV).
+
+This module is the Python host-side mirror of the reference interface: the
+functions below take the same arguments as the Fortran routines (M, N, A, IA,
+JA, DESCA, IPIV, INFO ...) with numpy arrays in Fortran order standing in for
+the Fortran arrays, and call the C ABI of ``libsl1x1gpu.so`` (declared in
+``include/sl1x1.h``) through ctypes. There is no CPU implementation here: if the
+CUDA library is missing the import of :func:`lib` raises, and without a GPU the
+routines return INFO <= -10000.
+
+Index and pivot conventions are the reference's: IA/JA/IB/JB are 1-based,
+IPIV holds 1-based global row numbers (SRC/pdgetrf.f:118-121).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _build
+
+__all__ = [
+    "lib", "descinit", "numroc", "blacs_gridinit", "blacs_gridinfo", "blacs_gridexit",
+    "blacs_exit", "pdgetrf", "pdgetrs", "pdgesv", "dgetrf_dev", "dgetrs_dev", "dgesv_dev",
+    "DLEN", "CTXT_", "M_", "N_", "MB_", "NB_", "LLD_",
+]
+
+DLEN = 9
+DTYPE_, CTXT_, M_, N_, MB_, NB_, RSRC_, CSRC_, LLD_ = range(9)
+
+_lib = None
+
+
+def lib(build_if_missing: bool = False):
+    """Load libsl1x1gpu.so (raises if it is not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.lib_path()
+    if not os.path.exists(path):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise RuntimeError(
+                f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
+            )
+    L = C.CDLL(path)
+    ip = C.POINTER(C.c_int)
+    vp = C.c_void_p
+    L.pdgetrf_.argtypes = [ip, ip, vp, ip, ip, ip, vp, ip]
+    L.pdgetrf_.restype = None
+    L.pdgetrs_.argtypes = [C.c_char_p, ip, ip, vp, ip, ip, ip, vp, vp, ip, ip, ip, ip, C.c_size_t]
+    L.pdgetrs_.restype = None
+    L.pdgesv_.argtypes = [ip, ip, vp, ip, ip, ip, vp, vp, ip, ip, ip, ip]
+    L.pdgesv_.restype = None
+    L.descinit_.argtypes = [vp, ip, ip, ip, ip, ip, ip, ip, ip, ip]
+    L.descinit_.restype = None
+    L.numroc_.argtypes = [ip, ip, ip, ip, ip]
+    L.numroc_.restype = C.c_int
+    L.blacs_pinfo_.argtypes = [ip, ip]
+    L.blacs_get_.argtypes = [ip, ip, ip]
+    L.blacs_gridinit_.argtypes = [ip, C.c_char_p, ip, ip, C.c_size_t]
+    L.blacs_gridinfo_.argtypes = [ip, ip, ip, ip, ip]
+    L.blacs_gridexit_.argtypes = [ip]
+    L.blacs_exit_.argtypes = [ip]
+    L.sl1x1_dgetrf_dev.argtypes = [C.c_int, C.c_int, vp, C.c_longlong, vp, C.c_int, vp]
+    L.sl1x1_dgetrf_dev.restype = C.c_int
+    L.sl1x1_dgetrs_dev.argtypes = [C.c_char, C.c_int, C.c_int, vp, C.c_longlong, vp, vp,
+                                   C.c_longlong, vp]
+    L.sl1x1_dgetrs_dev.restype = C.c_int
+    L.sl1x1_dgesv_dev.argtypes = [C.c_int, C.c_int, vp, C.c_longlong, vp, vp, C.c_longlong,
+                                  C.c_int, vp]
+    L.sl1x1_dgesv_dev.restype = C.c_int
+    L.sl1x1_finalize.argtypes = []
+    L.sl1x1_set_default_nb.argtypes = [C.c_int]
+    L.sl1x1_device_ok.restype = C.c_int
+    L.sl1x1_version.restype = C.c_char_p
+    L.sl1x1_prof_enable.argtypes = [C.c_int]
+    L.sl1x1_prof_read.argtypes = [C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.sl1x1_prof_read.restype = C.c_int
+    L.sl1x1_launch_count.restype = C.c_longlong
+    L.sl1x1_dmma_peak_tflops.restype = C.c_double
+    _lib = L
+    return L
+
+
+def _i(v):
+    return C.byref(C.c_int(int(v)))
+
+
+def _arr(a, dtype):
+    if a.dtype != dtype or not a.flags.f_contiguous:
+        raise TypeError(f"expected a Fortran-ordered {dtype} array")
+    return a.ctypes.data_as(C.c_void_p)
+
+
+# ---------------------------------------------------------------- BLACS shim
+def blacs_gridinit(nprow: int = 1, npcol: int = 1, order: str = "R") -> int:
+    ctxt = C.c_int(0)
+    lib().blacs_gridinit_(C.byref(ctxt), order.encode(), _i(nprow), _i(npcol), 1)
+    return ctxt.value
+
+
+def blacs_gridinfo(ictxt: int):
+    v = [C.c_int() for _ in range(4)]
+    lib().blacs_gridinfo_(_i(ictxt), *[C.byref(x) for x in v])
+    return tuple(x.value for x in v)
+
+
+def blacs_gridexit(ictxt: int):
+    lib().blacs_gridexit_(_i(ictxt))
+
+
+def blacs_exit(cont: int = 0):
+    lib().blacs_exit_(_i(cont))
+
+
+def numroc(n, nb, iproc, isrcproc, nprocs) -> int:
+    return lib().numroc_(_i(n), _i(nb), _i(iproc), _i(isrcproc), _i(nprocs))
+
+
+def descinit(m, n, mb, nb, irsrc, icsrc, ictxt, lld):
+    """DESCINIT: returns (desc int32[9], info)."""
+    desc = np.zeros(DLEN, dtype=np.int32)
+    info = C.c_int()
+    lib().descinit_(desc.ctypes.data_as(C.c_void_p), _i(m), _i(n), _i(mb), _i(nb), _i(irsrc),
+                    _i(icsrc), _i(ictxt), _i(lld), C.byref(info))
+    return desc, info.value
+
+
+def _desc(desc):
+    d = np.ascontiguousarray(desc, dtype=np.int32)
+    return d, d.ctypes.data_as(C.POINTER(C.c_int))
+
+
+# ---------------------------------------------------------------- LU routines
+def pdgetrf(m, n, a, ia, ja, desca, ipiv) -> int:
+    """PDGETRF(M, N, A, IA, JA, DESCA, IPIV, INFO): returns INFO; A and IPIV in place."""
+    d, dp = _desc(desca)
+    info = C.c_int()
+    lib().pdgetrf_(_i(m), _i(n), _arr(a, np.float64), _i(ia), _i(ja), dp,
+                   ipiv.ctypes.data_as(C.c_void_p), C.byref(info))
+    return info.value
+
+
+def pdgetrs(trans, n, nrhs, a, ia, ja, desca, ipiv, b, ib, jb, descb) -> int:
+    """PDGETRS(TRANS, N, NRHS, A, IA, JA, DESCA, IPIV, B, IB, JB, DESCB, INFO)."""
+    da, dap = _desc(desca)
+    db, dbp = _desc(descb)
+    info = C.c_int()
+    lib().pdgetrs_(trans.encode()[:1], _i(n), _i(nrhs), _arr(a, np.float64), _i(ia), _i(ja), dap,
+                   ipiv.ctypes.data_as(C.c_void_p), _arr(b, np.float64), _i(ib), _i(jb), dbp,
+                   C.byref(info), 1)
+    return info.value
+
+
+def pdgesv(n, nrhs, a, ia, ja, desca, ipiv, b, ib, jb, descb) -> int:
+    """PDGESV(N, NRHS, A, IA, JA, DESCA, IPIV, B, IB, JB, DESCB, INFO)."""
+    da, dap = _desc(desca)
+    db, dbp = _desc(descb)
+    info = C.c_int()
+    lib().pdgesv_(_i(n), _i(nrhs), _arr(a, np.float64), _i(ia), _i(ja), dap,
+                  ipiv.ctypes.data_as(C.c_void_p), _arr(b, np.float64), _i(ib), _i(jb), dbp,
+                  C.byref(info))
+    return info.value
+
+
+# ------------------------------------------------------------ phase timers
+PHASES = ["panel", "laswp", "trsm", "gemm", "solve", "mixed_gemm", "mixed_panel", "refine",
+          "batched"]
+
+
+def prof_enable(on: bool = True):
+    lib().sl1x1_prof_enable(1 if on else 0)
+
+
+def prof_read():
+    """{phase: (launches, device ms, algorithmic flops, algorithmic bytes)}."""
+    out = {}
+    for i, name in enumerate(PHASES):
+        n, ms, fl, by = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
+        lib().sl1x1_prof_read(i, C.byref(n), C.byref(ms), C.byref(fl), C.byref(by))
+        out[name] = (n.value, ms.value, fl.value, by.value)
+    return out
+
+
+def launch_count() -> int:
+    return int(lib().sl1x1_launch_count())
+
+
+# ------------------------------------------------------- device entry points
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    return C.c_void_p(int(stream))
+
+
+def dgetrf_dev(m, n, a_ptr, ldda, ipiv_ptr, nb=0, stream=None) -> int:
+    """sl1x1_dgetrf_dev on device pointers (e.g. torch ``.data_ptr()``)."""
+    return lib().sl1x1_dgetrf_dev(m, n, C.c_void_p(a_ptr), ldda, C.c_void_p(ipiv_ptr), nb,
+                                  _stream_ptr(stream))
+
+
+def dgetrs_dev(trans, n, nrhs, a_ptr, ldda, ipiv_ptr, b_ptr, lddb, stream=None) -> int:
+    return lib().sl1x1_dgetrs_dev(trans.encode()[:1], n, nrhs, C.c_void_p(a_ptr), ldda,
+                                  C.c_void_p(ipiv_ptr), C.c_void_p(b_ptr), lddb,
+                                  _stream_ptr(stream))
+
+
+def dgesv_dev(n, nrhs, a_ptr, ldda, ipiv_ptr, b_ptr, lddb, nb=0, stream=None) -> int:
+    return lib().sl1x1_dgesv_dev(n, nrhs, C.c_void_p(a_ptr), ldda, C.c_void_p(ipiv_ptr),
+                                 C.c_void_p(b_ptr), lddb, nb, _stream_ptr(stream))

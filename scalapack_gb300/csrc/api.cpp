@@ -1,0 +1,588 @@
+// Host layer of libsl1x1gpu.so: the reference-facing C ABI.
+//
+//  * argument validation with the reference's INFO codes (TOOLS/chk1mat.f,
+//    SRC/pdgetrf.f:170-197, SRC/pdgetrs.f:186-236, SRC/pdgesv.f:181-221) and
+//    PXERBLA-format messages (PBLAS/SRC/PTZBLAS/pxerbla.f:57-58);
+//  * Fortran-ABI PDGETRF / PDGETRS / PDGESV that stage sub(A), sub(B) and IPIV
+//    between host memory and library-owned device buffers;
+//  * a 1x1 BLACS shim, DESCINIT and NUMROC so that callers link without MPI;
+//  * device-pointer entry points for callers whose data already lives in HBM.
+// No routine falls back to the CPU: without a usable GPU every call returns an
+// INFO <= -10000.
+#include <cuda_runtime.h>
+#include <climits>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/sl1x1.h"
+#include "sl_internal.h"
+
+namespace {
+
+// Descriptor entries (0-based C indices of the Fortran DESC(1..9)).
+enum { DTYPE_ = 0, CTXT_ = 1, M_ = 2, N_ = 3, MB_ = 4, NB_ = 5, RSRC_ = 6, CSRC_ = 7, LLD_ = 8 };
+// Fortran positions of the descriptor entries (DESC(k) has k = index + 1).
+enum { FDTYPE = 1, FCTXT = 2, FM = 3, FN = 4, FMB = 5, FNB = 6, FRSRC = 7, FCSRC = 8, FLLD = 9 };
+
+std::mutex g_mu;
+
+// ---------------------------------------------------------------- BLACS shim
+struct Grid {
+  bool live = false;
+  int nprow = -1, npcol = -1;
+};
+std::vector<Grid> g_grids;
+
+void gridinfo(int ictxt, int* nprow, int* npcol, int* myrow, int* mycol) {
+  if (ictxt >= 0 && ictxt < (int)g_grids.size() && g_grids[ictxt].live &&
+      g_grids[ictxt].nprow == 1 && g_grids[ictxt].npcol == 1) {
+    *nprow = 1; *npcol = 1; *myrow = 0; *mycol = 0;
+  } else {
+    *nprow = -1; *npcol = -1; *myrow = -1; *mycol = -1;
+  }
+}
+
+int numroc(int n, int nb, int iproc, int isrcproc, int nprocs) {
+  // TOOLS/numroc.f:53-76
+  int mydist = (nprocs + iproc - isrcproc) % nprocs;
+  int nblocks = n / nb;
+  int r = (nblocks / nprocs) * nb;
+  int extra = nblocks % nprocs;
+  if (mydist < extra) r += nb;
+  else if (mydist == extra) r += n % nb;
+  return r;
+}
+
+void pxerbla(int ictxt, const char* name, int info) {
+  int nprow, npcol, myrow, mycol;
+  gridinfo(ictxt, &nprow, &npcol, &myrow, &mycol);
+  // FORMAT( '{', I5, ',', I5, '}:  On entry to ', A, ' parameter number ', I4, ' had an illegal value' )
+  std::printf("{%5d,%5d}:  On entry to %s parameter number %4d had an illegal value\n", myrow,
+              mycol, name, info);
+  std::fflush(stdout);
+}
+
+// CHK1MAT (TOOLS/chk1mat.f): checks one distributed-matrix argument and folds
+// the result into INFO with the reference's encoding (smallest position wins).
+void chk1mat(int ma, int mapos0, int na, int napos0, int ia, int ja, const int* desca,
+             int descapos0, int* info) {
+  const int DESCMULT = 100, BIGNUM = DESCMULT * DESCMULT;
+  if (*info >= 0) *info = BIGNUM;
+  else if (*info < -DESCMULT) *info = -*info;
+  else *info = -*info * DESCMULT;
+  const int mapos = mapos0 * DESCMULT, napos = napos0 * DESCMULT;
+  const int iapos = (descapos0 - 2) * DESCMULT, japos = (descapos0 - 1) * DESCMULT;
+  const int descapos = descapos0 * DESCMULT;
+  int nprow, npcol, myrow, mycol;
+  gridinfo(desca[CTXT_], &nprow, &npcol, &myrow, &mycol);
+  auto mn = [&](int v) { if (v < *info) *info = v; };
+  if (desca[DTYPE_] != 1) mn(descapos + FDTYPE);
+  else if (ma < 0) mn(mapos);
+  else if (na < 0) mn(napos);
+  else if (ia < 1) mn(iapos);
+  else if (ja < 1) mn(japos);
+  else if (desca[MB_] < 1) mn(descapos + FMB);
+  else if (desca[NB_] < 1) mn(descapos + FNB);
+  else if (desca[RSRC_] < 0 || desca[RSRC_] >= nprow) mn(descapos + FRSRC);
+  else if (desca[CSRC_] < 0 || desca[CSRC_] >= npcol) mn(descapos + FCSRC);
+  else if (desca[LLD_] < 1) mn(descapos + FLLD);
+  else if (desca[LLD_] < numroc(desca[M_], desca[MB_], myrow, desca[RSRC_], nprow)) {
+    if (numroc(desca[N_], desca[NB_], mycol, desca[CSRC_], npcol) > 0) mn(descapos + FLLD);
+  }
+  if (ma == 0 || na == 0) {
+    if (desca[M_] < 0) mn(descapos + FM);
+    if (desca[N_] < 0) mn(descapos + FN);
+  } else {
+    if (desca[M_] < 1) mn(descapos + FM);
+    else if (desca[N_] < 1) mn(descapos + FN);
+    else {
+      if (ia > desca[M_]) mn(iapos);
+      else if (ja > desca[N_]) mn(japos);
+      else {
+        if (ia + ma - 1 > desca[M_]) mn(mapos);
+        if (ja + na - 1 > desca[N_]) mn(napos);
+      }
+    }
+  }
+  if (*info == BIGNUM) *info = 0;
+  else if (*info % DESCMULT == 0) *info = -*info / DESCMULT;
+  else *info = -*info;
+}
+
+// ------------------------------------------------------------- device state
+struct DevState {
+  bool init = false;
+  bool ok = false;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  double* dA = nullptr; size_t capA = 0;
+  double* dB = nullptr; size_t capB = 0;
+  int* dipiv = nullptr; size_t capP = 0;
+  int* dsmall = nullptr;      // bar[2], status, info_col
+  double* dcand = nullptr;
+  int* dperm = nullptr; size_t capPerm = 0;
+  double* dbswap = nullptr; size_t capBs = 0;
+};
+DevState g_dev;
+int g_default_nb = 256;
+
+int cuda_info(cudaError_t e) { return -10000 - (int)e; }
+
+bool ensure_device() {
+  if (g_dev.init) return g_dev.ok;
+  g_dev.init = true;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) return false;
+  if (cudaGetDevice(&g_dev.device) != cudaSuccess) return false;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, g_dev.device) != cudaSuccess) return false;
+  if (prop.major != 10 || prop.minor != 3) {
+    std::fprintf(stderr, "sl1x1: device %d is sm_%d%d; this library is built for sm_103a only\n",
+                 g_dev.device, prop.major, prop.minor);
+    return false;
+  }
+  if (cudaStreamCreateWithFlags(&g_dev.stream, cudaStreamNonBlocking) != cudaSuccess) return false;
+  if (cudaMalloc(&g_dev.dsmall, 16 * sizeof(int)) != cudaSuccess) return false;
+  if (cudaMalloc(&g_dev.dcand, sl::panel_cand_doubles() * sizeof(double)) != cudaSuccess) return false;
+  g_dev.ok = true;
+  return true;
+}
+
+template <class T>
+cudaError_t grow(T** p, size_t* cap, size_t need) {
+  if (need <= *cap && *p) return cudaSuccess;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  size_t n = need < 1 ? 1 : need;
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e == cudaSuccess) *cap = n;
+  return e;
+}
+
+void release_all() {
+  if (!g_dev.ok) return;
+  cudaFree(g_dev.dA); cudaFree(g_dev.dB); cudaFree(g_dev.dipiv); cudaFree(g_dev.dsmall);
+  cudaFree(g_dev.dcand); cudaFree(g_dev.dperm); cudaFree(g_dev.dbswap);
+  if (g_dev.stream) cudaStreamDestroy(g_dev.stream);
+  g_dev = DevState();
+}
+
+sl::LuWork make_work() {
+  sl::LuWork w;
+  w.bar = g_dev.dsmall;
+  w.status = g_dev.dsmall + 2;
+  w.info_col = g_dev.dsmall + 3;
+  w.cand = g_dev.dcand;
+  w.perm = g_dev.dperm;
+  w.bswap = g_dev.dbswap;
+  w.perm_len = g_dev.capPerm;
+  w.bswap_len = g_dev.capBs;
+  return w;
+}
+
+cudaError_t ensure_solve_ws(int n, int nrhs) {
+  cudaError_t e = grow(&g_dev.dperm, &g_dev.capPerm, (size_t)n);
+  if (e != cudaSuccess) return e;
+  return grow(&g_dev.dbswap, &g_dev.capBs, (size_t)n * (size_t)nrhs);
+}
+
+// Reads the device status word and the first zero-pivot column after a
+// factorization; returns INFO (>0 singular, <=-20000 device status).
+int read_factor_info(cudaStream_t s, int mn, int* out_info) {
+  int h[2] = {0, 0};
+  cudaError_t e = cudaMemcpyAsync(h, g_dev.dsmall + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) { *out_info = cuda_info(e); return *out_info; }
+  if (h[0] != 0) { *out_info = -20000 - h[0]; return *out_info; }
+  *out_info = (h[1] >= 0 && h[1] < mn) ? h[1] + 1 : 0;
+  return *out_info;
+}
+
+long long round_ld(long long m) {
+  long long ld = m < 1 ? 1 : m;
+  return (ld + 31) / 32 * 32;
+}
+
+// ---- shared implementation of the host-ABI entry points ---------------------
+int factor_host(int m, int n, double* A, int ia, int ja, const int* desca, int* ipiv,
+                cudaStream_t s, long long* ldda_out) {
+  const long long lld = desca[LLD_];
+  const long long ldda = round_ld(m);
+  const int mn = m < n ? m : n;
+  cudaError_t e = grow(&g_dev.dA, &g_dev.capA, (size_t)ldda * (size_t)n);
+  if (e == cudaSuccess) e = grow(&g_dev.dipiv, &g_dev.capP, (size_t)(mn > 0 ? mn : 1));
+  if (e != cudaSuccess) return cuda_info(e);
+  const double* src = A + (ia - 1) + (long long)(ja - 1) * lld;
+  e = cudaMemcpy2DAsync(g_dev.dA, ldda * sizeof(double), src, lld * sizeof(double),
+                        (size_t)m * sizeof(double), n, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_info(e);
+  sl::LuWork w = make_work();
+  e = sl::dgetrf_device(m, n, g_dev.dA, ldda, g_dev.dipiv, desca[NB_], w, s);
+  if (e == cudaErrorInvalidValue) return -30000;
+  if (e != cudaSuccess) return cuda_info(e);
+  int info = 0;
+  read_factor_info(s, mn, &info);
+  if (info <= -10000) return info;
+  // copy the factors and pivots back: IPIV(IA+k) = IA + p (global 1-based row)
+  e = cudaMemcpy2DAsync(A + (ia - 1) + (long long)(ja - 1) * lld, lld * sizeof(double), g_dev.dA,
+                        ldda * sizeof(double), (size_t)m * sizeof(double), n,
+                        cudaMemcpyDeviceToHost, s);
+  std::vector<int> hp((size_t)(mn > 0 ? mn : 1));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(hp.data(), g_dev.dipiv, (size_t)mn * sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_info(e);
+  for (int k = 0; k < mn; ++k) ipiv[ia - 1 + k] = ia + hp[k];
+  if (ldda_out) *ldda_out = ldda;
+  return info;
+}
+
+int validate_getrf(const char* name, int m, int n, int ia, int ja, const int* desca) {
+  int nprow, npcol, myrow, mycol;
+  gridinfo(desca[CTXT_], &nprow, &npcol, &myrow, &mycol);
+  int info = 0;
+  if (nprow == -1) {
+    info = -(600 + FCTXT);
+  } else {
+    chk1mat(m, 1, n, 2, ia, ja, desca, 6, &info);
+    if (info == 0) {
+      int iroff = (ia - 1) % desca[MB_], icoff = (ja - 1) % desca[NB_];
+      if (iroff != 0) info = -4;
+      else if (icoff != 0) info = -5;
+      else if (desca[MB_] != desca[NB_]) info = -(600 + FNB);
+    }
+  }
+  if (info != 0) pxerbla(desca[CTXT_], name, -info);
+  return info;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---------------------------------------------------------------- PDGETRF
+void pdgetrf_(const int* M, const int* N, double* A, const int* IA, const int* JA,
+              const int* DESCA, int* IPIV, int* INFO) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  *INFO = validate_getrf("PDGETRF", *M, *N, *IA, *JA, DESCA);
+  if (*INFO != 0) return;
+  // Quick return (SRC/pdgetrf.f:201-206): tests the global M_A.
+  if (DESCA[M_] == 1) { IPIV[0] = 1; return; }
+  if (*M == 0 || *N == 0) return;
+  if (!ensure_device()) { *INFO = cuda_info(cudaErrorNoDevice); return; }
+  *INFO = factor_host(*M, *N, A, *IA, *JA, DESCA, IPIV, g_dev.stream, nullptr);
+}
+
+// ---------------------------------------------------------------- PDGETRS
+static int validate_getrs(char trans, int n, int nrhs, int ia, int ja, const int* desca, int ib,
+                          int jb, const int* descb) {
+  int nprow, npcol, myrow, mycol;
+  gridinfo(desca[CTXT_], &nprow, &npcol, &myrow, &mycol);
+  int info = 0;
+  if (nprow == -1) {
+    info = -(700 + FCTXT);
+  } else {
+    bool notran = (trans == 'N' || trans == 'n');
+    chk1mat(n, 2, n, 2, ia, ja, desca, 7, &info);
+    chk1mat(n, 2, nrhs, 3, ib, jb, descb, 12, &info);
+    if (info == 0) {
+      int iroffa = (ia - 1) % desca[MB_], icoffa = (ja - 1) % desca[NB_];
+      int iroffb = (ib - 1) % descb[MB_];
+      // INDXG2P is 0 for both on a 1x1 grid, so IBROW == IAROW.
+      if (!notran && !(trans == 'T' || trans == 't') && !(trans == 'C' || trans == 'c')) info = -1;
+      else if (iroffa != 0) info = -5;
+      else if (icoffa != 0) info = -6;
+      else if (desca[MB_] != desca[NB_]) info = -(700 + FNB);
+      else if (iroffb != 0) info = -10;
+      else if (descb[MB_] != desca[NB_]) info = -(1200 + FNB);
+      else if (desca[CTXT_] != descb[CTXT_]) info = -(1200 + FCTXT);
+    }
+  }
+  if (info != 0) pxerbla(desca[CTXT_], "PDGETRS", -info);
+  return info;
+}
+
+static int solve_host(char trans, int n, int nrhs, long long ldda, double* B, int ib, int jb,
+                      const int* descb, cudaStream_t s) {
+  const long long lldb = descb[LLD_];
+  const long long lddb = round_ld(n);
+  cudaError_t e = grow(&g_dev.dB, &g_dev.capB, (size_t)lddb * (size_t)nrhs);
+  if (e == cudaSuccess) e = ensure_solve_ws(n, nrhs);
+  if (e != cudaSuccess) return cuda_info(e);
+  double* hb = B + (ib - 1) + (long long)(jb - 1) * lldb;
+  e = cudaMemcpy2DAsync(g_dev.dB, lddb * sizeof(double), hb, lldb * sizeof(double),
+                        (size_t)n * sizeof(double), nrhs, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_info(e);
+  sl::LuWork w = make_work();
+  e = sl::dgetrs_device(trans, n, nrhs, g_dev.dA, ldda, g_dev.dipiv, g_dev.dB, lddb, w, s);
+  if (e != cudaSuccess) return cuda_info(e);
+  e = cudaMemcpy2DAsync(hb, lldb * sizeof(double), g_dev.dB, lddb * sizeof(double),
+                        (size_t)n * sizeof(double), nrhs, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_info(e);
+  return 0;
+}
+
+void pdgetrs_(const char* TRANS, const int* N, const int* NRHS, const double* A, const int* IA,
+              const int* JA, const int* DESCA, const int* IPIV, double* B, const int* IB,
+              const int* JB, const int* DESCB, int* INFO, size_t TRANS_len) {
+  (void)TRANS_len;
+  std::lock_guard<std::mutex> lk(g_mu);
+  const char trans = TRANS[0];
+  *INFO = validate_getrs(trans, *N, *NRHS, *IA, *JA, DESCA, *IB, *JB, DESCB);
+  if (*INFO != 0) return;
+  if (*N == 0 || *NRHS == 0) return;
+  if (!ensure_device()) { *INFO = cuda_info(cudaErrorNoDevice); return; }
+  const int n = *N, ia = *IA, ja = *JA;
+  const long long lld = DESCA[LLD_];
+  const long long ldda = round_ld(n);
+  cudaStream_t s = g_dev.stream;
+  cudaError_t e = grow(&g_dev.dA, &g_dev.capA, (size_t)ldda * (size_t)n);
+  if (e == cudaSuccess) e = grow(&g_dev.dipiv, &g_dev.capP, (size_t)n);
+  if (e != cudaSuccess) { *INFO = cuda_info(e); return; }
+  e = cudaMemcpy2DAsync(g_dev.dA, ldda * sizeof(double), A + (ia - 1) + (long long)(ja - 1) * lld,
+                        lld * sizeof(double), (size_t)n * sizeof(double), n,
+                        cudaMemcpyHostToDevice, s);
+  // IPIV holds global 1-based rows; the device path wants rows relative to IA.
+  std::vector<int> hp((size_t)n);
+  for (int k = 0; k < n; ++k) hp[k] = IPIV[ia - 1 + k] - ia;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(g_dev.dipiv, hp.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) { *INFO = cuda_info(e); return; }
+  *INFO = solve_host(trans, n, *NRHS, ldda, B, *IB, *JB, DESCB, s);
+}
+
+// ---------------------------------------------------------------- PDGESV
+void pdgesv_(const int* N, const int* NRHS, double* A, const int* IA, const int* JA,
+             const int* DESCA, int* IPIV, double* B, const int* IB, const int* JB,
+             const int* DESCB, int* INFO) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  int nprow, npcol, myrow, mycol;
+  gridinfo(DESCA[CTXT_], &nprow, &npcol, &myrow, &mycol);
+  int info = 0;
+  const int n = *N, nrhs = *NRHS, ia = *IA, ja = *JA, ib = *IB, jb = *JB;
+  if (nprow == -1) {
+    info = -(600 + FCTXT);
+  } else {
+    chk1mat(n, 1, n, 1, ia, ja, DESCA, 6, &info);
+    chk1mat(n, 1, nrhs, 2, ib, jb, DESCB, 11, &info);
+    if (info == 0) {
+      int iroffa = (ia - 1) % DESCA[MB_], icoffa = (ja - 1) % DESCA[NB_];
+      int iroffb = (ib - 1) % DESCB[MB_];
+      if (iroffa != 0) info = -4;
+      else if (icoffa != 0) info = -5;
+      else if (DESCA[MB_] != DESCA[NB_]) info = -(600 + FNB);
+      else if (icoffa != iroffb) info = -9;
+      else if (DESCB[MB_] != DESCA[NB_]) info = -(1100 + FNB);
+      else if (DESCA[CTXT_] != DESCB[CTXT_]) info = -(1100 + FCTXT);
+    }
+  }
+  if (info != 0) {
+    pxerbla(DESCA[CTXT_], "PDGESV", -info);
+    *INFO = info;
+    return;
+  }
+  // PDGETRF (SRC/pdgesv.f:229) -- its own validation cannot fail here.
+  *INFO = 0;
+  if (DESCA[M_] == 1) IPIV[0] = 1;
+  if (n == 0) return;
+  if (!ensure_device()) { *INFO = cuda_info(cudaErrorNoDevice); return; }
+  long long ldda = round_ld(n);
+  if (DESCA[M_] == 1) {
+    // 1x1 global matrix: PDGETRF returns at once with IPIV(1) = 1 and INFO = 0,
+    // so PDGETRS runs on the unfactored 1x1 A.
+    cudaStream_t s = g_dev.stream;
+    cudaError_t e = grow(&g_dev.dA, &g_dev.capA, (size_t)ldda);
+    if (e == cudaSuccess) e = grow(&g_dev.dipiv, &g_dev.capP, 1);
+    int zero = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(g_dev.dA, A + (ia - 1) + (long long)(ja - 1) * DESCA[LLD_], sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(g_dev.dipiv, &zero, sizeof(int), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { *INFO = cuda_info(e); return; }
+  } else {
+    *INFO = factor_host(n, n, A, ia, ja, DESCA, IPIV, g_dev.stream, &ldda);
+  }
+  if (*INFO != 0) return;  // singular (or GPU failure): the solve is skipped (pdgesv.f:231)
+  if (nrhs == 0) return;
+  *INFO = solve_host('N', n, nrhs, ldda, B, ib, jb, DESCB, g_dev.stream);
+}
+
+// ---------------------------------------------------------------- TOOLS
+int numroc_(const int* N, const int* NB, const int* IPROC, const int* ISRCPROC, const int* NPROCS) {
+  return numroc(*N, *NB, *IPROC, *ISRCPROC, *NPROCS);
+}
+
+void descinit_(int* DESC, const int* M, const int* N, const int* MB, const int* NB,
+               const int* IRSRC, const int* ICSRC, const int* ICTXT, const int* LLD, int* INFO) {
+  // TOOLS/descinit.f:148-192
+  int nprow, npcol, myrow, mycol;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    gridinfo(*ICTXT, &nprow, &npcol, &myrow, &mycol);
+  }
+  int info = 0;
+  if (*M < 0) info = -2;
+  else if (*N < 0) info = -3;
+  else if (*MB < 1) info = -4;
+  else if (*NB < 1) info = -5;
+  else if (*IRSRC < 0 || *IRSRC >= nprow) info = -6;
+  else if (*ICSRC < 0 || *ICSRC >= npcol) info = -7;
+  else if (nprow == -1) info = -8;
+  else {
+    int lr = numroc(*M, *MB, myrow, *IRSRC, nprow);
+    if (*LLD < (lr > 1 ? lr : 1)) info = -9;
+  }
+  if (info != 0) pxerbla(*ICTXT, "DESCINIT", -info);
+  auto mx = [](int a, int b) { return a > b ? a : b; };
+  auto mnf = [](int a, int b) { return a < b ? a : b; };
+  DESC[DTYPE_] = 1;
+  DESC[M_] = mx(0, *M);
+  DESC[N_] = mx(0, *N);
+  DESC[MB_] = mx(1, *MB);
+  DESC[NB_] = mx(1, *NB);
+  DESC[RSRC_] = mx(0, mnf(*IRSRC, nprow - 1));
+  DESC[CSRC_] = mx(0, mnf(*ICSRC, npcol - 1));
+  DESC[CTXT_] = *ICTXT;
+  int lr = (nprow > 0) ? numroc(DESC[M_], DESC[MB_], myrow, DESC[RSRC_], nprow) : 1;
+  DESC[LLD_] = mx(*LLD, mx(1, lr));
+  *INFO = info;
+}
+
+// ---------------------------------------------------------------- BLACS shim
+void blacs_pinfo_(int* MYPNUM, int* NPROCS) { *MYPNUM = 0; *NPROCS = 1; }
+
+void blacs_get_(const int* ICTXT, const int* WHAT, int* VAL) {
+  (void)ICTXT;
+  // WHAT = 0 (SGET_SYSCONTXT) and 10 (SGET_BLACSCONTXT) return the system
+  // context handle, which is 0 for the single process.
+  if (*WHAT == 0 || *WHAT == 10) *VAL = 0;
+  else *VAL = 0;
+}
+
+void blacs_gridinit_(int* ICTXT, const char* ORDER, const int* NPROW, const int* NPCOL,
+                     size_t ORDER_len) {
+  (void)ORDER; (void)ORDER_len;
+  std::lock_guard<std::mutex> lk(g_mu);
+  Grid g;
+  g.live = true;
+  g.nprow = *NPROW;
+  g.npcol = *NPCOL;
+  g_grids.push_back(g);
+  *ICTXT = (int)g_grids.size() - 1;
+}
+
+void blacs_gridinfo_(const int* ICTXT, int* NPROW, int* NPCOL, int* MYROW, int* MYCOL) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  gridinfo(*ICTXT, NPROW, NPCOL, MYROW, MYCOL);
+}
+
+void blacs_gridexit_(const int* ICTXT) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (*ICTXT >= 0 && *ICTXT < (int)g_grids.size()) g_grids[*ICTXT].live = false;
+}
+
+void blacs_exit_(const int* CONTINUE) {
+  (void)CONTINUE;
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto& g : g_grids) g.live = false;
+  release_all();
+}
+
+// ------------------------------------------------------- device entry points
+int sl1x1_dgetrf_dev(int m, int n, double* dA, long long ldda, int* dipiv, int nb, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (ldda < (m > 1 ? m : 1)) return -4;
+  if (m == 0 || n == 0) return 0;
+  if (!ensure_device()) return cuda_info(cudaErrorNoDevice);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (nb <= 0) nb = g_default_nb;
+  sl::LuWork w = make_work();
+  cudaError_t e = sl::dgetrf_device(m, n, dA, ldda, dipiv, nb, w, s);
+  if (e == cudaErrorInvalidValue) return -30000;
+  if (e != cudaSuccess) return cuda_info(e);
+  int mn = m < n ? m : n;
+  int info = 0;
+  read_factor_info(s, mn, &info);
+  if (info <= -10000) return info;
+  e = sl::ipiv_shift(dipiv, dipiv, mn, 1, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_info(e);
+  return info;
+}
+
+int sl1x1_dgetrs_dev(char trans, int n, int nrhs, const double* dA, long long ldda,
+                     const int* dipiv, double* dB, long long lddb, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  bool ok_t = trans == 'N' || trans == 'n' || trans == 'T' || trans == 't' || trans == 'C' ||
+              trans == 'c';
+  if (!ok_t) return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (ldda < (n > 1 ? n : 1)) return -5;
+  if (lddb < (n > 1 ? n : 1)) return -8;
+  if (n == 0 || nrhs == 0) return 0;
+  if (!ensure_device()) return cuda_info(cudaErrorNoDevice);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = grow(&g_dev.dipiv, &g_dev.capP, (size_t)n);
+  if (e == cudaSuccess) e = ensure_solve_ws(n, nrhs);
+  if (e != cudaSuccess) return cuda_info(e);
+  e = sl::ipiv_shift(dipiv, g_dev.dipiv, n, -1, s);
+  if (e != cudaSuccess) return cuda_info(e);
+  sl::LuWork w = make_work();
+  e = sl::dgetrs_device(trans, n, nrhs, dA, ldda, g_dev.dipiv, dB, lddb, w, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_info(e);
+  return 0;
+}
+
+int sl1x1_dgesv_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, double* dB,
+                    long long lddb, int nb, void* stream) {
+  int info = sl1x1_dgetrf_dev(n, n, dA, ldda, dipiv, nb, stream);
+  if (info != 0) return info;
+  return sl1x1_dgetrs_dev('N', n, nrhs, dA, ldda, dipiv, dB, lddb, stream);
+}
+
+void sl1x1_finalize(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  release_all();
+}
+
+void sl1x1_set_default_nb(int nb) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (nb > 0) g_default_nb = nb;
+}
+
+int sl1x1_device_ok(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return ensure_device() ? 1 : 0;
+}
+
+const char* sl1x1_version(void) { return "sl1x1-gb300 0.1 (sm_103a)"; }
+
+void sl1x1_prof_enable(int on) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!ensure_device()) return;
+  sl::prof_enable(on != 0);
+}
+
+int sl1x1_prof_read(int phase, long long* launches, double* ms, double* flops, double* bytes) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return sl::prof_read(phase, launches, ms, flops, bytes) ? 0 : -1;
+}
+
+long long sl1x1_launch_count(void) { return sl::launch_count(); }
+
+double sl1x1_dmma_peak_tflops(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!ensure_device()) return 0.0;
+  return sl::dmma_peak_tflops(g_dev.stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,67 @@
+// Internal interfaces shared by the sl1x1 translation units (not exported).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace sl {
+
+int num_sms();
+
+// ---- phase timers and launch counter (prof.cpp) ----
+enum Phase {
+  kPhPanel = 0,   // PDGETF2: sub-panel kernels and the in-panel swap/solve/update
+  kPhLaswp = 1,   // PDLASWP on the left and right column blocks
+  kPhTrsm = 2,    // PDTRSM for the U12 block row
+  kPhGemm = 3,    // PDGEMM trailing update (FP64 DMMA)
+  kPhSolve = 4,   // PDGETRS
+  kPhMixedGemm = 5,  // low-precision trailing update (tcgen05)
+  kPhMixedPanel = 6, // FP32 panel, swaps and solves of the mixed factorization
+  kPhRefine = 7,     // FP64 residuals, corrections and GMRES of the refinement
+  kPhBatched = 8,    // batched solver
+  kNumPhases = 9
+};
+void count_launches(int n);
+void phase_begin(int phase, cudaStream_t s);
+void phase_end(int phase, cudaStream_t s, double flops, double bytes);
+void prof_enable(bool on);
+bool prof_read(int phase, long long* launches, double* ms, double* flops, double* bytes);
+long long launch_count();
+
+// Register-only DMMA throughput loop (FP64 tensor peak calibration), TFLOP/s.
+double dmma_peak_tflops(cudaStream_t s);
+
+// C = alpha * op(A) * B + beta * C, FP64, column-major (dgemm_f64.cu).
+cudaError_t dgemm(bool transa, int m, int n, int k, double alpha, const double* A, long long lda,
+                  const double* B, long long ldb, double beta, double* C, long long ldc,
+                  cudaStream_t s);
+
+// Device workspace used by the FP64 factorization / solve (sized by the
+// caller through lu_workspace_bytes).
+struct LuWork {
+  int* bar;          // 2 ints: grid barrier state
+  int* status;       // 1 int: device status word (DevStatus)
+  int* info_col;     // 1 int: first zero-pivot column (0-based), INT_MAX if none
+  double* cand;      // candidate slots of the panel kernel
+  int* perm;         // n ints: composed row permutation (solve)
+  double* bswap;     // n * nrhs doubles: gathered right-hand sides (solve)
+  size_t perm_len;
+  size_t bswap_len;
+};
+
+size_t panel_cand_doubles();
+
+// FP64 LU of the m x n column-major matrix dA (leading dimension ldda),
+// right-looking, block size nb. dipiv receives min(m,n) 0-based pivot rows
+// relative to dA. ws->info_col receives the first zero-pivot column.
+cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, int nb,
+                          const LuWork& ws, cudaStream_t s);
+
+// FP64 solve with the factors of dgetrf_device (trans = 'N', 'T' or 'C').
+cudaError_t dgetrs_device(char trans, int n, int nrhs, const double* dA, long long ldda,
+                          const int* dipiv, double* dB, long long lddb, const LuWork& ws,
+                          cudaStream_t s);
+
+// dst[i] = src[i] + delta, n entries (device arrays).
+cudaError_t ipiv_shift(const int* src, int* dst, int n, int delta, cudaStream_t s);
+
+}  // namespace sl

@@ -1,0 +1,181 @@
+"""GPU parity tests of the plain FP64 path through the C ABI (pdgesv_,
+pdgetrf_, pdgetrs_ and the device entry points) against the CPU oracle.
+
+Bar: IPIV identical to the oracle's except in logged near-tie columns (top-2
+candidates within 1e-10 relative); scaled residuals ||A-PLU||/(||A|| max(M,N)
+eps) and ||Ax-b||/(||A|| ||x|| N eps) below 16 (LIN/pdlafchk.f,
+LIN/pdlaschk.f); exact INFO; untouched guard zones around every array.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from lu_helpers import RESID_THRESH, compare_ipiv, system
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+PADVAL = -9923.0  # the tester's guard value (pdludriver.f:77-79)
+
+
+@pytest.fixture(scope="module")
+def ctx(sl, gpu_required):
+    assert sl.lib().sl1x1_device_ok() == 1
+    return sl.blacs_gridinit(1, 1)
+
+
+def padded(a, pad_rows=3, pad_cols=2, ia=1, ja=1):
+    """Embed `a` at (ia, ja) of a larger Fortran array filled with PADVAL."""
+    m, n = a.shape
+    big = np.full((ia - 1 + m + pad_rows, ja - 1 + n + pad_cols), PADVAL, order="F")
+    big[ia - 1:ia - 1 + m, ja - 1:ja - 1 + n] = a
+    return big
+
+
+def guards_intact(big, ia, ja, m, n):
+    mask = np.ones(big.shape, dtype=bool)
+    mask[ia - 1:ia - 1 + m, ja - 1:ja - 1 + n] = False
+    return bool(np.all(big[mask] == PADVAL))
+
+
+def run_pdgesv(sl, ctx, A0, B0, nb, ia=1, ja=1):
+    n, nrhs = A0.shape[0], B0.shape[1]
+    Ab = padded(A0, ia=ia, ja=ja)
+    Bb = padded(B0, ia=ia, ja=1)
+    desca = np.array([1, ctx, Ab.shape[0], Ab.shape[1], nb, nb, 0, 0, Ab.shape[0]], np.int32)
+    descb = np.array([1, ctx, Bb.shape[0], Bb.shape[1], nb, nb, 0, 0, Bb.shape[0]], np.int32)
+    ipiv = np.full(Ab.shape[0] + nb + 4, -77, dtype=np.int32)
+    info = sl.pdgesv(n, nrhs, Ab, ia, ja, desca, ipiv, Bb, ia, 1, descb)
+    assert guards_intact(Ab, ia, ja, n, n)
+    assert guards_intact(Bb, ia, 1, n, nrhs)
+    # IPIV entries outside IPIV(IA:IA+N-1) are untouched
+    assert np.all(ipiv[:ia - 1] == -77) and np.all(ipiv[ia - 1 + n:] == -77)
+    LU = Ab[ia - 1:ia - 1 + n, ja - 1:ja - 1 + n]
+    X = Bb[ia - 1:ia - 1 + n, :nrhs]
+    rel = ipiv[ia - 1:ia - 1 + n] - (ia - 1)
+    return info, np.asfortranarray(LU), rel, np.asfortranarray(X)
+
+
+SMALL = [(1, 1), (2, 1), (3, 2), (31, 4), (64, 64), (65, 64), (257, 64), (257, 256), (1000, 64),
+         (1000, 256), (513, 1), (100, 2)]
+
+
+@pytest.mark.parametrize("n,nb", SMALL)
+def test_pdgesv_small_parity(sl, orc, ctx, n, nb):
+    A0, B0 = system(orc, n, 3)
+    info, LU, rel, X = run_pdgesv(sl, ctx, A0, B0, nb)
+    assert info == 0
+    bad, ties = compare_ipiv(orc, A0, rel, nb)
+    assert bad == 0, f"IPIV differs outside near-ties (ties logged: {ties})"
+    assert orc.fresid(LU, rel, A0) < RESID_THRESH
+    assert orc.sresid(A0, B0, X) < RESID_THRESH
+
+
+def test_example_known_answer_gpu(sl, orc, ctx):
+    d = json.load(open(os.path.join(GOLD, "dscaex.json")))
+    n = d["n"]
+    A0 = np.array(d["a_colmajor"]).reshape((n, n), order="F")
+    B0 = np.array(d["b"]).reshape((n, 1), order="F")
+    info, LU, rel, X = run_pdgesv(sl, ctx, A0, B0, d["nb"])
+    assert info == 0
+    np.testing.assert_allclose(X[:, 0], d["x_exact"], rtol=1e-13)
+    assert orc.sresid(A0, B0, X) < d["threshold"]
+
+
+@pytest.mark.parametrize("m,n", [(4, 4), (10, 12), (17, 13), (13, 13), (23, 23), (31, 31),
+                                 (57, 50)])
+@pytest.mark.parametrize("nb", [2, 3, 4, 5])
+def test_pdgetrf_lu_dat_shapes(sl, orc, ctx, m, n, nb):
+    # LU.dat sizes with the tester's own (-1,1] generator, factor only (M != N allowed)
+    A0 = orc.matgen(m, n, 100, kind=0)
+    Ab = padded(A0)
+    desc = np.array([1, ctx, Ab.shape[0], Ab.shape[1], nb, nb, 0, 0, Ab.shape[0]], np.int32)
+    ipiv = np.zeros(Ab.shape[0] + nb, dtype=np.int32)
+    info = sl.pdgetrf(m, n, Ab, 1, 1, desc, ipiv)
+    assert info == 0
+    assert guards_intact(Ab, 1, 1, m, n)
+    mn = min(m, n)
+    LU = np.asfortranarray(Ab[:m, :n])
+    bad, _ = compare_ipiv(orc, A0, ipiv[:mn], nb)
+    assert bad == 0
+    assert orc.fresid(LU, ipiv[:mn], A0) < 1.0  # LU.dat THRESH
+
+
+def test_submatrix_offsets(sl, orc, ctx):
+    nb, ia, ja, n = 8, 9, 17, 40
+    A0, B0 = system(orc, n, 2)
+    info, LU, rel, X = run_pdgesv(sl, ctx, A0, B0, nb, ia=ia, ja=ja)
+    assert info == 0
+    bad, _ = compare_ipiv(orc, A0, rel, nb)
+    assert bad == 0
+    assert orc.sresid(A0, B0, X) < RESID_THRESH
+
+
+def test_singular_info_and_no_solve(sl, orc, ctx):
+    n, nb = 80, 16
+    A0, B0 = system(orc, n, 1)
+    A0[:, 37] = 0.0
+    info, LU, rel, X = run_pdgesv(sl, ctx, A0, B0, nb)
+    _, _, infol = orc.lapack_dgetrf(A0)
+    assert info == infol == 38
+    np.testing.assert_array_equal(X, B0)  # PDGETRS skipped (pdgesv.f:231)
+    bad, _ = compare_ipiv(orc, A0, rel, nb)
+    assert bad == 0
+
+
+def test_zero_matrix_info_one(sl, orc, ctx):
+    n, nb = 10, 4
+    A0 = np.zeros((n, n), order="F")
+    Ab = padded(A0)
+    desc = np.array([1, ctx, Ab.shape[0], Ab.shape[1], nb, nb, 0, 0, Ab.shape[0]], np.int32)
+    ipiv = np.zeros(Ab.shape[0] + nb, dtype=np.int32)
+    assert sl.pdgetrf(n, n, Ab, 1, 1, desc, ipiv) == 1
+    np.testing.assert_array_equal(ipiv[:n], np.arange(1, n + 1))  # AMAX == 0 keeps the row
+
+
+@pytest.mark.parametrize("trans", ["N", "T", "C"])
+def test_pdgetrs_trans(sl, orc, ctx, trans):
+    n, nb, nrhs = 300, 32, 5
+    A0, B0 = system(orc, n, nrhs)
+    A = np.asfortranarray(A0.copy())
+    desc = np.array([1, ctx, n, n, nb, nb, 0, 0, n], np.int32)
+    ipiv = np.zeros(n + nb, dtype=np.int32)
+    assert sl.pdgetrf(n, n, A, 1, 1, desc, ipiv) == 0
+    X = np.asfortranarray(B0.copy())
+    descb = np.array([1, ctx, n, nrhs, nb, nb, 0, 0, n], np.int32)
+    assert sl.pdgetrs(trans, n, nrhs, A, 1, 1, desc, ipiv, X, 1, 1, descb) == 0
+    Aop = A0 if trans == "N" else np.asfortranarray(A0.T)
+    assert orc.sresid(Aop, B0, X) < RESID_THRESH
+
+
+def test_device_entry_points(sl, orc, ctx):
+    import torch
+
+    n, nrhs, nb = 777, 4, 64
+    A0, B0 = system(orc, n, nrhs)
+    ldda = 800
+    dA = torch.zeros((n, ldda), dtype=torch.float64, device="cuda")  # column-major via transpose
+    dA[:, :n] = torch.from_numpy(np.ascontiguousarray(A0.T)).cuda()
+    dB = torch.from_numpy(np.ascontiguousarray(B0.T)).cuda()
+    dpiv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    info = sl.dgesv_dev(n, nrhs, dA.data_ptr(), ldda, dpiv.data_ptr(), dB.data_ptr(), n, nb)
+    assert info == 0
+    X = np.asfortranarray(dB.cpu().numpy().T)
+    rel = dpiv.cpu().numpy()
+    bad, _ = compare_ipiv(orc, A0, rel, nb)
+    assert bad == 0
+    assert orc.sresid(A0, B0, X) < RESID_THRESH
+
+
+def test_config_n2048_nb64(sl, orc, ctx):
+    # Plain FP64 PDGESV, N=2048, NB=64, NRHS=1, U[-0.5,0.5] from the seeded LCG
+    n, nb = 2048, 64
+    A0, B0 = system(orc, n, 1)
+    info, LU, rel, X = run_pdgesv(sl, ctx, A0, B0, nb)
+    assert info == 0
+    bad, ties = compare_ipiv(orc, A0, rel, nb)
+    assert bad == 0, ties
+    assert orc.fresid(LU, rel, A0) < RESID_THRESH
+    assert orc.sresid(A0, B0, X) < RESID_THRESH
