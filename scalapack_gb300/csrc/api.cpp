@@ -27,7 +27,8 @@ enum { DTYPE_ = 0, CTXT_ = 1, M_ = 2, N_ = 3, MB_ = 4, NB_ = 5, RSRC_ = 6, CSRC_
 // Fortran positions of the descriptor entries (DESC(k) has k = index + 1).
 enum { FDTYPE = 1, FCTXT = 2, FM = 3, FN = 4, FMB = 5, FNB = 6, FRSRC = 7, FCSRC = 8, FLLD = 9 };
 
-std::mutex g_mu;
+std::mutex g_mu;       // device state and the LU entry points
+std::mutex g_grid_mu;  // the 1x1 BLACS shim's context table
 
 // ---------------------------------------------------------------- BLACS shim
 struct Grid {
@@ -36,11 +37,24 @@ struct Grid {
 };
 std::vector<Grid> g_grids;
 
-void gridinfo(int ictxt, int* nprow, int* npcol, int* myrow, int* mycol) {
+void shim_gridinfo(int ictxt, int* nprow, int* npcol, int* myrow, int* mycol) {
+  std::lock_guard<std::mutex> lk(g_grid_mu);
   if (ictxt >= 0 && ictxt < (int)g_grids.size() && g_grids[ictxt].live &&
       g_grids[ictxt].nprow == 1 && g_grids[ictxt].npcol == 1) {
     *nprow = 1; *npcol = 1; *myrow = 0; *mycol = 0;
   } else {
+    *nprow = -1; *npcol = -1; *myrow = -1; *mycol = -1;
+  }
+}
+
+// Grid query used by the LU routines. It goes through the exported
+// blacs_gridinfo_ symbol, so a real BLACS linked ahead of this library
+// answers instead of the shim. Any grid other than 1x1 is reported as an
+// invalid context (NPROW = -1): the GPU path computes on one process only.
+void gridinfo(int ictxt, int* nprow, int* npcol, int* myrow, int* mycol) {
+  int c = ictxt;
+  blacs_gridinfo_(&c, nprow, npcol, myrow, mycol);
+  if (*nprow != 1 || *npcol != 1) {
     *nprow = -1; *npcol = -1; *myrow = -1; *mycol = -1;
   }
 }
@@ -421,10 +435,8 @@ void descinit_(int* DESC, const int* M, const int* N, const int* MB, const int* 
                const int* IRSRC, const int* ICSRC, const int* ICTXT, const int* LLD, int* INFO) {
   // TOOLS/descinit.f:148-192
   int nprow, npcol, myrow, mycol;
-  {
-    std::lock_guard<std::mutex> lk(g_mu);
-    gridinfo(*ICTXT, &nprow, &npcol, &myrow, &mycol);
-  }
+  int c = *ICTXT;
+  blacs_gridinfo_(&c, &nprow, &npcol, &myrow, &mycol);
   int info = 0;
   if (*M < 0) info = -2;
   else if (*N < 0) info = -3;
@@ -467,7 +479,7 @@ void blacs_get_(const int* ICTXT, const int* WHAT, int* VAL) {
 void blacs_gridinit_(int* ICTXT, const char* ORDER, const int* NPROW, const int* NPCOL,
                      size_t ORDER_len) {
   (void)ORDER; (void)ORDER_len;
-  std::lock_guard<std::mutex> lk(g_mu);
+  std::lock_guard<std::mutex> lk(g_grid_mu);
   Grid g;
   g.live = true;
   g.nprow = *NPROW;
@@ -477,19 +489,21 @@ void blacs_gridinit_(int* ICTXT, const char* ORDER, const int* NPROW, const int*
 }
 
 void blacs_gridinfo_(const int* ICTXT, int* NPROW, int* NPCOL, int* MYROW, int* MYCOL) {
-  std::lock_guard<std::mutex> lk(g_mu);
-  gridinfo(*ICTXT, NPROW, NPCOL, MYROW, MYCOL);
+  shim_gridinfo(*ICTXT, NPROW, NPCOL, MYROW, MYCOL);
 }
 
 void blacs_gridexit_(const int* ICTXT) {
-  std::lock_guard<std::mutex> lk(g_mu);
+  std::lock_guard<std::mutex> lk(g_grid_mu);
   if (*ICTXT >= 0 && *ICTXT < (int)g_grids.size()) g_grids[*ICTXT].live = false;
 }
 
 void blacs_exit_(const int* CONTINUE) {
   (void)CONTINUE;
+  {
+    std::lock_guard<std::mutex> lk(g_grid_mu);
+    for (auto& g : g_grids) g.live = false;
+  }
   std::lock_guard<std::mutex> lk(g_mu);
-  for (auto& g : g_grids) g.live = false;
   release_all();
 }
 
