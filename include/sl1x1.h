@@ -81,6 +81,17 @@ int sl1x1_dgetrs_dev(char trans, int n, int nrhs, const double* dA, long long ld
 int sl1x1_dgesv_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, double* dB,
                     long long lddb, int nb, void* stream);
 
+/* Allocation-free FP64 LU (no counterpart in the reference): the same
+ * factorization, pivots and INFO as sl1x1_dgetrf_dev, for callers that may not
+ * allocate GPU memory (memory pools or arenas that own the device heap,
+ * loops that must not allocate after start-up). Its scratch is a static
+ * 1 MiB device array held by every GPU that loads this library until exit.
+ * The first call on a device looks up that array's address (make it before
+ * any stream capture); calls whose GPU work overlaps race on the shared array.
+ * M above 152 SMs x 768 rows is rejected with -30000 before any launch. */
+int sl1x1_dgetrf_noalloc(int m, int n, double* dA, long long ldda, int* dipiv, int nb,
+                         void* stream);
+
 /* ---- Library control ----------------------------------------------------- */
 /* Free every device buffer the library holds (also done by blacs_exit_). */
 void sl1x1_finalize(void);

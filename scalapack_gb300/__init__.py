@@ -73,6 +73,8 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_dgesv_dev.argtypes = [C.c_int, C.c_int, vp, C.c_longlong, vp, vp, C.c_longlong,
                                   C.c_int, vp]
     L.sl1x1_dgesv_dev.restype = C.c_int
+    L.sl1x1_dgetrf_noalloc.argtypes = [C.c_int, C.c_int, vp, C.c_longlong, vp, C.c_int, vp]
+    L.sl1x1_dgetrf_noalloc.restype = C.c_int
     L.sl1x1_finalize.argtypes = []
     L.sl1x1_set_default_nb.argtypes = [C.c_int]
     L.sl1x1_device_ok.restype = C.c_int
@@ -202,6 +204,12 @@ def dgetrf_dev(m, n, a_ptr, ldda, ipiv_ptr, nb=0, stream=None) -> int:
     """sl1x1_dgetrf_dev on device pointers (e.g. torch ``.data_ptr()``)."""
     return lib().sl1x1_dgetrf_dev(m, n, C.c_void_p(a_ptr), ldda, C.c_void_p(ipiv_ptr), nb,
                                   _stream_ptr(stream))
+
+
+def dgetrf_noalloc(m, n, a_ptr, ldda, ipiv_ptr, nb=0, stream=None) -> int:
+    """sl1x1_dgetrf_noalloc: the factorization without any GPU allocation."""
+    return lib().sl1x1_dgetrf_noalloc(m, n, C.c_void_p(a_ptr), ldda, C.c_void_p(ipiv_ptr), nb,
+                                      _stream_ptr(stream))
 
 
 def dgetrs_dev(trans, n, nrhs, a_ptr, ldda, ipiv_ptr, b_ptr, lddb, stream=None) -> int:

@@ -276,6 +276,10 @@ int validate_getrf(const char* name, int m, int n, int ia, int ja, const int* de
 
 }  // namespace
 
+namespace sl {
+int default_nb() { return g_default_nb; }
+}  // namespace sl
+
 extern "C" {
 
 // ---------------------------------------------------------------- PDGETRF

@@ -30,6 +30,11 @@ constexpr int PT = 256;      // threads per panel CTA
 constexpr int PLD = PW + 1;  // shared row stride (doubles): conflict-free row/column walks
 
 size_t panel_cand_doubles() { return (size_t)2 * PMAXG * (PW + 2) + 2 * PW; }
+static_assert(kPanelCandDoubles == (size_t)2 * PMAXG * (PW + 2) + 2 * PW, "slot layout");
+
+// Rows per CTA are capped by 200 KB of shared memory (rpc * 33 doubles),
+// rounded down to a multiple of 8: 768 rows; one CTA per SM.
+int panel_max_rows() { return num_sms() * 768; }
 
 // Factor rows [r0, m) x columns [c0, c0+w) (w <= 32) of A in place.
 // Writes ipiv[c0+k] = 0-based pivot row for k < min(w, m-r0); records the first

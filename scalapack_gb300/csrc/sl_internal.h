@@ -49,6 +49,19 @@ struct LuWork {
 };
 
 size_t panel_cand_doubles();
+// Candidate-slot doubles the panel kernel needs (2 parities x 1024 CTAs x
+// (key, row, 32 values) + 2 diagonal rows); panel_cand_doubles() returns it.
+constexpr size_t kPanelCandDoubles = (size_t)2 * 1024 * (32 + 2) + 2 * 32;
+// Largest M the FP64 panel supports on this device (rows held in shared memory).
+int panel_max_rows();
+// Block size used when a caller passes nb <= 0.
+int default_nb();
+// While an instance lives on a thread, phase timers record nothing on it
+// (they would create CUDA events).
+struct ProfSuppress {
+  ProfSuppress();
+  ~ProfSuppress();
+};
 
 // FP64 LU of the m x n column-major matrix dA (leading dimension ldda),
 // right-looking, block size nb. dipiv receives min(m,n) 0-based pivot rows
