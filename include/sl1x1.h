@@ -81,6 +81,14 @@ int sl1x1_dgetrs_dev(char trans, int n, int nrhs, const double* dA, long long ld
 int sl1x1_dgesv_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, double* dB,
                     long long lddb, int nb, void* stream);
 
+/* Low-precision trailing update on device data, the PDGEMM step of the
+ * mixed-precision factorization: C (m x n) -= L (m x k) * U (k x n), FP32
+ * column-major, with L and U rounded to BF16 (fmt 0) or FP16 (fmt 1) -- U per
+ * column scaled by a power of two -- multiplied on tcgen05 tensor cores with
+ * FP32 accumulation. Returns 0 or a negative INFO. */
+int sl1x1_lowp_update_dev(int fmt, int m, int n, int k, const float* dL, long long ldl,
+                          const float* dU, long long ldu, float* dC, long long ldc, void* stream);
+
 /* Allocation-free FP64 LU (no counterpart in the reference): the same
  * factorization, pivots and INFO as sl1x1_dgetrf_dev, for callers that may not
  * allocate GPU memory (memory pools or arenas that own the device heap,

@@ -75,6 +75,9 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_dgesv_dev.restype = C.c_int
     L.sl1x1_dgetrf_noalloc.argtypes = [C.c_int, C.c_int, vp, C.c_longlong, vp, C.c_int, vp]
     L.sl1x1_dgetrf_noalloc.restype = C.c_int
+    L.sl1x1_lowp_update_dev.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_longlong, vp,
+                                        C.c_longlong, vp, C.c_longlong, vp]
+    L.sl1x1_lowp_update_dev.restype = C.c_int
     L.sl1x1_finalize.argtypes = []
     L.sl1x1_set_default_nb.argtypes = [C.c_int]
     L.sl1x1_device_ok.restype = C.c_int

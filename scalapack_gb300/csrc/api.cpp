@@ -139,6 +139,9 @@ struct DevState {
   double* dcand = nullptr;
   int* dperm = nullptr; size_t capPerm = 0;
   double* dbswap = nullptr; size_t capBs = 0;
+  unsigned short* dA16 = nullptr; size_t capA16 = 0;
+  unsigned short* dB16 = nullptr; size_t capB16 = 0;
+  int* dcolexp = nullptr; size_t capCe = 0;
 };
 DevState g_dev;
 int g_default_nb = 256;
@@ -181,6 +184,7 @@ void release_all() {
   if (!g_dev.ok) return;
   cudaFree(g_dev.dA); cudaFree(g_dev.dB); cudaFree(g_dev.dipiv); cudaFree(g_dev.dsmall);
   cudaFree(g_dev.dcand); cudaFree(g_dev.dperm); cudaFree(g_dev.dbswap);
+  cudaFree(g_dev.dA16); cudaFree(g_dev.dB16); cudaFree(g_dev.dcolexp);
   if (g_dev.stream) cudaStreamDestroy(g_dev.stream);
   g_dev = DevState();
 }
@@ -565,6 +569,36 @@ int sl1x1_dgesv_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, dou
   int info = sl1x1_dgetrf_dev(n, n, dA, ldda, dipiv, nb, stream);
   if (info != 0) return info;
   return sl1x1_dgetrs_dev('N', n, nrhs, dA, ldda, dipiv, dB, lddb, stream);
+}
+
+int sl1x1_lowp_update_dev(int fmt, int m, int n, int k, const float* dL, long long ldl,
+                          const float* dU, long long ldu, float* dC, long long ldc, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (fmt != 0 && fmt != 1) return -1;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  if (k < 0) return -4;
+  if (m == 0 || n == 0 || k == 0) return 0;
+  if (!ensure_device()) return cuda_info(cudaErrorNoDevice);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int kpad = sl::lowp_kpad(k);
+  cudaError_t e = grow(&g_dev.dA16, &g_dev.capA16, (size_t)m * kpad);
+  if (e == cudaSuccess) e = grow(&g_dev.dB16, &g_dev.capB16, (size_t)n * kpad);
+  if (e == cudaSuccess) e = grow(&g_dev.dcolexp, &g_dev.capCe, (size_t)n);
+  if (e != cudaSuccess) return cuda_info(e);
+  const bool bf16 = (fmt == 0);
+  e = cudaMemsetAsync(g_dev.dsmall + 2, 0, sizeof(int), s);
+  if (e == cudaSuccess)
+    e = sl::lowp_pack(bf16, dL, ldl, m, dU, ldu, n, k, g_dev.dA16, g_dev.dB16, g_dev.dcolexp, s);
+  if (e == cudaSuccess)
+    e = sl::lowp_gemm(bf16, m, n, k, g_dev.dA16, g_dev.dB16, g_dev.dcolexp, dC, ldc,
+                      g_dev.dsmall + 2, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_info(e);
+  int st = 0;
+  e = cudaMemcpy(&st, g_dev.dsmall + 2, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_info(e);
+  return st ? -20000 - st : 0;
 }
 
 void sl1x1_finalize(void) {

@@ -1,0 +1,395 @@
+// Low-precision trailing update of the mixed-precision LU (the PDGEMM step of
+// SRC/pdgetrf.f:288-290 with 16-bit operands):
+//
+//   C (m x n, FP32, column-major) -= (A16 * B16^T) .* 2^e[col]
+//
+// A16 (m x k) and B16 (n x k) are BF16 or FP16 operand buffers stored K-major
+// (k contiguous), produced from the FP32 working matrix by lowp_pack_* below;
+// e[col] is the per-column power-of-two exponent that brought column `col` of
+// U12 into the 16-bit range. Products of 16-bit operands are exact in FP32 and
+// are accumulated in FP32 in tensor memory.
+//
+// Blackwell-native structure, one 128 x 256 output tile per CTA (4 warps):
+//   * warp 0 allocates 256 TMEM columns (the FP32 accumulator, lane = row);
+//   * one thread issues TMA loads (cp.async.bulk.tensor, 128-byte swizzle) of
+//     the 128x64 A and 256x64 B k-blocks into a 4-stage shared-memory ring,
+//     completion tracked by mbarrier transaction counts;
+//   * one thread issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=256,
+//     K=16) per 16-wide k-slice and frees each stage with tcgen05.commit;
+//   * all 4 warps read the accumulator back with tcgen05.ld (warp w owns TMEM
+//     lanes 32w..32w+31) and apply C -= acc * 2^e in a coalesced epilogue.
+// Every mbarrier wait is bounded; on timeout the CTA records kFlagTimeout in
+// the status word, drains what it issued, frees its TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "sl_internal.h"
+
+namespace sl {
+namespace {
+
+constexpr int BM = 128;
+constexpr int BN = 256;
+constexpr int BK = 64;       // 64 x 16-bit = 128 bytes: one swizzle row
+constexpr int STAGES = 4;
+constexpr int A_STAGE_BYTES = BM * BK * 2;  // 16 KB
+constexpr int B_STAGE_BYTES = BN * BK * 2;  // 32 KB
+constexpr int TMEM_COLS = 256;
+constexpr long long kWaitLimit = 1LL << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Bounded parity wait; returns false after kWaitLimit polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t addr = smem_u32(bar);
+  for (long long i = 0; i < kWaitLimit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (i > 256) __nanosleep(32);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, "
+      "{%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
+// groups 1024 bytes apart (SBO), descriptor version 1, start address in
+// 16-byte units. Advancing K by 16 elements (32 bytes) adds 2 to the start.
+__device__ __forceinline__ uint64_t smem_desc_sw128(const void* p) {
+  uint64_t addr = smem_u32(p);
+  uint64_t d = 0;
+  d |= (addr & 0x3FFFFULL) >> 4;          // start address
+  d |= (uint64_t)1 << 16;                 // LBO (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;       // SBO
+  d |= (uint64_t)1 << 46;                 // version
+  d |= (uint64_t)2 << 61;                 // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor for kind::f16: FP32 accumulator, A/B both BF16 or
+// both FP16, both K-major, N = 256, M = 128.
+__host__ __device__ constexpr uint32_t make_idesc(bool bf16) {
+  return (1u << 4)                          // D format: F32
+         | ((bf16 ? 1u : 0u) << 7)          // A format
+         | ((bf16 ? 1u : 0u) << 10)         // B format
+         | ((uint32_t)(BN >> 3) << 17)      // N / 8
+         | ((uint32_t)(BM >> 4) << 24);     // M / 16
+}
+
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct __align__(8) GemmSmemTail {
+  uint64_t full[STAGES];
+  uint64_t empty[STAGES];
+  uint64_t done;
+  uint32_t tmem_base;
+};
+
+__global__ void __launch_bounds__(128, 1)
+lowp_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                 float* C, long long ldc, int m, int n, int k, const int* __restrict__ col_exp,
+                 uint32_t idesc, int* status) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-byte alignment for the swizzled stages
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* sA = base;
+  unsigned char* sB = base + STAGES * A_STAGE_BYTES;
+  GemmSmemTail* tail = (GemmSmemTail*)(sB + STAGES * B_STAGE_BYTES);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const int nk = (k + BK - 1) / BK;
+  __shared__ int s_fail;
+  __shared__ int s_issued, s_consumed;
+
+  if (threadIdx.x == 0) {
+    s_fail = 0;
+    s_issued = 0;
+    s_consumed = 0;
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&tail->full[s], 1);
+      mbar_init(&tail->empty[s], 1);
+    }
+    mbar_init(&tail->done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tail->tmem_base)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tail->tmem_base;
+
+  if (warp == 0 && lane == 0) {
+    // TMA producer
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
+    for (int kb = 0; kb < nk; ++kb) {
+      const int s = kb % STAGES;
+      if (kb >= STAGES && !mbar_wait(&tail->empty[s], ((kb / STAGES) - 1) & 1)) {
+        atomicExch(status, (int)kFlagTimeout);
+        s_fail = 1;
+        break;
+      }
+      mbar_expect_tx(&tail->full[s], A_STAGE_BYTES + B_STAGE_BYTES);
+      tma_load_2d(sA + s * A_STAGE_BYTES, &tmA, &tail->full[s], kb * BK, m0);
+      tma_load_2d(sB + s * B_STAGE_BYTES, &tmB, &tail->full[s], kb * BK, n0);
+      s_issued = kb + 1;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    for (int kb = 0; kb < nk; ++kb) {
+      const int s = kb % STAGES;
+      if (!mbar_wait(&tail->full[s], (kb / STAGES) & 1)) {
+        atomicExch(status, (int)kFlagTimeout);
+        s_fail = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; ++kk) {
+        uint64_t ad = smem_desc_sw128(sA + s * A_STAGE_BYTES + kk * 32);
+        uint64_t bd = smem_desc_sw128(sB + s * B_STAGE_BYTES + kk * 32);
+        umma_f16(tmem, ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+      }
+      umma_commit(&tail->empty[s]);
+      s_consumed = kb + 1;
+    }
+    umma_commit(&tail->done);  // arrives when every issued MMA has completed
+  }
+  __syncwarp();
+  // Epilogue: all warps wait for the accumulator.
+  bool ok = mbar_wait(&tail->done, 0);
+  if (!ok) atomicExch(status, (int)kFlagTimeout);
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  __syncthreads();
+  if (ok && !s_fail) {
+    const int row = m0 + warp * 32 + lane;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      if (n0 + c0 >= n) break;  // warp-uniform
+      float v[32];
+      tmem_ld32(trow + (uint32_t)c0, v);
+      if (row < m) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int col = n0 + c0 + j;
+          if (col < n) {
+            float* cp = C + (long long)row + (long long)col * ldc;
+            *cp = fmaf(-v[j], ldexpf(1.0f, col_exp[col]), *cp);
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (s_fail && threadIdx.x == 0) {
+    // Drain TMA copies that were issued but never consumed (bounded waits).
+    for (int kb = s_consumed; kb < s_issued; ++kb)
+      mbar_wait(&tail->full[kb % STAGES], (kb / STAGES) & 1);
+  }
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS));
+  }
+}
+
+// ---- operand packing (FP32 working matrix -> 16-bit K-major operands) ------
+
+template <bool BF16>
+__device__ __forceinline__ unsigned short to16(float x) {
+  if (BF16) return __bfloat16_as_ushort(__float2bfloat16_rn(x));
+  return __half_as_ushort(__float2half_rn(x));
+}
+
+// A16[i*ldk + kk] = L21[i + kk*lda]  (m x k, transpose to K-major), kk < kpad
+// zero-filled beyond k. 32x32 tiles through shared memory.
+template <bool BF16>
+__global__ void pack_a_kernel(const float* __restrict__ L, long long lda, int m, int k, int kpad,
+                              unsigned short* A16) {
+  __shared__ float t[32][33];
+  const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    int kk = k0 + r, i = i0 + threadIdx.x;
+    t[r][threadIdx.x] = (i < m && kk < k) ? L[i + (long long)kk * lda] : 0.f;
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    int i = i0 + r, kk = k0 + threadIdx.x;
+    if (i < m && kk < kpad) A16[(long long)i * kpad + kk] = to16<BF16>(t[threadIdx.x][r]);
+  }
+}
+
+// Per-column exponent of U12 (k x n, column-major): e[j] = exponent that
+// scales max|U12[:,j]| into [0.5, 1); B16[j*kpad + kk] = U12[kk + j*ldu] * 2^-e.
+template <bool BF16>
+__global__ void pack_b_kernel(const float* __restrict__ U, long long ldu, int k, int n, int kpad,
+                              unsigned short* B16, int* col_exp) {
+  const int j = blockIdx.x;
+  if (j >= n) return;
+  __shared__ float s_max[32];
+  float mx = 0.f;
+  for (int kk = threadIdx.x; kk < k; kk += blockDim.x) mx = fmaxf(mx, fabsf(U[kk + (long long)j * ldu]));
+  for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    mx = threadIdx.x < (blockDim.x >> 5) ? s_max[threadIdx.x] : 0.f;
+    for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    if (threadIdx.x == 0) {
+      int e = 0;
+      if (mx > 0.f && isfinite(mx)) frexpf(mx, &e);
+      s_max[0] = __int_as_float(e);
+    }
+  }
+  __syncthreads();
+  const int e = __float_as_int(s_max[0]);
+  if (threadIdx.x == 0) col_exp[j] = e;
+  const float sc = ldexpf(1.0f, -e);
+  for (int kk = threadIdx.x; kk < kpad; kk += blockDim.x)
+    B16[(long long)j * kpad + kk] = to16<BF16>(kk < k ? U[kk + (long long)j * ldu] * sc : 0.f);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+// 2D tensor map over a rows x kpad row-major 16-bit operand, box {64, box_rows}.
+bool make_map(CUtensorMap* map, const void* ptr, int rows, int kpad, int box_rows) {
+  auto enc = get_encode();
+  if (!enc) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)kpad, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)kpad * 2};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void*>(ptr), dims, strides,
+                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+size_t lowp_gemm_smem_bytes() {
+  return 1024 + (size_t)STAGES * (A_STAGE_BYTES + B_STAGE_BYTES) + sizeof(GemmSmemTail) + 64;
+}
+
+int lowp_kpad(int k) { return (k + BK - 1) / BK * BK; }
+
+cudaError_t lowp_pack(bool bf16, const float* L, long long lda, int m, const float* U,
+                      long long ldu, int n, int k, unsigned short* A16, unsigned short* B16,
+                      int* col_exp, cudaStream_t s) {
+  const int kpad = lowp_kpad(k);
+  if (m > 0) {
+    dim3 g((m + 31) / 32, (kpad + 31) / 32), b(32, 8);
+    if (bf16) pack_a_kernel<true><<<g, b, 0, s>>>(L, lda, m, k, kpad, A16);
+    else pack_a_kernel<false><<<g, b, 0, s>>>(L, lda, m, k, kpad, A16);
+    count_launches(1);
+  }
+  if (n > 0) {
+    if (bf16) pack_b_kernel<true><<<n, 128, 0, s>>>(U, ldu, k, n, kpad, B16, col_exp);
+    else pack_b_kernel<false><<<n, 128, 0, s>>>(U, ldu, k, n, kpad, B16, col_exp);
+    count_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t lowp_gemm(bool bf16, int m, int n, int k, const unsigned short* A16,
+                      const unsigned short* B16, const int* col_exp, float* C, long long ldc,
+                      int* status, cudaStream_t s) {
+  if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
+  const int kpad = lowp_kpad(k);
+  CUtensorMap ta, tb;
+  if (!make_map(&ta, A16, m, kpad, BM) || !make_map(&tb, B16, n, kpad, BN))
+    return cudaErrorInvalidResourceHandle;
+  const size_t smem = lowp_gemm_smem_bytes();
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(lowp_gemm_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dim3 grid((m + BM - 1) / BM, (n + BN - 1) / BN);
+  lowp_gemm_kernel<<<grid, 128, smem, s>>>(ta, tb, C, ldc, m, n, kpad, col_exp, make_idesc(bf16),
+                                           status);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+}  // namespace sl

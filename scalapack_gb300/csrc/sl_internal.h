@@ -74,6 +74,19 @@ cudaError_t dgetrs_device(char trans, int n, int nrhs, const double* dA, long lo
                           const int* dipiv, double* dB, long long lddb, const LuWork& ws,
                           cudaStream_t s);
 
+// ---- low-precision trailing update (mixed_gemm.cu) ----
+// Pack L21 (m x k FP32 col-major) and U12 (k x n FP32 col-major, per-column
+// power-of-two scaled) into 16-bit K-major operands of k rounded up to 64.
+int lowp_kpad(int k);
+size_t lowp_gemm_smem_bytes();
+cudaError_t lowp_pack(bool bf16, const float* L, long long lda, int m, const float* U,
+                      long long ldu, int n, int k, unsigned short* A16, unsigned short* B16,
+                      int* col_exp, cudaStream_t s);
+// C (m x n FP32 col-major) -= (A16 B16^T) .* 2^col_exp (tcgen05, FP32 accumulate).
+cudaError_t lowp_gemm(bool bf16, int m, int n, int k, const unsigned short* A16,
+                      const unsigned short* B16, const int* col_exp, float* C, long long ldc,
+                      int* status, cudaStream_t s);
+
 // dst[i] = src[i] + delta, n entries (device arrays).
 cudaError_t ipiv_shift(const int* src, int* dst, int n, int delta, cudaStream_t s);
 
