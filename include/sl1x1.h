@@ -89,6 +89,26 @@ int sl1x1_dgesv_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, dou
 int sl1x1_lowp_update_dev(int fmt, int m, int n, int k, const float* dL, long long ldl,
                           const float* dU, long long ldu, float* dC, long long ldc, void* stream);
 
+/* Mixed-precision solve with iterative refinement (no routine of this form
+ * exists in the reference; the interface follows LAPACK DSGESV). A (FP64,
+ * n x n, device) is factored in FP32 with the trailing updates on tcgen05
+ * tensor cores in BF16 (fmt 0), FP16 (fmt 1) or split BF16x3 (fmt 2) with FP32
+ * accumulation; X is
+ * refined in FP64 (classical refinement, then GMRES-IR when a step fails to
+ * halve the scaled residual) until ||b-Ax||/(||A|| ||x|| N eps) <= tol
+ * (tol <= 0: 1.0). If refinement stalls, the FP64 factorization is used.
+ * dipiv receives the pivots of the factorization that produced X (0-based
+ * rows). keep_a = 1 keeps A intact in every case (an FP64 copy is made for the
+ * fallback); keep_a = 0 lets the fallback factor A in place (DSGESV).
+ * *iter (DSGESV convention): >= 0 refinement steps taken; -1 the low-precision
+ * factorization failed; -3 refinement did not converge (fallback used).
+ * stats[8] = {classical steps, GMRES-IR outer steps, GMRES inner iterations,
+ * fell back (0/1), final scaled residual, ||A||_inf, factor ms, refine ms}.
+ * Returns INFO (> 0: A is exactly singular in FP64). */
+int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, const double* dB,
+                       long long lddb, double* dX, long long lddx, int fmt, int nb, double tol,
+                       int keep_a, int* iter, double* stats, void* stream);
+
 /* Allocation-free FP64 LU (no counterpart in the reference): the same
  * factorization, pivots and INFO as sl1x1_dgetrf_dev, for callers that may not
  * allocate GPU memory (memory pools or arenas that own the device heap,

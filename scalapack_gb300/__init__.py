@@ -78,6 +78,10 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_lowp_update_dev.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_longlong, vp,
                                         C.c_longlong, vp, C.c_longlong, vp]
     L.sl1x1_lowp_update_dev.restype = C.c_int
+    L.sl1x1_dgesv_ir_dev.argtypes = [C.c_int, C.c_int, vp, C.c_longlong, vp, vp, C.c_longlong, vp,
+                                     C.c_longlong, C.c_int, C.c_int, C.c_double, C.c_int,
+                                     C.POINTER(C.c_int), C.POINTER(C.c_double), vp]
+    L.sl1x1_dgesv_ir_dev.restype = C.c_int
     L.sl1x1_finalize.argtypes = []
     L.sl1x1_set_default_nb.argtypes = [C.c_int]
     L.sl1x1_device_ok.restype = C.c_int
@@ -213,6 +217,23 @@ def dgetrf_noalloc(m, n, a_ptr, ldda, ipiv_ptr, nb=0, stream=None) -> int:
     """sl1x1_dgetrf_noalloc: the factorization without any GPU allocation."""
     return lib().sl1x1_dgetrf_noalloc(m, n, C.c_void_p(a_ptr), ldda, C.c_void_p(ipiv_ptr), nb,
                                       _stream_ptr(stream))
+
+
+IR_STATS = ["classical", "gmres_outer", "gmres_inner", "fell_back", "sresid", "anorm",
+            "factor_ms", "refine_ms"]
+
+
+def dgesv_ir_dev(n, nrhs, a_ptr, ldda, ipiv_ptr, b_ptr, lddb, x_ptr, lddx, fmt="bf16", nb=256,
+                 tol=1.0, keep_a=True, stream=None):
+    """Mixed-precision LU-IR (sl1x1_dgesv_ir_dev). Returns (info, iter, stats dict)."""
+    it = C.c_int()
+    st = (C.c_double * 8)()
+    f = {"bf16": 0, "fp16": 1, "bf16x3": 2}[fmt] if isinstance(fmt, str) else int(fmt)
+    info = lib().sl1x1_dgesv_ir_dev(n, nrhs, C.c_void_p(a_ptr), ldda, C.c_void_p(ipiv_ptr),
+                                    C.c_void_p(b_ptr), lddb, C.c_void_p(x_ptr), lddx, f, nb,
+                                    float(tol), 1 if keep_a else 0, C.byref(it), st,
+                                    _stream_ptr(stream))
+    return info, it.value, dict(zip(IR_STATS, list(st)))
 
 
 def dgetrs_dev(trans, n, nrhs, a_ptr, ldda, ipiv_ptr, b_ptr, lddb, stream=None) -> int:

@@ -139,6 +139,19 @@ struct DevState {
   double* dcand = nullptr;
   int* dperm = nullptr; size_t capPerm = 0;
   double* dbswap = nullptr; size_t capBs = 0;
+  // mixed-precision workspace
+  float* dF = nullptr; size_t capF = 0;
+  int* dpermx = nullptr; size_t capPermx = 0;
+  double* dR = nullptr; size_t capR = 0;
+  double* dD = nullptr; size_t capD = 0;
+  float* dXf = nullptr; size_t capXf = 0;
+  float* dXt = nullptr; size_t capXt = 0;
+  double* dcm = nullptr; size_t capCm = 0;
+  double* dV = nullptr; size_t capV = 0;
+  double* dw = nullptr; size_t capW = 0;
+  double* dAx = nullptr; size_t capAx = 0;
+  double* dh = nullptr; size_t capH = 0;
+  double* dAcopy = nullptr; size_t capAcopy = 0;
   unsigned short* dA16 = nullptr; size_t capA16 = 0;
   unsigned short* dB16 = nullptr; size_t capB16 = 0;
   int* dcolexp = nullptr; size_t capCe = 0;
@@ -185,6 +198,9 @@ void release_all() {
   cudaFree(g_dev.dA); cudaFree(g_dev.dB); cudaFree(g_dev.dipiv); cudaFree(g_dev.dsmall);
   cudaFree(g_dev.dcand); cudaFree(g_dev.dperm); cudaFree(g_dev.dbswap);
   cudaFree(g_dev.dA16); cudaFree(g_dev.dB16); cudaFree(g_dev.dcolexp);
+  cudaFree(g_dev.dF); cudaFree(g_dev.dpermx); cudaFree(g_dev.dR); cudaFree(g_dev.dD);
+  cudaFree(g_dev.dXf); cudaFree(g_dev.dXt); cudaFree(g_dev.dcm); cudaFree(g_dev.dV);
+  cudaFree(g_dev.dw); cudaFree(g_dev.dAx); cudaFree(g_dev.dh); cudaFree(g_dev.dAcopy);
   if (g_dev.stream) cudaStreamDestroy(g_dev.stream);
   g_dev = DevState();
 }
@@ -574,24 +590,23 @@ int sl1x1_dgesv_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, dou
 int sl1x1_lowp_update_dev(int fmt, int m, int n, int k, const float* dL, long long ldl,
                           const float* dU, long long ldu, float* dC, long long ldc, void* stream) {
   std::lock_guard<std::mutex> lk(g_mu);
-  if (fmt != 0 && fmt != 1) return -1;
+  if (fmt < 0 || fmt > 2) return -1;
   if (m < 0) return -2;
   if (n < 0) return -3;
   if (k < 0) return -4;
   if (m == 0 || n == 0 || k == 0) return 0;
   if (!ensure_device()) return cuda_info(cudaErrorNoDevice);
   cudaStream_t s = (cudaStream_t)stream;
-  const int kpad = sl::lowp_kpad(k);
+  const int kpad = sl::lowp_kpad(k) * sl::lowp_kmult(fmt);
   cudaError_t e = grow(&g_dev.dA16, &g_dev.capA16, (size_t)m * kpad);
   if (e == cudaSuccess) e = grow(&g_dev.dB16, &g_dev.capB16, (size_t)n * kpad);
   if (e == cudaSuccess) e = grow(&g_dev.dcolexp, &g_dev.capCe, (size_t)n);
   if (e != cudaSuccess) return cuda_info(e);
-  const bool bf16 = (fmt == 0);
   e = cudaMemsetAsync(g_dev.dsmall + 2, 0, sizeof(int), s);
   if (e == cudaSuccess)
-    e = sl::lowp_pack(bf16, dL, ldl, m, dU, ldu, n, k, g_dev.dA16, g_dev.dB16, g_dev.dcolexp, s);
+    e = sl::lowp_pack(fmt, dL, ldl, m, dU, ldu, n, k, g_dev.dA16, g_dev.dB16, g_dev.dcolexp, s);
   if (e == cudaSuccess)
-    e = sl::lowp_gemm(bf16, m, n, k, g_dev.dA16, g_dev.dB16, g_dev.dcolexp, dC, ldc,
+    e = sl::lowp_gemm(fmt, m, n, k, g_dev.dA16, g_dev.dB16, g_dev.dcolexp, dC, ldc,
                       g_dev.dsmall + 2, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_info(e);
@@ -599,6 +614,73 @@ int sl1x1_lowp_update_dev(int fmt, int m, int n, int k, const float* dL, long lo
   e = cudaMemcpy(&st, g_dev.dsmall + 2, sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_info(e);
   return st ? -20000 - st : 0;
+}
+
+int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, const double* dB,
+                       long long lddb, double* dX, long long lddx, int fmt, int nb, double tol,
+                       int keep_a, int* iter, double* stats, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (n < 0) return -1;
+  if (nrhs < 0) return -2;
+  if (ldda < (n > 1 ? n : 1)) return -4;
+  if (lddb < (n > 1 ? n : 1)) return -7;
+  if (lddx < (n > 1 ? n : 1)) return -9;
+  if (fmt < 0 || fmt > 2) return -10;
+  if (iter) *iter = 0;
+  if (n == 0 || nrhs == 0) return 0;
+  if (!ensure_device()) return cuda_info(cudaErrorNoDevice);
+  cudaStream_t s = (cudaStream_t)stream;
+  sl::IrOptions opt;
+  opt.fmt = fmt;
+  opt.nb = nb > 0 ? nb : 256;
+  opt.nb_fp64 = g_default_nb;
+  if (tol > 0) opt.tol = tol;
+  const long long ldf = round_ld(n);
+  const int kpad = sl::lowp_kpad(opt.nb) * sl::lowp_kmult(fmt);
+  const size_t m1 = (size_t)opt.gmres_m + 1;
+  cudaError_t e = cudaSuccess;
+#define GROW(p, c, cnt) if (e == cudaSuccess) e = grow(&g_dev.p, &g_dev.c, (size_t)(cnt))
+  GROW(dF, capF, (size_t)ldf * n);
+  GROW(dA16, capA16, (size_t)n * kpad);
+  GROW(dB16, capB16, (size_t)n * kpad);
+  GROW(dcolexp, capCe, n);
+  GROW(dpermx, capPermx, n);
+  GROW(dR, capR, (size_t)n * nrhs);
+  GROW(dD, capD, n);
+  GROW(dXf, capXf, (size_t)n * nrhs);
+  GROW(dXt, capXt, (size_t)n * nrhs);
+  GROW(dcm, capCm, 2 * (size_t)nrhs + 8);
+  GROW(dV, capV, (size_t)n * m1);
+  GROW(dw, capW, n);
+  GROW(dAx, capAx, n);
+  GROW(dh, capH, m1 + 8);
+  GROW(dperm, capPerm, n);
+  GROW(dbswap, capBs, (size_t)n * nrhs);
+  if (keep_a) GROW(dAcopy, capAcopy, (size_t)ldf * n);
+#undef GROW
+  if (e != cudaSuccess) return cuda_info(e);
+  sl::MixedWork mw;
+  mw.F = g_dev.dF; mw.ldf = ldf;
+  mw.A16 = g_dev.dA16; mw.B16 = g_dev.dB16; mw.col_exp = g_dev.dcolexp;
+  mw.perm = g_dev.dpermx; mw.R = g_dev.dR; mw.D = g_dev.dD;
+  mw.Xf = g_dev.dXf; mw.Xtmp = g_dev.dXt; mw.colmax = g_dev.dcm;
+  mw.V = g_dev.dV; mw.w = g_dev.dw; mw.Ax = g_dev.dAx; mw.h = g_dev.dh;
+  mw.Acopy = keep_a ? g_dev.dAcopy : nullptr; mw.ldacopy = ldf;
+  sl::LuWork w = make_work();
+  sl::IrStats st;
+  e = sl::dgesv_ir_device(n, nrhs, dA, ldda, dB, lddb, dX, lddx, g_dev.dipiv == nullptr ? dipiv : dipiv,
+                          opt, &st, w, mw, s);
+  if (e == cudaErrorInvalidValue) return -30000;
+  if (e != cudaSuccess) return cuda_info(e);
+  if (stats) {
+    stats[0] = st.classical; stats[1] = st.gmres_outer; stats[2] = st.gmres_inner;
+    stats[3] = st.fell_back; stats[4] = st.sresid; stats[5] = st.anorm;
+    stats[6] = st.factor_ms; stats[7] = st.refine_ms;
+  }
+  if (st.dev_status) return -20000 - st.dev_status;
+  if (iter) *iter = st.fell_back ? (st.gmres_outer > 0 || st.classical > 0 ? -3 : -1)
+                                 : st.classical + st.gmres_outer;
+  return st.info;
 }
 
 void sl1x1_finalize(void) {

@@ -144,56 +144,6 @@ dgemm_dmma_kernel(int m, int n, int k, double alpha, const double* __restrict__ 
       }
 }
 
-// Narrow right-hand side update used by the triangular solves: C(m x n) +=
-// alpha * A(m x k) * B(k x n) with n <= NC <= 16, k <= 64 (one thread per row,
-// SIMT FP64 -- the same pipe rate as DMMA, without padding n up to 8).
-template <bool TRANSA, int NC>
-__global__ void __launch_bounds__(256)
-dgemm_narrow_kernel(int m, int n, int k, double alpha, const double* __restrict__ A,
-                    long long lda, const double* __restrict__ B, long long ldb, double* C,
-                    long long ldc) {
-  __shared__ double Bs[64][NC];
-  for (int c = threadIdx.x; c < 64 * NC; c += blockDim.x) {
-    int kk = c % 64, nn = c / 64;
-    Bs[kk][nn] = (kk < k && nn < n) ? B[kk + (long long)nn * ldb] : 0.0;
-  }
-  __syncthreads();
-  long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= m) return;
-  double acc[NC];
-#pragma unroll
-  for (int j = 0; j < NC; ++j) acc[j] = 0.0;
-  for (int kk = 0; kk < k; ++kk) {
-    double a = TRANSA ? A[kk + row * lda] : A[row + (long long)kk * lda];
-#pragma unroll
-    for (int j = 0; j < NC; ++j) acc[j] = fma(a, Bs[kk][j], acc[j]);
-  }
-#pragma unroll
-  for (int j = 0; j < NC; ++j)
-    if (j < n) C[row + (long long)j * ldc] += alpha * acc[j];
-}
-
-template <bool TA, int NC>
-static cudaError_t launch_narrow(int m, int n, int k, double alpha, const double* A, long long lda,
-                                 const double* B, long long ldb, double* C, long long ldc,
-                                 cudaStream_t s) {
-  dim3 grid((m + 255) / 256);
-  dgemm_narrow_kernel<TA, NC><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, C, ldc);
-  count_launches(1);
-  return cudaGetLastError();
-}
-
-template <bool TA>
-static cudaError_t narrow_dispatch(int m, int n, int k, double alpha, const double* A,
-                                   long long lda, const double* B, long long ldb, double* C,
-                                   long long ldc, cudaStream_t s) {
-  if (n == 1) return launch_narrow<TA, 1>(m, n, k, alpha, A, lda, B, ldb, C, ldc, s);
-  if (n <= 2) return launch_narrow<TA, 2>(m, n, k, alpha, A, lda, B, ldb, C, ldc, s);
-  if (n <= 4) return launch_narrow<TA, 4>(m, n, k, alpha, A, lda, B, ldb, C, ldc, s);
-  if (n <= 8) return launch_narrow<TA, 8>(m, n, k, alpha, A, lda, B, ldb, C, ldc, s);
-  return launch_narrow<TA, 16>(m, n, k, alpha, A, lda, B, ldb, C, ldc, s);
-}
-
 template <int BM, int BN, int WM, int WN, bool TA>
 static cudaError_t launch_dmma(int m, int n, int k, double alpha, const double* A, long long lda,
                                const double* B, long long ldb, double beta, double* C,
@@ -232,10 +182,6 @@ cudaError_t dgemm(bool transa, int m, int n, int k, double alpha, const double* 
   if (m <= 0 || n <= 0) return cudaSuccess;
   if (k <= 0) {
     if (beta == 1.0) return cudaSuccess;
-  }
-  if (n <= 16 && k <= 64 && beta == 1.0) {
-    if (transa) return narrow_dispatch<true>(m, n, k, alpha, A, lda, B, ldb, C, ldc, s);
-    return narrow_dispatch<false>(m, n, k, alpha, A, lda, B, ldb, C, ldc, s);
   }
   // Pick the tile so that the grid covers the SMs: 128x128 when there are at
   // least ~2 waves of big tiles, 64x64 otherwise.

@@ -1,0 +1,512 @@
+// Type-generic LU kernels (T = double for the plain FP64 path, float for the
+// FP32 panel of the mixed-precision path) and their launch helpers.
+//
+//   panel_kernel<T>      PDGETF2 (SRC/pdgetf2.f:206-237) on a <=32-column sub-panel
+//   laswp_kernel<T>      PDLASWP (SRC/pdlaswp.f:163-172)
+//   trsm_strip_kernel<T> PDTRSM diagonal-block solves (PB_CptrsmAB.c)
+//   permute_rows_kernel<T>, gemm_skinny_kernel<T>  PDLAPIV and the narrow
+//                        off-diagonal updates of PDGETRS
+#pragma once
+#include <climits>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "sl_internal.h"
+
+namespace sl {
+
+constexpr int PW = 32;       // sub-panel width held in shared memory
+constexpr int PMAXG = 1024;  // max CTAs of the panel kernel
+constexpr int PT = 256;      // threads per panel CTA
+constexpr int PLD = PW + 1;  // shared row stride: conflict-free row and column walks
+
+// Factor rows [r0, m) x columns [c0, c0+w) (w <= 32) of A in place.
+//
+// Cooperative launch, one CTA per contiguous slice of rpc rows, the slice held
+// in shared memory. Per column: warp-shuffle IDAMAX inside each CTA, each
+// CTA's best (|x|, row) and its row values published to an L2 slot array
+// (double-buffered by column parity), one bounded grid barrier, then every CTA
+// selects the same winner (largest |x|, lowest row on ties), exchanges the
+// winner and diagonal rows it owns, scales its part of the column by ONE/GMAX
+// (reciprocal then multiply, SRC/pdgetf2.f:224) and applies the rank-1 update
+// with lanes = columns. Writes ipiv[c0+k] = r0 + pivot (0-based rows of A) for
+// k < min(w, m-r0) and the first exactly-zero pivot column into *info_col.
+template <typename T>
+__global__ void __launch_bounds__(PT)
+panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ipiv,
+             int* info_col, double* cand, int* bar, int* status) {
+  extern __shared__ __align__(16) unsigned char panel_smem[];
+  T* tile = reinterpret_cast<T*>(panel_smem);  // [rpc][PLD]
+  __shared__ double s_U[PW], s_D[PW];
+  __shared__ double s_wk[PT / 32];
+  __shared__ int s_wr[PT / 32];
+  __shared__ int s_row;
+  __shared__ int s_piv;
+  __shared__ double s_gmax;
+
+  const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int R = m - r0;
+  const int kw = min(w, R);
+  const int lo = b * rpc;                   // first local row (relative to r0)
+  const int nr = max(0, min(rpc, R - lo));  // rows owned
+  double* diag = cand + (size_t)2 * PMAXG * (PW + 2);
+
+  for (int c = 0; c < w; ++c)
+    for (int r = tid; r < nr; r += PT)
+      tile[r * PLD + c] = A[(long long)(r0 + lo + r) + (long long)(c0 + c) * lda];
+  __syncthreads();
+
+  for (int k = 0; k < kw; ++k) {
+    const int d = k;  // diagonal row relative to r0
+    const int par = k & 1;
+    // --- local IDAMAX over owned rows >= d ---
+    double key = -2.0;
+    int row = INT_MAX;
+    for (int r = tid; r < nr; r += PT) {
+      int gr = lo + r;
+      if (gr >= d) amax_combine(key, row, amax_key((double)tile[r * PLD + k]), gr);
+    }
+    warp_amax(key, row);
+    if (lane == 0) { s_wk[warp] = key; s_wr[warp] = row; }
+    __syncthreads();
+    if (warp == 0) {
+      key = lane < PT / 32 ? s_wk[lane] : -2.0;
+      row = lane < PT / 32 ? s_wr[lane] : INT_MAX;
+      warp_amax(key, row);
+      if (lane == 0) {
+        s_row = row;
+        double* slot = cand + ((size_t)par * PMAXG + b) * (PW + 2);
+        slot[0] = key;
+        slot[1] = (double)row;
+      }
+    }
+    __syncthreads();
+    {
+      double* slot = cand + ((size_t)par * PMAXG + b) * (PW + 2);
+      int lr = s_row;
+      if (tid < w && lr != INT_MAX) slot[2 + tid] = (double)tile[(lr - lo) * PLD + tid];
+      if (d >= lo && d < lo + nr && tid < w) diag[par * PW + tid] = (double)tile[(d - lo) * PLD + tid];
+    }
+    __threadfence();
+    if (!grid_barrier(bar, G, status)) return;
+
+    // --- global winner (largest |x|, lowest row on ties) ---
+    key = -2.0;
+    row = INT_MAX;
+    for (int q = tid; q < G; q += PT) {
+      const double* slot = cand + ((size_t)par * PMAXG + q) * (PW + 2);
+      double k2 = __ldcg(slot);
+      double r2 = __ldcg(slot + 1);
+      int ri = (r2 >= (double)INT_MAX) ? INT_MAX : (int)r2;
+      amax_combine(key, row, k2, ri);
+    }
+    warp_amax(key, row);
+    if (lane == 0) { s_wk[warp] = key; s_wr[warp] = row; }
+    __syncthreads();
+    if (warp == 0) {
+      key = lane < PT / 32 ? s_wk[lane] : -2.0;
+      row = lane < PT / 32 ? s_wr[lane] : INT_MAX;
+      warp_amax(key, row);
+      if (lane == 0) { s_row = row; s_wk[0] = key; }
+    }
+    __syncthreads();
+    const int grow = s_row;
+    const double gkey = s_wk[0];
+    if (tid < w) s_D[tid] = __ldcg(diag + par * PW + tid);
+    __syncthreads();
+    if (tid == 0) {
+      // IDAMAX keeps the first element when it is NaN; AMAX == 0 selects the
+      // diagonal row (PBLAS/SRC/pdamax_.c:486).
+      int piv = grow;
+      double dv = s_D[k];
+      if (dv != dv || gkey == 0.0) piv = d;
+      s_piv = piv;
+    }
+    __syncthreads();
+    const int piv = s_piv;
+    if (tid < w) {
+      if (piv == d) s_U[tid] = s_D[tid];
+      else s_U[tid] = __ldcg(cand + ((size_t)par * PMAXG + piv / rpc) * (PW + 2) + 2 + tid);
+    }
+    __syncthreads();
+    if (tid == 0) s_gmax = s_U[k];
+    // --- row interchange inside the sub-panel (PDSWAP, pdgetf2.f:218) ---
+    if (piv != d && tid < w) {
+      if (d >= lo && d < lo + nr) tile[(d - lo) * PLD + tid] = (T)s_U[tid];
+      if (piv >= lo && piv < lo + nr) tile[(piv - lo) * PLD + tid] = (T)s_D[tid];
+    }
+    __syncthreads();
+    const T gmax = (T)s_gmax;
+    if (b == 0 && tid == 0) {
+      ipiv[c0 + k] = r0 + piv;
+      if (gmax == (T)0) atomicMin(info_col, c0 + k);
+    }
+    // --- scale by ONE/GMAX (PDSCAL, pdgetf2.f:224) and rank-1 update (PDGER) ---
+    const bool scale = (gmax != (T)0);
+    const T rinv = scale ? (T)1 / gmax : (T)0;
+    const T u = (lane < w) ? (T)s_U[lane] : (T)0;
+    for (int r = warp; r < nr; r += PT / 32) {
+      int gr = lo + r;
+      if (gr <= d) continue;
+      T l = tile[r * PLD + k];
+      if (scale) l *= rinv;
+      __syncwarp();
+      if (lane == k) tile[r * PLD + k] = l;
+      else if (lane > k && lane < w) tile[r * PLD + lane] = fma(-l, u, tile[r * PLD + lane]);
+    }
+    __syncthreads();
+  }
+
+  for (int c = 0; c < w; ++c)
+    for (int r = tid; r < nr; r += PT)
+      A[(long long)(r0 + lo + r) + (long long)(c0 + c) * lda] = tile[r * PLD + c];
+}
+
+// Sequential row interchanges k1..k2-1 (rows i <-> ipiv[i]) on the columns
+// [cb1,ce1) and [cb2,ce2); one thread per column (PDLASWP 'Forward','Rows').
+template <typename T>
+__global__ void __launch_bounds__(256)
+laswp_kernel(T* A, long long lda, int k1, int k2, const int* __restrict__ ipiv, int cb1, int ce1,
+             int cb2, int ce2) {
+  __shared__ int s_piv[1024];
+  const int npiv = k2 - k1;
+  for (int i = threadIdx.x; i < npiv && i < 1024; i += blockDim.x) s_piv[i] = ipiv[k1 + i];
+  __syncthreads();
+  const long long n1 = ce1 - cb1, n2 = ce2 - cb2;
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n1 + n2) return;
+  long long col = idx < n1 ? cb1 + idx : cb2 + (idx - n1);
+  T* a = A + col * lda;
+  for (int i = 0; i < npiv; ++i) {
+    int p = i < 1024 ? s_piv[i] : ipiv[k1 + i];
+    int r = k1 + i;
+    if (p != r) {
+      T t = a[r];
+      a[r] = a[p];
+      a[p] = t;
+    }
+  }
+}
+
+// op(T) X = B for a w x w triangle (w <= 256) and a strip of NC columns of B
+// per CTA, held in shared memory. FORWARD solves top-down (lower, or upper^T),
+// otherwise bottom-up. Non-unit diagonals divide (reference DTRSM semantics).
+template <typename T, bool UPPER, bool TRANS, bool UNIT, int NC>
+__global__ void __launch_bounds__(256)
+trsm_strip_kernel(int w, int ncols, const T* __restrict__ Tm, long long ldt, T* B, long long ldb) {
+  constexpr bool FORWARD = (UPPER == TRANS);
+  constexpr int RG = 256 / NC;  // row groups
+  extern __shared__ __align__(16) unsigned char strip_smem[];
+  T* Bs = reinterpret_cast<T*>(strip_smem);  // [w][NC+1]
+  const int LD = NC + 1;
+  const int tid = threadIdx.x;
+  const int c = tid % NC, rg = tid / NC;
+  const long long col0 = (long long)blockIdx.x * NC;
+  const int nc = (int)min((long long)NC, ncols - col0);
+  for (int i = tid; i < w * NC; i += 256) {
+    int r = i % w, cc = i / w;
+    Bs[r * LD + cc] = cc < nc ? B[r + (col0 + cc) * ldb] : (T)0;
+  }
+  __syncthreads();
+  auto E = [&](int i, int j) -> T {
+    return TRANS ? Tm[j + (long long)i * ldt] : Tm[i + (long long)j * ldt];
+  };
+  for (int s = 0; s < w; ++s) {
+    const int i = FORWARD ? s : w - 1 - s;
+    if (!UNIT) {
+      if (tid < NC) Bs[i * LD + tid] = Bs[i * LD + tid] / E(i, i);
+      __syncthreads();
+    }
+    const T xi = Bs[i * LD + c];
+    if (FORWARD) {
+      for (int r = i + 1 + rg; r < w; r += RG) Bs[r * LD + c] = fma(-E(r, i), xi, Bs[r * LD + c]);
+    } else {
+      for (int r = rg; r < i; r += RG) Bs[r * LD + c] = fma(-E(r, i), xi, Bs[r * LD + c]);
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < w * NC; i += 256) {
+    int r = i % w, cc = i / w;
+    if (cc < nc) B[r + (col0 + cc) * ldb] = Bs[r * LD + cc];
+  }
+}
+
+// op(T) x = b for a w x w diagonal block (w <= 128) and few right-hand sides:
+// the CTA stages the block in shared memory (row stride w+1, conflict-free),
+// then each warp solves one column with its 4 rows per lane held in registers;
+// x_i is broadcast with a shuffle, so no block-wide barrier sits on the
+// dependency chain. Non-unit diagonals divide (reference DTRSM semantics).
+template <typename T, bool UPPER, bool TRANS, bool UNIT>
+__global__ void __launch_bounds__(128)
+trsv_warp_kernel(int w, int ncols, const T* __restrict__ Tm, long long ldt, T* B, long long ldb) {
+  extern __shared__ __align__(16) unsigned char trsv_smem[];
+  T* Ts = reinterpret_cast<T*>(trsv_smem);  // Ts[r*(w+1) + i] = op(T)(r, i)
+  const int W1 = w + 1;
+  for (int idx = threadIdx.x; idx < w * w; idx += blockDim.x) {
+    int r, i;
+    if (!TRANS) { r = idx % w; i = idx / w; }  // coalesced along r
+    else { i = idx % w; r = idx / w; }         // coalesced along i
+    Ts[r * W1 + i] = TRANS ? Tm[i + (long long)r * ldt] : Tm[r + (long long)i * ldt];
+  }
+  __syncthreads();
+  constexpr bool FORWARD = (UPPER == TRANS);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long col = (long long)blockIdx.x * 4 + warp;
+  if (col >= ncols) return;
+  T x[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    int r = lane + 32 * q;
+    x[q] = r < w ? B[r + col * ldb] : (T)0;
+  }
+  for (int s = 0; s < w; ++s) {
+    const int i = FORWARD ? s : w - 1 - s;
+    const int qi = i >> 5, li = i & 31;
+    if (!UNIT && lane == li) {
+      const T dinv = Ts[i * W1 + i];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (q == qi) x[q] = x[q] / dinv;
+    }
+    T own = x[0];
+#pragma unroll
+    for (int q = 1; q < 4; ++q)
+      if (q == qi) own = x[q];
+    const T xi = __shfl_sync(0xffffffffu, own, li);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int r = lane + 32 * q;
+      if (r < w && (FORWARD ? r > i : r < i)) x[q] = fma(-Ts[r * W1 + i], xi, x[q]);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    int r = lane + 32 * q;
+    if (r < w) B[r + col * ldb] = x[q];
+  }
+}
+
+// dst(i, c) = src(perm[i], c) (forward) or dst(perm[i], c) = src(i, c) (inverse).
+template <typename TS, typename TD>
+__global__ void permute_rows_kernel(const TS* __restrict__ src, long long lds, TD* dst,
+                                    long long ldd, const int* __restrict__ perm, int n, int nrhs,
+                                    int inverse) {
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)n * nrhs) return;
+  int i = (int)(idx % n), c = (int)(idx / n);
+  int p = perm[i];
+  if (!inverse) dst[i + c * ldd] = (TD)src[p + c * lds];
+  else dst[p + c * ldd] = (TD)src[i + c * lds];
+}
+
+// C (m x n) += alpha * op(A) (m x k) * B (k x n) for n <= NC <= 16 and any k:
+// one thread per row of C, B staged in 64-row chunks through shared memory.
+// Used for the narrow off-diagonal updates of the triangular solves and for
+// residuals b - A x with a few right-hand sides.
+template <typename T, bool TRANSA, int NC>
+__global__ void __launch_bounds__(256)
+gemm_skinny_kernel(int m, int n, int k, T alpha, const T* __restrict__ A, long long lda,
+                   const T* __restrict__ B, long long ldb, T* C, long long ldc) {
+  __shared__ T Bs[64][NC];
+  const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  T acc[NC];
+#pragma unroll
+  for (int j = 0; j < NC; ++j) acc[j] = (T)0;
+  for (int k0 = 0; k0 < k; k0 += 64) {
+    const int kc = min(64, k - k0);
+    __syncthreads();
+    for (int c = threadIdx.x; c < 64 * NC; c += blockDim.x) {
+      int kk = c % 64, nn = c / 64;
+      Bs[kk][nn] = (kk < kc && nn < n) ? B[(k0 + kk) + (long long)nn * ldb] : (T)0;
+    }
+    __syncthreads();
+    if (row < m) {
+#pragma unroll 16
+      for (int kk = 0; kk < kc; ++kk) {
+        T a = TRANSA ? A[(k0 + kk) + row * lda] : A[row + (long long)(k0 + kk) * lda];
+#pragma unroll
+        for (int j = 0; j < NC; ++j) acc[j] = fma(a, Bs[kk][j], acc[j]);
+      }
+    }
+  }
+  if (row < m) {
+#pragma unroll
+    for (int j = 0; j < NC; ++j)
+      if (j < n) C[row + (long long)j * ldc] += alpha * acc[j];
+  }
+}
+
+// ------------------------------------------------------------ launch helpers
+
+template <typename T>
+inline cudaError_t launch_panel(T* A, long long lda, int m, int r0, int c0, int w, int* ipiv,
+                                const LuWork& ws, cudaStream_t s) {
+  const int R = m - r0;
+  const int nsm = num_sms();
+  int rpc = (R + nsm - 1) / nsm;
+  if (rpc < 64) rpc = 64;
+  rpc = (rpc + 7) & ~7;
+  const int G = (R + rpc - 1) / rpc;
+  const size_t smem = sizeof(T) * (size_t)rpc * PLD;
+  if (smem > 200 * 1024 || G > PMAXG) return cudaErrorInvalidValue;  // M beyond the panel limit
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(panel_kernel<T>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  cudaError_t e = cudaMemsetAsync(ws.bar, 0, 2 * sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  void* args[] = {&A, &lda, &m, &r0, &c0, &w, (void*)&rpc, &ipiv, (void*)&ws.info_col,
+                  (void*)&ws.cand, (void*)&ws.bar, (void*)&ws.status};
+  count_launches(1);
+  return cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(PT), args, smem, s);
+}
+
+template <typename T>
+inline cudaError_t laswp(T* A, long long lda, int k1, int k2, const int* ipiv, int cb1, int ce1,
+                         int cb2, int ce2, cudaStream_t s) {
+  const long long ncols = (long long)(ce1 - cb1) + (ce2 - cb2);
+  if (ncols <= 0 || k2 <= k1) return cudaSuccess;
+  dim3 grid((unsigned)((ncols + 255) / 256));
+  laswp_kernel<T><<<grid, 256, 0, s>>>(A, lda, k1, k2, ipiv, cb1, ce1, cb2, ce2);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+template <typename T, bool UPPER, bool TRANS, bool UNIT, int NC = 8>
+inline cudaError_t trsm_strip(int w, int ncols, const T* Tm, long long ldt, T* B, long long ldb,
+                              cudaStream_t s) {
+  if (w <= 0 || ncols <= 0) return cudaSuccess;
+  const size_t smem = sizeof(T) * (size_t)w * (NC + 1);
+  auto kern = trsm_strip_kernel<T, UPPER, TRANS, UNIT, NC>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         100 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  dim3 grid((ncols + NC - 1) / NC);
+  kern<<<grid, 256, smem, s>>>(w, ncols, Tm, ldt, B, ldb);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+template <typename T, bool TA, int NC>
+inline cudaError_t launch_skinny(int m, int n, int k, T alpha, const T* A, long long lda,
+                                 const T* B, long long ldb, T* C, long long ldc, cudaStream_t s) {
+  dim3 grid((m + 255) / 256);
+  gemm_skinny_kernel<T, TA, NC><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, C, ldc);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+// C += alpha * op(A) * B for n <= 16 columns.
+template <typename T>
+inline cudaError_t gemm_skinny(bool transa, int m, int n, int k, T alpha, const T* A,
+                               long long lda, const T* B, long long ldb, T* C, long long ldc,
+                               cudaStream_t s) {
+  if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
+#define SL_SK(NC)                                                                              \
+  return transa ? launch_skinny<T, true, NC>(m, n, k, alpha, A, lda, B, ldb, C, ldc, s)        \
+                : launch_skinny<T, false, NC>(m, n, k, alpha, A, lda, B, ldb, C, ldc, s)
+  if (n == 1) { SL_SK(1); }
+  if (n <= 2) { SL_SK(2); }
+  if (n <= 4) { SL_SK(4); }
+  if (n <= 8) { SL_SK(8); }
+  SL_SK(16);
+#undef SL_SK
+}
+
+template <typename TS, typename TD>
+inline cudaError_t permute_rows(const TS* src, long long lds, TD* dst, long long ldd,
+                                const int* perm, int n, int nrhs, int inverse, cudaStream_t s) {
+  const long long total = (long long)n * nrhs;
+  if (total <= 0) return cudaSuccess;
+  permute_rows_kernel<TS, TD><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(
+      src, lds, dst, ldd, perm, n, nrhs, inverse);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+#define SL_TRY(x)                     \
+  do {                                \
+    cudaError_t _e = (x);             \
+    if (_e != cudaSuccess) return _e; \
+  } while (0)
+
+// C += alpha op(A) B for the off-diagonal blocks of the solves (defined per
+// type: FP64 in lu_f64.cu with DMMA for wide B, FP32 in mixed.cu).
+template <typename T>
+cudaError_t gemm_update(bool transa, int m, int n, int k, T alpha, const T* A, long long lda,
+                        const T* B, long long ldb, T* C, long long ldc, cudaStream_t s);
+template <>
+cudaError_t gemm_update<double>(bool, int, int, int, double, const double*, long long,
+                                const double*, long long, double*, long long, cudaStream_t);
+template <>
+cudaError_t gemm_update<float>(bool, int, int, int, float, const float*, long long, const float*,
+                               long long, float*, long long, cudaStream_t);
+
+template <typename T, bool UPPER, bool TRANS, bool UNIT>
+inline cudaError_t diag_solve(int kb, int nrhs, const T* Td, long long lda, T* X, long long ldx,
+                              cudaStream_t s) {
+  if (kb <= 128 && nrhs <= 16) {
+    // Few right-hand sides: one warp per column, the block in shared memory.
+    auto kern = trsv_warp_kernel<T, UPPER, TRANS, UNIT>;
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           140 * 1024);
+      if (e != cudaSuccess) return e;
+      attr_set = true;
+    }
+    const size_t smem = sizeof(T) * (size_t)kb * (kb + 1);
+    kern<<<(nrhs + 3) / 4, 128, smem, s>>>(kb, nrhs, Td, lda, X, ldx);
+    count_launches(1);
+    return cudaGetLastError();
+  }
+  return trsm_strip<T, UPPER, TRANS, UNIT, 8>(kb, nrhs, Td, lda, X, ldx, s);
+}
+
+// Blocked triangular solve op(T) X = X with the n x n LU factors in A:
+// lower = unit-lower L, otherwise non-unit upper U; trans solves with T^T.
+// Diagonal blocks (256 wide for large n, 64 otherwise) are solved in shared
+// memory; off-diagonal blocks are applied with gemm_update.
+template <typename T>
+inline cudaError_t tri_solve(bool lower, bool trans, bool unit, int n, int nrhs, const T* A,
+                             long long lda, T* X, long long ldx, cudaStream_t s) {
+  const int KB = nrhs <= 16 ? 128 : (n >= 2048 ? 256 : 64);
+  const bool forward = (lower != trans);
+  const int nblk = (n + KB - 1) / KB;
+  for (int bi = 0; bi < nblk; ++bi) {
+    const int b = forward ? bi : nblk - 1 - bi;
+    const int k0 = b * KB;
+    const int kb = (n - k0) < KB ? (n - k0) : KB;
+    const T* Td = A + k0 + (long long)k0 * lda;
+    if (lower && !trans) SL_TRY((diag_solve<T, false, false, true>(kb, nrhs, Td, lda, X + k0, ldx, s)));
+    else if (!lower && !trans) {
+      if (unit) SL_TRY((diag_solve<T, true, false, true>(kb, nrhs, Td, lda, X + k0, ldx, s)));
+      else SL_TRY((diag_solve<T, true, false, false>(kb, nrhs, Td, lda, X + k0, ldx, s)));
+    } else if (!lower && trans) SL_TRY((diag_solve<T, true, true, false>(kb, nrhs, Td, lda, X + k0, ldx, s)));
+    else SL_TRY((diag_solve<T, false, true, true>(kb, nrhs, Td, lda, X + k0, ldx, s)));
+    if (forward) {
+      const int rest = n - k0 - kb;
+      if (rest > 0) {
+        // X[k0+kb:] -= op(T)[k0+kb:, k0:k0+kb] * X[k0:k0+kb]
+        const T* Aoff = trans ? A + k0 + (long long)(k0 + kb) * lda : A + (k0 + kb) + (long long)k0 * lda;
+        SL_TRY(gemm_update<T>(trans, rest, nrhs, kb, (T)-1, Aoff, lda, X + k0, ldx, X + k0 + kb, ldx, s));
+      }
+    } else if (k0 > 0) {
+      // X[0:k0] -= op(T)[0:k0, k0:k0+kb] * X[k0:k0+kb]
+      const T* Aoff = trans ? A + k0 : A + (long long)k0 * lda;
+      SL_TRY(gemm_update<T>(trans, k0, nrhs, kb, (T)-1, Aoff, lda, X + k0, ldx, X, ldx, s));
+    }
+  }
+  return cudaSuccess;
+}
+
+}  // namespace sl

@@ -1,0 +1,546 @@
+// Mixed-precision LU with iterative refinement (LU-IR) on one GB300.
+//
+// Factorization (the PDGETRF loop of SRC/pdgetrf.f:254-295 in low precision):
+// the FP64 matrix is copied to an FP32 working matrix; the panel (PDGETF2),
+// row interchanges (PDLASWP) and U12 solve (PDTRSM) run in FP32 with the same
+// kernels as the FP64 path, and the trailing update (PDGEMM) rounds L21 and
+// U12 to BF16 or FP16 -- U12 scaled per column by a power of two -- and
+// multiplies them on tcgen05 tensor cores with FP32 accumulation
+// (mixed_gemm.cu).
+//
+// Refinement: FP64 is kept only for the residual b - A x (the original FP64
+// matrix stays untouched in HBM), the solution update and the GMRES
+// orthogonalization. Corrections are solved with the FP32 factors (right-hand
+// side scaled by a power of two into FP32 range). Classical refinement runs up
+// to `max_ir` steps and stops when the tester's scaled residual
+// ||b - A x||_inf / (||A||_inf ||x||_inf N eps) (TESTING/traditional/LIN/
+// pdlaschk.f:185-187) is at or below `tol`; when a step fails to halve it,
+// GMRES-IR takes over (GMRES on the left-preconditioned system (LU)^-1 A d =
+// (LU)^-1 r, classical Gram-Schmidt applied twice, Givens rotations). When
+// GMRES-IR also stalls, the FP64 factorization of the DMMA path is run and the
+// system is solved in plain FP64 (the reference's PDGERFS stall rule,
+// SRC/pdgerfs.f:552, motivates the halving test).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "lu_kernels.cuh"
+#include "sl_internal.h"
+
+namespace sl {
+
+// ------------------------------------------------------------ FP32 SIMT GEMM
+// C (m x n) += alpha op(A) (m x k) B (k x n), FP32, column-major. 64x64 tiles,
+// K-step 16, 256 threads each computing 4x4. Used for the in-panel updates of
+// the FP32 factorization (k = 32) and for wide right-hand sides in the solves.
+template <bool TRANSA>
+__global__ void __launch_bounds__(256)
+sgemm_simt_kernel(int m, int n, int k, float alpha, const float* __restrict__ A, long long lda,
+                  const float* __restrict__ B, long long ldb, float* C, long long ldc) {
+  __shared__ float As[16][64 + 4];
+  __shared__ float Bs[16][64 + 4];
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;
+  const long long m0 = (long long)blockIdx.x * 64, n0 = (long long)blockIdx.y * 64;
+  float acc[4][4] = {};
+  for (int k0 = 0; k0 < k; k0 += 16) {
+    for (int c = tid; c < 64 * 16; c += 256) {
+      int mm, kk;
+      if (!TRANSA) { kk = c / 64; mm = c % 64; } else { mm = c / 16; kk = c % 16; }
+      long long gm = m0 + mm, gk = k0 + kk;
+      As[kk][mm] = (gm < m && gk < k) ? (TRANSA ? A[gk + gm * lda] : A[gm + gk * lda]) : 0.f;
+      int nn = c / 16, kb = c % 16;
+      long long gn = n0 + nn, gkb = k0 + kb;
+      Bs[kb][nn] = (gn < n && gkb < k) ? B[gkb + gn * ldb] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      long long r = m0 + ty * 4 + i, c = n0 + tx * 4 + j;
+      if (r < m && c < n) C[r + c * ldc] += alpha * acc[i][j];
+    }
+}
+
+static cudaError_t sgemm_simt(bool transa, int m, int n, int k, float alpha, const float* A,
+                              long long lda, const float* B, long long ldb, float* C,
+                              long long ldc, cudaStream_t s) {
+  if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
+  dim3 grid((m + 63) / 64, (n + 63) / 64);
+  if (transa) sgemm_simt_kernel<true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, C, ldc);
+  else sgemm_simt_kernel<false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, C, ldc);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+template <>
+cudaError_t gemm_update<float>(bool transa, int m, int n, int k, float alpha, const float* A,
+                               long long lda, const float* B, long long ldb, float* C,
+                               long long ldc, cudaStream_t s) {
+  if (n <= 16) return gemm_skinny<float>(transa, m, n, k, alpha, A, lda, B, ldb, C, ldc, s);
+  return sgemm_simt(transa, m, n, k, alpha, A, lda, B, ldb, C, ldc, s);
+}
+
+// ------------------------------------------------------------ small kernels
+__global__ void d2s_kernel(const double* __restrict__ A, long long lda, int m, int n, float* F,
+                           long long ldf) {
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long total = (long long)m * n;
+  for (; idx < total; idx += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(idx % m);
+    long long j = idx / m;
+    F[i + j * ldf] = (float)A[i + j * lda];
+  }
+}
+
+// out[c] = max_i |X(i,c)| (NaN propagates), one CTA per column.
+__global__ void colmax_abs_kernel(const double* __restrict__ X, long long ldx, int n, double* out) {
+  __shared__ double sm[32];
+  const int c = blockIdx.x;
+  double mx = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double v = fabs(X[i + (long long)c * ldx]);
+    mx = (v > mx || v != v) ? v : mx;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    double o = __shfl_xor_sync(0xffffffffu, mx, off);
+    mx = (o > mx || o != o) ? o : mx;
+  }
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    mx = threadIdx.x < (blockDim.x >> 5) ? sm[threadIdx.x] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) {
+      double o = __shfl_xor_sync(0xffffffffu, mx, off);
+      mx = (o > mx || o != o) ? o : mx;
+    }
+    if (threadIdx.x == 0) out[c] = mx;
+  }
+}
+
+// ||A||_inf = max_i sum_j |A(i,j)|: row sums by threads over rows.
+__global__ void rowsum_abs_kernel(const double* __restrict__ A, long long lda, int n,
+                                  double* rows) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int j = 0; j < n; ++j) s += fabs(A[i + (long long)j * lda]);
+  rows[i] = s;
+}
+
+// Fx(:,c) = float(R(:,c) * 2^-e_c) with e_c the exponent of colmax[c].
+__global__ void scale_to_float_kernel(const double* __restrict__ R, long long ldr, int n, int ncols,
+                                      const double* __restrict__ colmax, float* Fx,
+                                      long long ldf) {
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)n * ncols) return;
+  int i = (int)(idx % n), c = (int)(idx / n);
+  int e = 0;
+  double mx = colmax[c];
+  if (mx > 0.0 && isfinite(mx)) frexp(mx, &e);
+  Fx[i + (long long)c * ldf] = (float)ldexp(R[i + (long long)c * ldr], -e);
+}
+
+// X(:,c) = beta * X(:,c) + double(Fx(:,c)) * 2^e_c.
+__global__ void float_scaled_add_kernel(const float* __restrict__ Fx, long long ldf, int n,
+                                        int ncols, const double* __restrict__ colmax, double beta,
+                                        double* X, long long ldx) {
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)n * ncols) return;
+  int i = (int)(idx % n), c = (int)(idx / n);
+  int e = 0;
+  double mx = colmax[c];
+  if (mx > 0.0 && isfinite(mx)) frexp(mx, &e);
+  double v = ldexp((double)Fx[i + (long long)c * ldf], e);
+  double* xp = X + i + (long long)c * ldx;
+  *xp = (beta == 0.0) ? v : beta * *xp + v;
+}
+
+// h[i] = V(:,i) . w for i < ncols (one CTA per column, fixed reduction order).
+__global__ void dots_kernel(const double* __restrict__ V, long long ldv, int n, int ncols,
+                            const double* __restrict__ w, double* h) {
+  __shared__ double sm[32];
+  const int c = blockIdx.x;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s = fma(V[i + (long long)c * ldv], w[i], s);
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? sm[threadIdx.x] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (threadIdx.x == 0) h[c] = s;
+  }
+}
+
+// w -= V(:, 0:ncols) h
+__global__ void sub_vh_kernel(const double* __restrict__ V, long long ldv, int n, int ncols,
+                              const double* __restrict__ h, double* w) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = w[i];
+  for (int c = 0; c < ncols; ++c) s = fma(-V[i + (long long)c * ldv], h[c], s);
+  w[i] = s;
+}
+
+// y = alpha * x (n entries), alpha read from device memory as 1/alpha_inv.
+__global__ void scale_vec_kernel(const double* __restrict__ x, int n, const double* alpha_inv,
+                                 double* y) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = x[i] / alpha_inv[0];
+}
+
+// x += V(:,0:k) y (host-supplied coefficients in device memory).
+__global__ void add_vy_kernel(const double* __restrict__ V, long long ldv, int n, int k,
+                              const double* __restrict__ y, double* x) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = x[i];
+  for (int c = 0; c < k; ++c) s = fma(V[i + (long long)c * ldv], y[c], s);
+  x[i] = s;
+}
+
+// y += x
+__global__ void axpy1_kernel(int n, const double* __restrict__ x, double* y) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] += x[i];
+}
+
+static unsigned blocks_for(long long n, int t = 256) {
+  long long b = (n + t - 1) / t;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+// ---------------------------------------------------- FP32 factorization
+cudaError_t sgetrf_mixed_device(int n, float* F, long long ldf, int* dipiv, int nb, int fmt,
+                                const LuWork& ws, const MixedWork& mw, cudaStream_t s) {
+  SL_TRY(cudaMemsetAsync(ws.status, 0, sizeof(int), s));
+  SL_TRY(cudaMemsetAsync(ws.info_col, 0x7f, sizeof(int), s));
+  const int m = n, mn = n;
+  if (nb > 1024) nb = 1024;
+  auto Fp = [&](long long i, long long j) { return F + i + j * ldf; };
+  for (int j = 0; j < mn; j += nb) {
+    const int jb = (mn - j) < nb ? (mn - j) : nb;
+    phase_begin(kPhMixedPanel, s);
+    for (int c = 0; c < jb; c += PW) {
+      const int w = (jb - c) < PW ? (jb - c) : PW;
+      const int r0 = j + c;
+      SL_TRY(launch_panel<float>(F, ldf, m, r0, r0, w, dipiv, ws, s));
+      const int kw = (m - r0) < w ? (m - r0) : w;
+      SL_TRY(laswp<float>(F, ldf, r0, r0 + kw, dipiv, j, r0, r0 + w, j + jb, s));
+      if (c + w < jb) {
+        SL_TRY((trsm_strip<float, false, false, true>(kw, jb - c - w, Fp(r0, r0), ldf,
+                                                       Fp(r0, r0 + w), ldf, s)));
+        if (r0 + kw < m)
+          SL_TRY(sgemm_simt(false, m - r0 - kw, jb - c - w, kw, -1.f, Fp(r0 + kw, r0), ldf,
+                            Fp(r0, r0 + w), ldf, Fp(r0 + kw, r0 + w), ldf, s));
+      }
+    }
+    SL_TRY(laswp<float>(F, ldf, j, j + jb, dipiv, 0, j, j + jb, n, s));
+    if (j + jb < n)
+      SL_TRY((trsm_strip<float, false, false, true>(jb, n - j - jb, Fp(j, j), ldf, Fp(j, j + jb),
+                                                     ldf, s)));
+    phase_end(kPhMixedPanel, s, 0.0, 0.0);
+    if (j + jb < n && j + jb < m) {
+      const int mr = m - j - jb, nr = n - j - jb;
+      phase_begin(kPhMixedGemm, s);
+      SL_TRY(lowp_pack(fmt, Fp(j + jb, j), ldf, mr, Fp(j, j + jb), ldf, nr, jb, mw.A16, mw.B16,
+                       mw.col_exp, s));
+      SL_TRY(lowp_gemm(fmt, mr, nr, jb, mw.A16, mw.B16, mw.col_exp, Fp(j + jb, j + jb), ldf,
+                       ws.status, s));
+      const int kp = lowp_kpad(jb) * lowp_kmult(fmt);
+      phase_end(kPhMixedGemm, s, 2.0 * mr * (double)nr * jb,
+                8.0 * (double)mr * nr + 2.0 * ((double)mr + nr) * kp);
+    }
+  }
+  return cudaGetLastError();
+}
+
+// Solve with the FP32 factors: Xf (n x nrhs, ld n) overwritten in place.
+static cudaError_t sgetrs_inplace(int n, int nrhs, const float* F, long long ldf, const int* perm,
+                                  float* Xf, float* tmp, cudaStream_t s) {
+  SL_TRY((permute_rows<float, float>(Xf, n, tmp, n, perm, n, nrhs, 0, s)));
+  SL_TRY(tri_solve<float>(true, false, true, n, nrhs, F, ldf, tmp, n, s));
+  SL_TRY(tri_solve<float>(false, false, false, n, nrhs, F, ldf, tmp, n, s));
+  return cudaMemcpyAsync(Xf, tmp, sizeof(float) * (size_t)n * nrhs, cudaMemcpyDeviceToDevice, s);
+}
+
+// out = (LU)^-1 r in FP64 via the FP32 factors: r scaled per column by a power
+// of two into FP32, solved, scaled back. beta = 0 overwrites, 1 accumulates.
+static cudaError_t precond_apply(int n, int ncols, const double* r, long long ldr, double beta,
+                                 double* out, long long ldo, const float* F, long long ldf,
+                                 const MixedWork& mw, cudaStream_t s) {
+  colmax_abs_kernel<<<ncols, 1024, 0, s>>>(r, ldr, n, mw.colmax);
+  scale_to_float_kernel<<<blocks_for((long long)n * ncols), 256, 0, s>>>(r, ldr, n, ncols,
+                                                                         mw.colmax, mw.Xf, n);
+  count_launches(2);
+  SL_TRY(sgetrs_inplace(n, ncols, F, ldf, mw.perm, mw.Xf, mw.Xtmp, s));
+  float_scaled_add_kernel<<<blocks_for((long long)n * ncols), 256, 0, s>>>(mw.Xf, n, n, ncols,
+                                                                           mw.colmax, beta, out, ldo);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+// R = B - A X (FP64) for ncols columns.
+static cudaError_t residual(int n, int ncols, const double* A, long long lda, const double* B,
+                            long long ldb, const double* X, long long ldx, double* R,
+                            cudaStream_t s) {
+  SL_TRY(cudaMemcpy2DAsync(R, n * sizeof(double), B, ldb * sizeof(double), n * sizeof(double),
+                           ncols, cudaMemcpyDeviceToDevice, s));
+  return gemm_update<double>(false, n, ncols, n, -1.0, A, lda, X, ldx, R, n, s);
+}
+
+// Scaled residual per column (host): ||r||/(||A|| ||x|| n eps).
+static cudaError_t scaled_residuals(int n, int ncols, const double* R, const double* X,
+                                    long long ldx, double anorm, const MixedWork& mw,
+                                    cudaStream_t s, std::vector<double>& out) {
+  colmax_abs_kernel<<<ncols, 1024, 0, s>>>(R, n, n, mw.colmax);
+  colmax_abs_kernel<<<ncols, 1024, 0, s>>>(X, ldx, n, mw.colmax + ncols);
+  count_launches(2);
+  std::vector<double> h(2 * (size_t)ncols);
+  SL_TRY(cudaMemcpyAsync(h.data(), mw.colmax, sizeof(double) * 2 * ncols, cudaMemcpyDeviceToHost, s));
+  SL_TRY(cudaStreamSynchronize(s));
+  const double eps = std::ldexp(1.0, -53);
+  out.resize(ncols);
+  for (int c = 0; c < ncols; ++c) out[c] = h[c] / (h[ncols + c] * anorm * eps * n);
+  return cudaSuccess;
+}
+
+// GMRES on (LU)^-1 A d = (LU)^-1 r for one column; d overwritten (starts 0).
+// Returns the number of inner iterations in *its.
+static cudaError_t gmres_column(int n, const double* A, long long lda, const double* r, double* d,
+                                const float* F, long long ldf, const MixedWork& mw, int mmax,
+                                double rtol, int* its, cudaStream_t s) {
+  double* V = mw.V;  // n x (mmax+1)
+  const long long ldv = n;
+  double* w = mw.w;
+  std::vector<double> H((size_t)(mmax + 1) * mmax, 0.0), cs(mmax), sn(mmax), g(mmax + 1, 0.0);
+  std::vector<double> hcol(mmax + 2);
+  *its = 0;
+  // v0 = M^-1 r / beta
+  SL_TRY(precond_apply(n, 1, r, n, 0.0, w, n, F, ldf, mw, s));
+  dots_kernel<<<1, 1024, 0, s>>>(w, n, n, 1, w, mw.h);
+  count_launches(1);
+  double beta2 = 0.0;
+  SL_TRY(cudaMemcpyAsync(&beta2, mw.h, sizeof(double), cudaMemcpyDeviceToHost, s));
+  SL_TRY(cudaStreamSynchronize(s));
+  const double beta = std::sqrt(beta2);
+  SL_TRY(cudaMemsetAsync(d, 0, sizeof(double) * n, s));
+  if (!(beta > 0.0) || !std::isfinite(beta)) return cudaSuccess;
+  SL_TRY(cudaMemcpyAsync(mw.h + mmax + 4, &beta, sizeof(double), cudaMemcpyHostToDevice, s));
+  scale_vec_kernel<<<blocks_for(n), 256, 0, s>>>(w, n, mw.h + mmax + 4, V);
+  count_launches(1);
+  g[0] = beta;
+  int k = 0;
+  for (; k < mmax; ++k) {
+    // w = M^-1 A v_k
+    SL_TRY(cudaMemsetAsync(mw.Ax, 0, sizeof(double) * n, s));
+    SL_TRY(gemm_update<double>(false, n, 1, n, 1.0, A, lda, V + (long long)k * ldv, ldv, mw.Ax, n, s));
+    SL_TRY(precond_apply(n, 1, mw.Ax, n, 0.0, w, n, F, ldf, mw, s));
+    // classical Gram-Schmidt, twice
+    std::fill(hcol.begin(), hcol.end(), 0.0);
+    for (int pass = 0; pass < 2; ++pass) {
+      dots_kernel<<<k + 1, 1024, 0, s>>>(V, ldv, n, k + 1, w, mw.h);
+      sub_vh_kernel<<<blocks_for(n), 256, 0, s>>>(V, ldv, n, k + 1, mw.h, w);
+      count_launches(2);
+      std::vector<double> hp(k + 1);
+      SL_TRY(cudaMemcpyAsync(hp.data(), mw.h, sizeof(double) * (k + 1), cudaMemcpyDeviceToHost, s));
+      SL_TRY(cudaStreamSynchronize(s));
+      for (int i = 0; i <= k; ++i) hcol[i] += hp[i];
+    }
+    dots_kernel<<<1, 1024, 0, s>>>(w, n, n, 1, w, mw.h);
+    count_launches(1);
+    double nw2 = 0.0;
+    SL_TRY(cudaMemcpyAsync(&nw2, mw.h, sizeof(double), cudaMemcpyDeviceToHost, s));
+    SL_TRY(cudaStreamSynchronize(s));
+    const double hk1 = std::sqrt(nw2);
+    hcol[k + 1] = hk1;
+    if (hk1 > 0.0 && std::isfinite(hk1)) {
+      SL_TRY(cudaMemcpyAsync(mw.h + mmax + 4, &hk1, sizeof(double), cudaMemcpyHostToDevice, s));
+      scale_vec_kernel<<<blocks_for(n), 256, 0, s>>>(w, n, mw.h + mmax + 4, V + (long long)(k + 1) * ldv);
+      count_launches(1);
+    }
+    // apply previous rotations, then a new one
+    for (int i = 0; i < k; ++i) {
+      double t = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
+      hcol[i + 1] = -sn[i] * hcol[i] + cs[i] * hcol[i + 1];
+      hcol[i] = t;
+    }
+    const double a = hcol[k], b = hcol[k + 1];
+    const double rr = std::hypot(a, b);
+    cs[k] = rr > 0 ? a / rr : 1.0;
+    sn[k] = rr > 0 ? b / rr : 0.0;
+    hcol[k] = rr;
+    hcol[k + 1] = 0.0;
+    g[k + 1] = -sn[k] * g[k];
+    g[k] = cs[k] * g[k];
+    for (int i = 0; i <= k; ++i) H[(size_t)i + (size_t)k * (mmax + 1)] = hcol[i];
+    *its = k + 1;
+    if (std::fabs(g[k + 1]) <= rtol * beta || !(hk1 > 0.0)) { ++k; break; }
+  }
+  // y = H(0:k,0:k)^-1 g ; d = V y
+  std::vector<double> y(k, 0.0);
+  for (int i = k - 1; i >= 0; --i) {
+    double t = g[i];
+    for (int j = i + 1; j < k; ++j) t -= H[(size_t)i + (size_t)j * (mmax + 1)] * y[j];
+    const double hii = H[(size_t)i + (size_t)i * (mmax + 1)];
+    y[i] = hii != 0.0 ? t / hii : 0.0;
+  }
+  if (k > 0) {
+    SL_TRY(cudaMemcpyAsync(mw.h, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    add_vy_kernel<<<blocks_for(n), 256, 0, s>>>(V, ldv, n, k, mw.h, d);
+    count_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t dgesv_ir_device(int n, int nrhs, double* dA, long long lda, const double* dB,
+                            long long ldb, double* dX, long long ldx, int* dipiv,
+                            const IrOptions& opt, IrStats* st, const LuWork& ws,
+                            const MixedWork& mw, cudaStream_t s) {
+  *st = IrStats();
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  cudaEventRecord(e0, s);
+  // ||A||_inf of the FP64 matrix (for the scaled residual)
+  rowsum_abs_kernel<<<blocks_for(n), 256, 0, s>>>(dA, lda, n, mw.w);
+  colmax_abs_kernel<<<1, 1024, 0, s>>>(mw.w, n, n, mw.colmax);
+  count_launches(2);
+  double anorm = 0.0;
+  SL_TRY(cudaMemcpyAsync(&anorm, mw.colmax, sizeof(double), cudaMemcpyDeviceToHost, s));
+  // FP32 working copy and low-precision factorization
+  d2s_kernel<<<4 * num_sms(), 256, 0, s>>>(dA, lda, n, n, mw.F, mw.ldf);
+  count_launches(1);
+  SL_TRY(sgetrf_mixed_device(n, mw.F, mw.ldf, dipiv, opt.nb, opt.fmt, ws, mw, s));
+  SL_TRY(perm_compose(dipiv, n, mw.perm, s));
+  int hstat[2] = {0, 0};
+  SL_TRY(cudaMemcpyAsync(hstat, ws.status, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  SL_TRY(cudaStreamSynchronize(s));
+  cudaEventRecord(e1, s);
+  st->anorm = anorm;
+  bool ok_factor = (hstat[0] == 0) && !(hstat[1] >= 0 && hstat[1] < n);
+  bool converged = false;
+  std::vector<double> sres, prev;
+  phase_begin(kPhRefine, s);
+  if (ok_factor) {
+    // x0 = (LU)^-1 b
+    SL_TRY(precond_apply(n, nrhs, dB, ldb, 0.0, dX, ldx, mw.F, mw.ldf, mw, s));
+    SL_TRY(residual(n, nrhs, dA, lda, dB, ldb, dX, ldx, mw.R, s));
+    SL_TRY(scaled_residuals(n, nrhs, mw.R, dX, ldx, anorm, mw, s, sres));
+    bool use_gmres = false;
+    for (int it = 0; it < opt.max_ir; ++it) {
+      double worst = *std::max_element(sres.begin(), sres.end());
+      if (std::isfinite(worst) && worst <= opt.tol) { converged = true; break; }
+      if (!prev.empty()) {
+        double pw = *std::max_element(prev.begin(), prev.end());
+        if (!(worst <= 0.5 * pw)) { use_gmres = true; break; }  // stalled
+      }
+      prev = sres;
+      SL_TRY(precond_apply(n, nrhs, mw.R, n, 1.0, dX, ldx, mw.F, mw.ldf, mw, s));
+      st->classical += 1;
+      SL_TRY(residual(n, nrhs, dA, lda, dB, ldb, dX, ldx, mw.R, s));
+      SL_TRY(scaled_residuals(n, nrhs, mw.R, dX, ldx, anorm, mw, s, sres));
+    }
+    if (!converged) {
+      double worst = *std::max_element(sres.begin(), sres.end());
+      converged = std::isfinite(worst) && worst <= opt.tol;
+      if (!converged) use_gmres = true;
+    }
+    if (use_gmres && !converged) {
+      prev.clear();
+      for (int outer = 0; outer < opt.max_gmres_outer; ++outer) {
+        double worst = *std::max_element(sres.begin(), sres.end());
+        if (std::isfinite(worst) && worst <= opt.tol) { converged = true; break; }
+        if (!prev.empty()) {
+          double pw = *std::max_element(prev.begin(), prev.end());
+          if (!(worst <= 0.9 * pw)) break;  // GMRES-IR stalled too
+        }
+        prev = sres;
+        for (int c = 0; c < nrhs; ++c) {
+          if (sres[c] <= opt.tol) continue;
+          int its = 0;
+          SL_TRY(gmres_column(n, dA, lda, mw.R + (long long)c * n, mw.D, mw.F, mw.ldf, mw,
+                              opt.gmres_m, opt.gmres_rtol, &its, s));
+          st->gmres_inner += its;
+          axpy1_kernel<<<blocks_for(n), 256, 0, s>>>(n, mw.D, dX + (long long)c * ldx);  // x_c += d
+          count_launches(1);
+        }
+        st->gmres_outer += 1;
+        SL_TRY(residual(n, nrhs, dA, lda, dB, ldb, dX, ldx, mw.R, s));
+        SL_TRY(scaled_residuals(n, nrhs, mw.R, dX, ldx, anorm, mw, s, sres));
+      }
+      if (!converged) {
+        double worst = *std::max_element(sres.begin(), sres.end());
+        converged = std::isfinite(worst) && worst <= opt.tol;
+      }
+    }
+  }
+  phase_end(kPhRefine, s, 0.0, 0.0);
+  if (!converged) {
+    // FP64 fallback with the DMMA path: on a copy of A when one was provided
+    // (A preserved, the residual is reported), else in place as LAPACK DSGESV
+    // does (A returns the FP64 factors).
+    st->fell_back = 1;
+    double* Af = dA;
+    long long ldaf = lda;
+    if (mw.Acopy) {
+      SL_TRY(cudaMemcpy2DAsync(mw.Acopy, mw.ldacopy * sizeof(double), dA, lda * sizeof(double),
+                               n * sizeof(double), n, cudaMemcpyDeviceToDevice, s));
+      Af = mw.Acopy;
+      ldaf = mw.ldacopy;
+    }
+    SL_TRY(dgetrf_device(n, n, Af, ldaf, dipiv, opt.nb_fp64, ws, s));
+    SL_TRY(cudaMemcpyAsync(hstat, ws.status, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    SL_TRY(cudaStreamSynchronize(s));
+    if (hstat[0] != 0) {
+      st->dev_status = hstat[0];
+    } else if (hstat[1] >= 0 && hstat[1] < n) {
+      st->info = hstat[1] + 1;
+    } else {
+      SL_TRY(cudaMemcpy2DAsync(dX, ldx * sizeof(double), dB, ldb * sizeof(double),
+                               n * sizeof(double), nrhs, cudaMemcpyDeviceToDevice, s));
+      SL_TRY(dgetrs_device('N', n, nrhs, Af, ldaf, dipiv, dX, ldx, ws, s));
+      if (mw.Acopy) {
+        SL_TRY(residual(n, nrhs, dA, lda, dB, ldb, dX, ldx, mw.R, s));
+        SL_TRY(scaled_residuals(n, nrhs, mw.R, dX, ldx, anorm, mw, s, sres));
+      } else {
+        sres.assign(nrhs, -1.0);  // A was overwritten: the residual is not available here
+      }
+    }
+  }
+  cudaEventRecord(e2, s);
+  SL_TRY(cudaEventSynchronize(e2));
+  float t1 = 0.f, t2 = 0.f;
+  cudaEventElapsedTime(&t1, e0, e1);
+  cudaEventElapsedTime(&t2, e1, e2);
+  st->factor_ms = t1;
+  st->refine_ms = t2;
+  st->sresid = sres.empty() ? -1.0 : *std::max_element(sres.begin(), sres.end());
+  st->converged = converged ? 1 : 0;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  return cudaGetLastError();
+}
+
+}  // namespace sl

@@ -234,15 +234,20 @@ lowp_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
       if (n0 + c0 >= n) break;  // warp-uniform
       float v[32];
       tmem_ld32(trow + (uint32_t)c0, v);
+      const int ncol = min(32, n - (n0 + c0));
+      // Batch the 32 column scales and the 32 C loads before any store so the
+      // loads are in flight together (C may alias nothing else, but the
+      // compiler cannot know that across the stores).
+      float cv[32], sc[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) sc[j] = (j < ncol) ? ldexpf(1.0f, __ldg(col_exp + n0 + c0 + j)) : 0.f;
+      float* cbase = C + (long long)row + (long long)(n0 + c0) * ldc;
       if (row < m) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int col = n0 + c0 + j;
-          if (col < n) {
-            float* cp = C + (long long)row + (long long)col * ldc;
-            *cp = fmaf(-v[j], ldexpf(1.0f, col_exp[col]), *cp);
-          }
-        }
+        for (int j = 0; j < 32; ++j) cv[j] = (j < ncol) ? cbase[(long long)j * ldc] : 0.f;
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (j < ncol) cbase[(long long)j * ldc] = fmaf(-v[j], sc[j], cv[j]);
       }
     }
   }
@@ -261,6 +266,14 @@ lowp_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
 }
 
 // ---- operand packing (FP32 working matrix -> 16-bit K-major operands) ------
+
+__device__ __forceinline__ unsigned short bf16_hi(float x) {
+  return __bfloat16_as_ushort(__float2bfloat16_rn(x));
+}
+__device__ __forceinline__ unsigned short bf16_lo(float x) {
+  float hi = __bfloat162float(__float2bfloat16_rn(x));
+  return __bfloat16_as_ushort(__float2bfloat16_rn(x - hi));
+}
 
 template <bool BF16>
 __device__ __forceinline__ unsigned short to16(float x) {
@@ -283,6 +296,64 @@ __global__ void pack_a_kernel(const float* __restrict__ L, long long lda, int m,
   for (int r = threadIdx.y; r < 32; r += 8) {
     int i = i0 + r, kk = k0 + threadIdx.x;
     if (i < m && kk < kpad) A16[(long long)i * kpad + kk] = to16<BF16>(t[threadIdx.x][r]);
+  }
+}
+
+// Split packing for the 3-term BF16 product (fmt "bf16x3"): with x = hi + lo
+// (both BF16), A*B ~= Ahi*Bhi + Ahi*Blo + Alo*Bhi, formed by one GEMM over a
+// K dimension of 3*kpad: A3 = [Ahi | Ahi | Alo], B3 = [Bhi | Blo | Bhi].
+__global__ void pack_a3_kernel(const float* __restrict__ L, long long lda, int m, int k, int kpad,
+                               unsigned short* A3) {
+  __shared__ float t[32][33];
+  const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    int kk = k0 + r, i = i0 + threadIdx.x;
+    t[r][threadIdx.x] = (i < m && kk < k) ? L[i + (long long)kk * lda] : 0.f;
+  }
+  __syncthreads();
+  const long long ld3 = 3LL * kpad;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    int i = i0 + r, kk = k0 + threadIdx.x;
+    if (i < m && kk < kpad) {
+      float x = t[threadIdx.x][r];
+      unsigned short h = bf16_hi(x), l = bf16_lo(x);
+      A3[(long long)i * ld3 + kk] = h;
+      A3[(long long)i * ld3 + kpad + kk] = h;
+      A3[(long long)i * ld3 + 2 * kpad + kk] = l;
+    }
+  }
+}
+
+__global__ void pack_b3_kernel(const float* __restrict__ U, long long ldu, int k, int n, int kpad,
+                               unsigned short* B3, int* col_exp) {
+  const int j = blockIdx.x;
+  if (j >= n) return;
+  __shared__ float s_max[32];
+  float mx = 0.f;
+  for (int kk = threadIdx.x; kk < k; kk += blockDim.x) mx = fmaxf(mx, fabsf(U[kk + (long long)j * ldu]));
+  for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    mx = threadIdx.x < (blockDim.x >> 5) ? s_max[threadIdx.x] : 0.f;
+    for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    if (threadIdx.x == 0) {
+      int e = 0;
+      if (mx > 0.f && isfinite(mx)) frexpf(mx, &e);
+      s_max[0] = __int_as_float(e);
+    }
+  }
+  __syncthreads();
+  const int e = __float_as_int(s_max[0]);
+  if (threadIdx.x == 0) col_exp[j] = e;
+  const float sc = ldexpf(1.0f, -e);
+  const long long ld3 = 3LL * kpad;
+  for (int kk = threadIdx.x; kk < kpad; kk += blockDim.x) {
+    float x = kk < k ? U[kk + (long long)j * ldu] * sc : 0.f;
+    unsigned short h = bf16_hi(x), l = bf16_lo(x);
+    B3[(long long)j * ld3 + kk] = h;
+    B3[(long long)j * ld3 + kpad + kk] = l;
+    B3[(long long)j * ld3 + 2 * kpad + kk] = h;
   }
 }
 
@@ -351,10 +422,25 @@ size_t lowp_gemm_smem_bytes() {
 
 int lowp_kpad(int k) { return (k + BK - 1) / BK * BK; }
 
-cudaError_t lowp_pack(bool bf16, const float* L, long long lda, int m, const float* U,
+int lowp_kmult(int fmt) { return fmt == 2 ? 3 : 1; }
+
+cudaError_t lowp_pack(int fmt, const float* L, long long lda, int m, const float* U,
                       long long ldu, int n, int k, unsigned short* A16, unsigned short* B16,
                       int* col_exp, cudaStream_t s) {
   const int kpad = lowp_kpad(k);
+  if (fmt == 2) {
+    if (m > 0) {
+      dim3 g((m + 31) / 32, (kpad + 31) / 32), b(32, 8);
+      pack_a3_kernel<<<g, b, 0, s>>>(L, lda, m, k, kpad, A16);
+      count_launches(1);
+    }
+    if (n > 0) {
+      pack_b3_kernel<<<n, 128, 0, s>>>(U, ldu, k, n, kpad, B16, col_exp);
+      count_launches(1);
+    }
+    return cudaGetLastError();
+  }
+  const bool bf16 = (fmt == 0);
   if (m > 0) {
     dim3 g((m + 31) / 32, (kpad + 31) / 32), b(32, 8);
     if (bf16) pack_a_kernel<true><<<g, b, 0, s>>>(L, lda, m, k, kpad, A16);
@@ -369,11 +455,12 @@ cudaError_t lowp_pack(bool bf16, const float* L, long long lda, int m, const flo
   return cudaGetLastError();
 }
 
-cudaError_t lowp_gemm(bool bf16, int m, int n, int k, const unsigned short* A16,
+cudaError_t lowp_gemm(int fmt, int m, int n, int k, const unsigned short* A16,
                       const unsigned short* B16, const int* col_exp, float* C, long long ldc,
                       int* status, cudaStream_t s) {
   if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
-  const int kpad = lowp_kpad(k);
+  const bool bf16 = (fmt != 1);
+  const int kpad = lowp_kpad(k) * lowp_kmult(fmt);
   CUtensorMap ta, tb;
   if (!make_map(&ta, A16, m, kpad, BM) || !make_map(&tb, B16, n, kpad, BN))
     return cudaErrorInvalidResourceHandle;

@@ -77,15 +77,62 @@ cudaError_t dgetrs_device(char trans, int n, int nrhs, const double* dA, long lo
 // ---- low-precision trailing update (mixed_gemm.cu) ----
 // Pack L21 (m x k FP32 col-major) and U12 (k x n FP32 col-major, per-column
 // power-of-two scaled) into 16-bit K-major operands of k rounded up to 64.
+// fmt: 0 BF16, 1 FP16, 2 BF16x3 (hi/lo split, 3 products along a K of 3*kpad).
 int lowp_kpad(int k);
+int lowp_kmult(int fmt);
 size_t lowp_gemm_smem_bytes();
-cudaError_t lowp_pack(bool bf16, const float* L, long long lda, int m, const float* U,
+cudaError_t lowp_pack(int fmt, const float* L, long long lda, int m, const float* U,
                       long long ldu, int n, int k, unsigned short* A16, unsigned short* B16,
                       int* col_exp, cudaStream_t s);
 // C (m x n FP32 col-major) -= (A16 B16^T) .* 2^col_exp (tcgen05, FP32 accumulate).
-cudaError_t lowp_gemm(bool bf16, int m, int n, int k, const unsigned short* A16,
+cudaError_t lowp_gemm(int fmt, int m, int n, int k, const unsigned short* A16,
                       const unsigned short* B16, const int* col_exp, float* C, long long ldc,
                       int* status, cudaStream_t s);
+
+// ---- mixed-precision LU-IR (mixed.cu) ----
+struct MixedWork {
+  float* F = nullptr;          // FP32 working matrix, n x n, leading dimension ldf
+  long long ldf = 0;
+  unsigned short* A16 = nullptr;  // 16-bit GEMM operands (rows x kpad)
+  unsigned short* B16 = nullptr;
+  int* col_exp = nullptr;      // per-column exponents of U12
+  int* perm = nullptr;         // composed pivot permutation (n)
+  double* R = nullptr;         // residuals n x nrhs
+  double* D = nullptr;         // GMRES correction (n)
+  float* Xf = nullptr;         // FP32 right-hand sides n x nrhs
+  float* Xtmp = nullptr;       // n x nrhs
+  double* colmax = nullptr;    // 2*nrhs + 8
+  double* V = nullptr;         // Krylov basis n x (gmres_m + 1)
+  double* w = nullptr;         // n
+  double* Ax = nullptr;        // n
+  double* h = nullptr;         // gmres_m + 8
+  double* Acopy = nullptr;     // optional FP64 copy of A for the fallback (keeps A)
+  long long ldacopy = 0;
+};
+struct IrOptions {
+  int fmt = 0;              // 0: BF16 trailing update, 1: FP16, 2: BF16x3 split
+  int nb = 256;             // block size of the low-precision factorization
+  int nb_fp64 = 256;        // block size of the FP64 fallback
+  int max_ir = 10;          // classical refinement steps
+  int max_gmres_outer = 10; // GMRES-IR outer steps
+  int gmres_m = 100;        // GMRES iterations per outer step
+  double gmres_rtol = 1e-10;
+  double tol = 1.0;         // target scaled residual
+};
+struct IrStats {
+  int classical = 0, gmres_outer = 0, gmres_inner = 0, fell_back = 0, converged = 0;
+  int info = 0, dev_status = 0;
+  double sresid = 0.0, anorm = 0.0, factor_ms = 0.0, refine_ms = 0.0;
+};
+cudaError_t sgetrf_mixed_device(int n, float* F, long long ldf, int* dipiv, int nb, int fmt,
+                                const LuWork& ws, const MixedWork& mw, cudaStream_t s);
+cudaError_t dgesv_ir_device(int n, int nrhs, double* dA, long long lda, const double* dB,
+                            long long ldb, double* dX, long long ldx, int* dipiv,
+                            const IrOptions& opt, IrStats* st, const LuWork& ws,
+                            const MixedWork& mw, cudaStream_t s);
+
+// perm[i] = original row ending in row i after the n interchanges i <-> ipiv[i].
+cudaError_t perm_compose(const int* dipiv, int n, int* perm, cudaStream_t s);
 
 // dst[i] = src[i] + delta, n entries (device arrays).
 cudaError_t ipiv_shift(const int* src, int* dst, int n, int delta, cudaStream_t s);

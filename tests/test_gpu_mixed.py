@@ -13,17 +13,28 @@ pytestmark = pytest.mark.gpu
 
 
 def _ref_update(torch, C, L, U, fmt):
-    dt = torch.bfloat16 if fmt == 0 else torch.float16
     mx = U.abs().amax(dim=0)
     e = torch.where(mx > 0, torch.frexp(mx)[1], torch.zeros_like(mx, dtype=torch.int32))
-    Us = (U * torch.ldexp(torch.ones_like(mx), -e)).to(dt).double()
+    Usc = U * torch.ldexp(torch.ones_like(mx), -e)
+    scale = torch.ldexp(torch.ones_like(mx, dtype=torch.float64), e.int())
+    if fmt == 2:  # BF16x3: hi*hi + hi*lo + lo*hi
+        def split(x):
+            hi = x.to(torch.bfloat16).float()
+            return hi.double(), (x - hi).to(torch.bfloat16).double()
+        Lh, Ll = split(L)
+        Uh, Ul = split(Usc)
+        prod = Lh @ Uh + Lh @ Ul + Ll @ Uh
+        bound = Lh.abs() @ Uh.abs() + Lh.abs() @ Ul.abs() + Ll.abs() @ Uh.abs()
+        return C.double() - prod * scale, bound * scale
+    dt = torch.bfloat16 if fmt == 0 else torch.float16
+    Us = Usc.to(dt).double()
     L16 = L.to(dt).double()
-    prod = (L16 @ Us) * torch.ldexp(torch.ones_like(mx, dtype=torch.float64), e.to(torch.float64).int())
-    bound = (L16.abs() @ Us.abs()) * torch.ldexp(torch.ones_like(mx, dtype=torch.float64), e.int())
+    prod = (L16 @ Us) * scale
+    bound = (L16.abs() @ Us.abs()) * scale
     return C.double() - prod, bound
 
 
-@pytest.mark.parametrize("fmt", [0, 1])
+@pytest.mark.parametrize("fmt", [0, 1, 2])
 @pytest.mark.parametrize("m,n,k", [(128, 256, 64), (1000, 700, 256), (300, 20, 100), (4096, 4096, 256),
                                    (129, 257, 512), (7, 3, 16)])
 def test_lowp_update_matches_reference(sl, gpu_required, fmt, m, n, k):
@@ -44,3 +55,65 @@ def test_lowp_update_matches_reference(sl, gpu_required, fmt, m, n, k):
     err = (got - ref).abs()
     tol = 4.0 * k * 2.0 ** -23 * bound + 2.0 ** -22 * ref.abs() + 1e-30
     assert bool((err <= tol).all()), float((err / tol).max())
+
+
+def _dev_colmajor(torch, M):
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(M).T)).cuda()
+
+
+def _solve_ir(sl, torch, A0, B0, fmt, tol=1.0, nb=256):
+    n, nrhs = A0.shape[0], B0.shape[1]
+    dA = _dev_colmajor(torch, A0)
+    dB = _dev_colmajor(torch, B0)
+    dX = torch.zeros_like(dB)
+    dpiv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    info, it, st = sl.dgesv_ir_dev(n, nrhs, dA.data_ptr(), n, dpiv.data_ptr(), dB.data_ptr(), n,
+                                   dX.data_ptr(), n, fmt=fmt, nb=nb, tol=tol, keep_a=True)
+    A_after = dA.cpu().numpy().T
+    return info, it, st, np.asfortranarray(dX.cpu().numpy().T), A_after
+
+
+@pytest.mark.parametrize("fmt", ["bf16", "fp16", "bf16x3"])
+@pytest.mark.parametrize("n,nrhs,nb", [(64, 1, 32), (1000, 2, 256), (2500, 1, 256), (700, 3, 128)])
+def test_mixed_ir_reaches_fp64_backward_error(sl, orc, gpu_required, fmt, n, nrhs, nb):
+    import torch
+    from lu_helpers import system
+
+    A0, B0 = system(orc, n, nrhs)
+    info, it, st, X, A_after = _solve_ir(sl, torch, A0, B0, fmt, nb=nb)
+    assert info == 0
+    np.testing.assert_array_equal(A_after, A0)  # keep_a: A untouched
+    sr = orc.sresid(A0, B0, X)  # the FP64 oracle's scaled residual
+    assert sr < 16.0
+    assert st["sresid"] <= 1.0 + 1e-9 or st["fell_back"] == 1
+    assert st["fell_back"] == 0, st
+    assert it >= 0
+
+
+@pytest.mark.parametrize("kappa", [1e2, 1e4, 1e6, 1e8])
+def test_mixed_ir_conditioning_sweep(sl, orc, gpu_required, kappa):
+    # A = U diag(s) V^T with seeded Householder reflectors, s geometric 1 -> 1/kappa
+    import torch
+
+    n, nrhs = 384, 4
+    A0 = orc.gen_conditioned(n, kappa, nrefl=16, seed=1000)
+    B0 = orc.matgen(n, nrhs, 200, kind=0)  # uniform (-1, 1]
+    for fmt in ("bf16", "bf16x3"):
+        info, it, st, X, _ = _solve_ir(sl, torch, A0, B0, fmt, nb=64)
+        assert info == 0
+        assert orc.sresid(A0, B0, X) < 16.0  # refinement or the FP64 fallback, never worse
+        if kappa <= 1e2 or (fmt == "bf16x3" and kappa <= 1e4):
+            assert st["fell_back"] == 0, (fmt, st)
+
+
+def test_mixed_ir_singular_falls_back_and_reports_info(sl, orc, gpu_required):
+    import torch
+    from lu_helpers import system
+
+    n = 200
+    A0, B0 = system(orc, n, 1)
+    A0[:, 17] = 0.0
+    info, it, st, X, _ = _solve_ir(sl, torch, A0, B0, "bf16", nb=64)
+    assert info == 18
+    assert st["fell_back"] == 1 and it == -1
