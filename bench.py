@@ -51,6 +51,11 @@ def parse():
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--mixed-n", type=int, default=32768,
+                   help="size of the mixed-precision LU-IR comparison (0 disables it)")
+    p.add_argument("--mixed-fmts", default="bf16x3,fp16,bf16")
+    p.add_argument("--batch", type=int, default=4096,
+                   help="systems in the batched-solver comparison (0 disables it)")
     return p.parse_args()
 
 
@@ -149,6 +154,125 @@ def cpu_solve_sample(A, B, nb, budget_s=25.0):
             "sample": f"oracle PDGESV restatement (OpenBLAS, {cores} threads), N={n} NB={nb} "
                       f"NRHS={B.shape[1]}, one solve of {dt:.2f} s",
             "blas_loaded": orc.blas_loaded(), "seconds": dt, "n": n}
+
+
+def torch_sresid(torch, A, B, X):
+    """Tester scaled residual max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf N eps), FP64."""
+    n = A.shape[0]
+    R = B - A @ X
+    anorm = A.abs().sum(dim=1).max()
+    return float((R.abs().amax(dim=0) / (X.abs().amax(dim=0) * anorm * 2.0 ** -53 * n)).max())
+
+
+def mixed_section(sl, torch, dev, args, stream):
+    """Config: mixed-precision LU-IR at N=mixed_n, NRHS=1, A and B iid U[-0.5,0.5] FP64,
+    against the plain FP64 GPU solve of the same system (time-to-solution, device-resident)."""
+    n = args.mixed_n
+    g = torch.Generator(device=dev).manual_seed(args.seed + 17)
+    At = torch.rand((n, n), dtype=torch.float64, device=dev, generator=g) - 0.5  # column-major A^T view
+    Bt = torch.rand((1, n), dtype=torch.float64, device=dev, generator=g) - 0.5
+    A, B = At.T, Bt.T
+    out = {"workload": f"mixed-precision LU-IR N={n} NRHS=1, A,B iid U[-0.5,0.5] FP64 "
+                       "(torch Philox seed), tol: scaled residual <= 1", "n": n, "runs": {}}
+    piv = torch.zeros(n, dtype=torch.int32, device=dev)
+    Xt = torch.zeros_like(Bt)
+    # small warm-up so that workspace growth and first-launch costs are outside the timings
+    w = n
+    sl.dgesv_ir_dev(w, 1, At.data_ptr(), n, piv.data_ptr(), Bt.data_ptr(), n, Xt.data_ptr(), n,
+                    fmt="bf16x3", keep_a=True, stream=stream.cuda_stream)
+    for fmt in [f for f in args.mixed_fmts.split(",") if f]:
+        Xt.zero_()
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        info, it, st = sl.dgesv_ir_dev(n, 1, At.data_ptr(), n, piv.data_ptr(), Bt.data_ptr(), n,
+                                       Xt.data_ptr(), n, fmt=fmt, nb=256, tol=1.0, keep_a=True,
+                                       stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        out["runs"][fmt] = {"info": info, "iter": it, "time_to_solution_ms": ms,
+                            "factor_ms": st["factor_ms"], "refine_ms": st["refine_ms"],
+                            "classical_steps": int(st["classical"]),
+                            "gmres_outer": int(st["gmres_outer"]),
+                            "gmres_inner": int(st["gmres_inner"]),
+                            "fell_back_to_fp64": bool(st["fell_back"]),
+                            "sresid": torch_sresid(torch, A, B, Xt.T),
+                            "tflops_2n3_3": 2.0 * n ** 3 / 3.0 / (ms * 1e-3) / 1e12}
+    # plain FP64 GPU solve of the same system
+    Ac = At.clone()
+    Bc = Bt.clone()
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    info = sl.dgesv_dev(n, 1, Ac.data_ptr(), n, piv.data_ptr(), Bc.data_ptr(), n, 256,
+                        stream=stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms64 = e0.elapsed_time(e1)
+    out["fp64"] = {"info": info, "time_to_solution_ms": ms64, "sresid": torch_sresid(torch, A, B, Bc.T),
+                   "tflops_2n3_3": 2.0 * n ** 3 / 3.0 / (ms64 * 1e-3) / 1e12}
+    for fmt, r in out["runs"].items():
+        r["time_ratio_vs_fp64"] = r["time_to_solution_ms"] / ms64
+        r["meets_target"] = bool(r["sresid"] < 16.0 and r["time_ratio_vs_fp64"] <= 1.0 / 3.0)
+    del Ac, Bc, At, Bt
+    torch.cuda.empty_cache()
+    return out
+
+
+def batched_section(sl, torch, dev, args, stream):
+    """Config: 4096 independent FP64 systems, N ~ U{16..512}, NRHS ~ U{1..8}, entries
+    U[-0.5,0.5] plus a diagonal shift N/4 on half the batch; FP64 and FP32-factor +
+    FP64-IR plans, each executed as one CUDA graph of persistent launches."""
+    rng = np.random.default_rng(args.seed + 5)
+    count = args.batch
+    ns = rng.integers(16, 513, size=count)
+    rs = rng.integers(1, 9, size=count)
+    g = torch.Generator(device=dev).manual_seed(args.seed + 5)
+    dA, dB, dX = [], [], []
+    for i in range(count):
+        n, r = int(ns[i]), int(rs[i])
+        a = torch.rand((n, n), dtype=torch.float64, device=dev, generator=g) - 0.5
+        if i % 2 == 0:
+            a.diagonal().add_(n / 4.0)
+        dA.append(a)
+        dB.append(torch.rand((r, n), dtype=torch.float64, device=dev, generator=g) - 0.5)
+        dX.append(torch.zeros((r, n), dtype=torch.float64, device=dev))
+    systems = [(dA[i].data_ptr(), int(ns[i]), int(ns[i]), dB[i].data_ptr(), int(ns[i]), int(rs[i]),
+                dX[i].data_ptr(), int(ns[i])) for i in range(count)]
+    flops = float(sum(2.0 * int(n) ** 3 / 3.0 for n in ns))
+    out = {"workload": f"{count} systems, N~U{{16..512}}, NRHS~U{{1..8}}, U[-0.5,0.5] "
+                       "+ N/4 diagonal shift on half (torch Philox seed)",
+           "systems": count, "sum_2n3_3_gflop": flops / 1e9, "modes": {}}
+    for mode, name in ((0, "fp64"), (1, "fp32_factor_fp64_ir")):
+        t0 = time.perf_counter()
+        plan = sl.BatchPlan(systems, mode=mode, tol=1.0, autotune=True, stream=stream.cuda_stream)
+        plan_s = time.perf_counter() - t0
+        for _ in range(2):
+            plan.execute()
+        reps = 5
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            plan.execute()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / reps
+        info, its, sr = plan.results()
+        srv = np.array(sr)
+        itv = np.array(its)
+        out["modes"][name] = {
+            "solves_per_s": count / (ms * 1e-3), "ms_per_batch": ms,
+            "tflops_2n3_3": flops / (ms * 1e-3) / 1e12, "plan_create_s": plan_s,
+            "shape": plan.shape(), "nonzero_info": int(np.count_nonzero(info)),
+            "sresid_max": float(srv.max()), "sresid_median": float(np.median(srv)),
+            "refine_steps_mean": float(itv[itv >= 0].mean()) if mode == 1 else 0.0,
+            "fp64_pass_systems": int(np.count_nonzero(itv == -1)) if mode == 1 else 0}
+        plan.close()
+    del dA, dB, dX
+    torch.cuda.empty_cache()
+    return out
 
 
 def dist_init(args):
@@ -337,6 +461,13 @@ def run_gpu(args):
         cpu = cpu_solve_sample(A, B, nb)
         cpu.pop("n", None)
 
+    mixed = None
+    if args.mixed_n > 0:
+        mixed = mixed_section(sl, torch, dev, args, stream)
+    batched = None
+    if args.batch > 0:
+        batched = batched_section(sl, torch, dev, args, stream)
+
     # cuBLAS DGEMM yardstick (run and timed only, never on the product path)
     yard = None
     try:
@@ -367,6 +498,8 @@ def run_gpu(args):
             "gpu_launches": launches,
             "accuracy": {"sresid": sresid, "threshold": 16.0},
             "phases": phase_summary,
+            "mixed_ir": mixed,
+            "batched": batched,
             "yardstick_cublas_dgemm_tflops": yard,
         }
         print(json.dumps(line), flush=True)

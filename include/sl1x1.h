@@ -109,6 +109,30 @@ int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, 
                        long long lddb, double* dX, long long lddx, int fmt, int nb, double tol,
                        int keep_a, int* iter, double* stats, void* stream);
 
+/* ---- Batched solver (no single routine of the reference; each system is a
+ * PDGESV on a 1x1 grid). A plan describes `batch` independent systems
+ * A_i X_i = B_i with 1 <= n[i] <= 512 and 1 <= nrhs[i] <= 8, each A_i, B_i,
+ * X_i a column-major device array (host arrays of device pointers and leading
+ * dimensions). A_i and B_i are not modified. mode 0 factors and solves in
+ * FP64; mode 1 factors in FP32 and refines in FP64 until the scaled residual
+ * ||b-Ax||/(||A|| ||x|| n eps) <= tol (tol <= 0: 1.0), re-solving in FP64 any
+ * system that does not get there in 10 steps. Plan creation sorts the systems
+ * by size, allocates the workspace, optionally autotunes the kernel shape
+ * (threads per CTA, GEMM column chunk, CTAs per SM) on this batch, and
+ * captures the execution (one persistent launch per pass) in a CUDA graph.
+ * Results per system: INFO (> 0: exactly singular), refinement steps (-1:
+ * solved by the FP64 pass after refinement stalled) and the scaled residual. */
+typedef struct sl1x1_batch_plan_s* sl1x1_batch_plan;
+int sl1x1_batch_plan_create(sl1x1_batch_plan* plan, int batch, const int* n, const int* nrhs,
+                            const double* const* dA, const int* lda, const double* const* dB,
+                            const int* ldb, double* const* dX, const int* ldx, int mode, double tol,
+                            int autotune, void* stream);
+int sl1x1_batch_plan_execute(sl1x1_batch_plan plan, void* stream);
+int sl1x1_batch_plan_results(sl1x1_batch_plan plan, int* info, int* iters, double* sresid,
+                             void* stream);
+int sl1x1_batch_plan_shape(sl1x1_batch_plan plan, int* threads, int* chunk, int* ctas_per_sm);
+void sl1x1_batch_plan_destroy(sl1x1_batch_plan plan);
+
 /* Allocation-free FP64 LU (no counterpart in the reference): the same
  * factorization, pivots and INFO as sl1x1_dgetrf_dev, for callers that may not
  * allocate GPU memory (memory pools or arenas that own the device heap,

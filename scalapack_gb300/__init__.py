@@ -82,6 +82,15 @@ def lib(build_if_missing: bool = False):
                                      C.c_longlong, C.c_int, C.c_int, C.c_double, C.c_int,
                                      C.POINTER(C.c_int), C.POINTER(C.c_double), vp]
     L.sl1x1_dgesv_ir_dev.restype = C.c_int
+    L.sl1x1_batch_plan_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, vp, vp, vp, vp, vp, vp,
+                                          vp, vp, C.c_int, C.c_double, C.c_int, vp]
+    L.sl1x1_batch_plan_create.restype = C.c_int
+    L.sl1x1_batch_plan_execute.argtypes = [vp, vp]
+    L.sl1x1_batch_plan_execute.restype = C.c_int
+    L.sl1x1_batch_plan_results.argtypes = [vp, vp, vp, vp, vp]
+    L.sl1x1_batch_plan_results.restype = C.c_int
+    L.sl1x1_batch_plan_shape.argtypes = [vp, vp, vp, vp]
+    L.sl1x1_batch_plan_destroy.argtypes = [vp]
     L.sl1x1_finalize.argtypes = []
     L.sl1x1_set_default_nb.argtypes = [C.c_int]
     L.sl1x1_device_ok.restype = C.c_int
@@ -234,6 +243,54 @@ def dgesv_ir_dev(n, nrhs, a_ptr, ldda, ipiv_ptr, b_ptr, lddb, x_ptr, lddx, fmt="
                                     float(tol), 1 if keep_a else 0, C.byref(it), st,
                                     _stream_ptr(stream))
     return info, it.value, dict(zip(IR_STATS, list(st)))
+
+
+class BatchPlan:
+    """Batched solver plan over device arrays (torch tensors or raw pointers).
+
+    systems: list of (a_ptr, lda, n, b_ptr, ldb, nrhs, x_ptr, ldx); mode 0 = FP64,
+    1 = FP32 factors + FP64 refinement. execute() replays the captured CUDA graph.
+    """
+
+    def __init__(self, systems, mode=0, tol=1.0, autotune=True, stream=None):
+        k = len(systems)
+        I = C.c_int * k
+        P = C.c_void_p * k
+        self.batch = k
+        self._keep = (I(*[s[2] for s in systems]), I(*[s[5] for s in systems]),
+                      P(*[s[0] for s in systems]), I(*[s[1] for s in systems]),
+                      P(*[s[3] for s in systems]), I(*[s[4] for s in systems]),
+                      P(*[s[6] for s in systems]), I(*[s[7] for s in systems]))
+        n, r, a, lda, b, ldb, x, ldx = self._keep
+        self.plan = C.c_void_p()
+        info = lib().sl1x1_batch_plan_create(C.byref(self.plan), k, n, r, a, lda, b, ldb, x, ldx,
+                                             mode, float(tol), 1 if autotune else 0,
+                                             _stream_ptr(stream))
+        if info != 0:
+            raise RuntimeError(f"sl1x1_batch_plan_create INFO={info}")
+        self.stream = stream
+
+    def execute(self):
+        info = lib().sl1x1_batch_plan_execute(self.plan, _stream_ptr(self.stream))
+        if info != 0:
+            raise RuntimeError(f"sl1x1_batch_plan_execute INFO={info}")
+
+    def results(self):
+        info = (C.c_int * self.batch)()
+        its = (C.c_int * self.batch)()
+        sr = (C.c_double * self.batch)()
+        lib().sl1x1_batch_plan_results(self.plan, info, its, sr, _stream_ptr(self.stream))
+        return list(info), list(its), list(sr)
+
+    def shape(self):
+        t, c, s = C.c_int(), C.c_int(), C.c_int()
+        lib().sl1x1_batch_plan_shape(self.plan, C.byref(t), C.byref(c), C.byref(s))
+        return {"threads": t.value, "chunk": c.value, "ctas_per_sm": s.value}
+
+    def close(self):
+        if self.plan:
+            lib().sl1x1_batch_plan_destroy(self.plan)
+            self.plan = C.c_void_p()
 
 
 def dgetrs_dev(trans, n, nrhs, a_ptr, ldda, ipiv_ptr, b_ptr, lddb, stream=None) -> int:

@@ -683,6 +683,56 @@ int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, 
   return st.info;
 }
 
+int sl1x1_batch_plan_create(sl1x1_batch_plan* plan, int batch, const int* n, const int* nrhs,
+                            const double* const* dA, const int* lda, const double* const* dB,
+                            const int* ldb, double* const* dX, const int* ldx, int mode, double tol,
+                            int autotune, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!plan) return -1;
+  *plan = nullptr;
+  if (batch < 0) return -2;
+  for (int i = 0; i < batch; ++i) {
+    if (n[i] < 1 || n[i] > 512) return -3;
+    if (nrhs[i] < 1 || nrhs[i] > 8) return -4;
+    if (lda[i] < n[i]) return -6;
+    if (ldb[i] < n[i]) return -8;
+    if (ldx[i] < n[i]) return -10;
+  }
+  if (mode != 0 && mode != 1) return -11;
+  if (!ensure_device()) return cuda_info(cudaErrorNoDevice);
+  sl::BatchPlan* p = nullptr;
+  cudaError_t e = sl::batch_plan_create(&p, batch, n, nrhs, dA, lda, dB, ldb, dX, ldx, mode, tol,
+                                        autotune, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_info(e);
+  *plan = reinterpret_cast<sl1x1_batch_plan>(p);
+  return 0;
+}
+
+int sl1x1_batch_plan_execute(sl1x1_batch_plan plan, void* stream) {
+  if (!plan) return -1;
+  cudaError_t e = sl::batch_plan_execute(reinterpret_cast<sl::BatchPlan*>(plan), (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  return e == cudaSuccess ? 0 : cuda_info(e);
+}
+
+int sl1x1_batch_plan_results(sl1x1_batch_plan plan, int* info, int* iters, double* sresid,
+                             void* stream) {
+  if (!plan) return -1;
+  cudaError_t e = sl::batch_plan_results(reinterpret_cast<sl::BatchPlan*>(plan), info, iters,
+                                         sresid, (cudaStream_t)stream);
+  return e == cudaSuccess ? 0 : cuda_info(e);
+}
+
+int sl1x1_batch_plan_shape(sl1x1_batch_plan plan, int* threads, int* chunk, int* ctas_per_sm) {
+  if (!plan) return -1;
+  sl::batch_plan_shape(reinterpret_cast<sl::BatchPlan*>(plan), threads, chunk, ctas_per_sm);
+  return 0;
+}
+
+void sl1x1_batch_plan_destroy(sl1x1_batch_plan plan) {
+  sl::batch_plan_destroy(reinterpret_cast<sl::BatchPlan*>(plan));
+}
+
 void sl1x1_finalize(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   release_all();

@@ -433,12 +433,6 @@ inline cudaError_t permute_rows(const TS* src, long long lds, TD* dst, long long
   return cudaGetLastError();
 }
 
-#define SL_TRY(x)                     \
-  do {                                \
-    cudaError_t _e = (x);             \
-    if (_e != cudaSuccess) return _e; \
-  } while (0)
-
 // C += alpha op(A) B for the off-diagonal blocks of the solves (defined per
 // type: FP64 in lu_f64.cu with DMMA for wide B, FP32 in mixed.cu).
 template <typename T>

@@ -3,6 +3,14 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 
+#ifndef SL_TRY
+#define SL_TRY(x)                     \
+  do {                                \
+    cudaError_t _e = (x);             \
+    if (_e != cudaSuccess) return _e; \
+  } while (0)
+#endif
+
 namespace sl {
 
 int num_sms();
@@ -130,6 +138,18 @@ cudaError_t dgesv_ir_device(int n, int nrhs, double* dA, long long lda, const do
                             long long ldb, double* dX, long long ldx, int* dipiv,
                             const IrOptions& opt, IrStats* st, const LuWork& ws,
                             const MixedWork& mw, cudaStream_t s);
+
+// ---- batched solver (batched.cu) ----
+struct BatchPlan;
+cudaError_t batch_plan_create(BatchPlan** out, int batch, const int* n, const int* nrhs,
+                              const double* const* A, const int* lda, const double* const* B,
+                              const int* ldb, double* const* X, const int* ldx, int mode,
+                              double tol, int autotune, cudaStream_t s);
+cudaError_t batch_plan_execute(BatchPlan* p, cudaStream_t s);
+cudaError_t batch_plan_results(BatchPlan* p, int* info, int* iters, double* sresid,
+                               cudaStream_t s);
+void batch_plan_shape(const BatchPlan* p, int* threads, int* chunk, int* ctas);
+void batch_plan_destroy(BatchPlan* p);
 
 // perm[i] = original row ending in row i after the n interchanges i <-> ipiv[i].
 cudaError_t perm_compose(const int* dipiv, int n, int* perm, cudaStream_t s);
