@@ -149,6 +149,11 @@ int sl1x1_dgetrf_noalloc(int m, int n, double* dA, long long ldda, int* dipiv, i
 void sl1x1_finalize(void);
 /* Block size NB used by the device entry points when nb <= 0 (default 256). */
 void sl1x1_set_default_nb(int nb);
+/* Smallest row slice per CTA of the cooperative panel kernel (8..768,
+ * default 64, i.e. one CTA per SM for tall panels): larger slices mean fewer
+ * CTAs per per-column grid barrier but more serial work per CTA. Changes only
+ * the speed, not the results. */
+void sl1x1_set_panel_rows(int rows);
 /* 1 if the library found a usable sm_103 device, else 0. */
 int sl1x1_device_ok(void);
 /* Version string. */

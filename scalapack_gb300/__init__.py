@@ -93,6 +93,7 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_batch_plan_destroy.argtypes = [vp]
     L.sl1x1_finalize.argtypes = []
     L.sl1x1_set_default_nb.argtypes = [C.c_int]
+    L.sl1x1_set_panel_rows.argtypes = [C.c_int]
     L.sl1x1_device_ok.restype = C.c_int
     L.sl1x1_version.restype = C.c_char_p
     L.sl1x1_prof_enable.argtypes = [C.c_int]
@@ -188,7 +189,7 @@ def pdgesv(n, nrhs, a, ia, ja, desca, ipiv, b, ib, jb, descb) -> int:
 
 # ------------------------------------------------------------ phase timers
 PHASES = ["panel", "laswp", "trsm", "gemm", "solve", "mixed_gemm", "mixed_panel", "refine",
-          "batched"]
+          "batched", "residual", "precond"]
 
 
 def prof_enable(on: bool = True):

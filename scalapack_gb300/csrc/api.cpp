@@ -152,6 +152,9 @@ struct DevState {
   double* dAx = nullptr; size_t capAx = 0;
   double* dh = nullptr; size_t capH = 0;
   double* dAcopy = nullptr; size_t capAcopy = 0;
+  int* dchain = nullptr; size_t capChain = 0;
+  double* dsplitk = nullptr; size_t capSplitk = 0;
+  int chain_epoch = 0;
   unsigned short* dA16 = nullptr; size_t capA16 = 0;
   unsigned short* dB16 = nullptr; size_t capB16 = 0;
   int* dcolexp = nullptr; size_t capCe = 0;
@@ -201,6 +204,8 @@ void release_all() {
   cudaFree(g_dev.dF); cudaFree(g_dev.dpermx); cudaFree(g_dev.dR); cudaFree(g_dev.dD);
   cudaFree(g_dev.dXf); cudaFree(g_dev.dXt); cudaFree(g_dev.dcm); cudaFree(g_dev.dV);
   cudaFree(g_dev.dw); cudaFree(g_dev.dAx); cudaFree(g_dev.dh); cudaFree(g_dev.dAcopy);
+  cudaFree(g_dev.dchain); cudaFree(g_dev.dsplitk);
+  sl::splitk_scratch() = sl::SplitKScratch();
   if (g_dev.stream) cudaStreamDestroy(g_dev.stream);
   g_dev = DevState();
 }
@@ -657,6 +662,19 @@ int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, 
   GROW(dperm, capPerm, n);
   GROW(dbswap, capBs, (size_t)n * nrhs);
   if (keep_a) GROW(dAcopy, capAcopy, (size_t)ldf * n);
+  GROW(dsplitk, capSplitk, (size_t)32 * 4 * n);  // split-K partials of the FP64 products
+  if (e == cudaSuccess) {
+    sl::splitk_scratch().ptr = g_dev.dsplitk;
+    sl::splitk_scratch().bytes = g_dev.capSplitk * sizeof(double);
+  }
+  {
+    const size_t need = (size_t)(n + 63) / 64 + 8;
+    if (need > g_dev.capChain || !g_dev.dchain) {
+      GROW(dchain, capChain, need);
+      if (e == cudaSuccess) e = cudaMemsetAsync(g_dev.dchain, 0, sizeof(int) * g_dev.capChain, s);
+      g_dev.chain_epoch = 0;  // fresh flags
+    }
+  }
 #undef GROW
   if (e != cudaSuccess) return cuda_info(e);
   sl::MixedWork mw;
@@ -666,6 +684,9 @@ int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, 
   mw.Xf = g_dev.dXf; mw.Xtmp = g_dev.dXt; mw.colmax = g_dev.dcm;
   mw.V = g_dev.dV; mw.w = g_dev.dw; mw.Ax = g_dev.dAx; mw.h = g_dev.dh;
   mw.Acopy = keep_a ? g_dev.dAcopy : nullptr; mw.ldacopy = ldf;
+  mw.chain = g_dev.dchain; mw.epoch = &g_dev.chain_epoch; mw.status = g_dev.dsmall + 4;
+  if (e == cudaSuccess) e = cudaMemsetAsync(mw.status, 0, sizeof(int), s);
+  if (e != cudaSuccess) return cuda_info(e);
   sl::LuWork w = make_work();
   sl::IrStats st;
   e = sl::dgesv_ir_device(n, nrhs, dA, ldda, dB, lddb, dX, lddx, g_dev.dipiv == nullptr ? dipiv : dipiv,
@@ -736,6 +757,11 @@ void sl1x1_batch_plan_destroy(sl1x1_batch_plan plan) {
 void sl1x1_finalize(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   release_all();
+}
+
+void sl1x1_set_panel_rows(int rows) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  sl::set_panel_min_rows(rows);
 }
 
 void sl1x1_set_default_nb(int nb) {

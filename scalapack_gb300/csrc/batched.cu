@@ -390,7 +390,7 @@ __device__ void run_system(const BatchArgs& a, int sys, bool fp64_pass, unsigned
     __syncthreads();
     return;
   }
-  if (sizeof(TF) == 8) {
+  if constexpr (sizeof(TF) == 8) {
     // FP64: X = B, solve, residual
     for (int idx = tid; idx < n * nrhs; idx += NT) {
       int i = idx % n, c = idx / n;
@@ -406,58 +406,59 @@ __device__ void run_system(const BatchArgs& a, int sys, bool fp64_pass, unsigned
     }
     __syncthreads();
     return;
-  }
-  // FP32 factors + FP64 refinement.
-  for (int idx = tid; idx < n * nrhs; idx += NT) {
-    int i = idx % n, c = idx / n;
-    X[i + (long long)c * ldx] = 0.0;
-  }
-  __syncthreads();
-  // initial residual r = b (x = 0)
-  double sr = residual_system(A, lda, n, B, ldb, X, ldx, nrhs, Rs, s_red);
-  int steps = 0;
-  if (tid == 0) s_ok = 0;
-  __syncthreads();
-  for (int it = 0; it <= kMaxIr; ++it) {
-    if (it > 0 && sr <= a.tol) { if (tid == 0) s_ok = 1; break; }
-    if (it == kMaxIr) break;
-    // correction: scale each residual column by a power of two into FP32, solve
-    __shared__ int s_exp[kBMaxRhs];
-    if (tid < nrhs) {
-      double mx = 0.0;
-      for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(Rs[i + tid * n]));
-      int e = 0;
-      if (mx > 0.0 && isfinite(mx)) frexp(mx, &e);
-      s_exp[tid] = e;
-    }
-    __syncthreads();
-    // copy the scaled residual into an FP32 buffer laid out like X (ld = n)
-    TF* Cx = Xs + n * nrhs;  // second half of the Xs region (n*nrhs <= 4096 floats)
+  } else {
+    // FP32 factors + FP64 refinement.
     for (int idx = tid; idx < n * nrhs; idx += NT) {
       int i = idx % n, c = idx / n;
-      Cx[i + c * n] = (TF)ldexp(Rs[i + c * n], -s_exp[c]);
+      X[i + (long long)c * ldx] = 0.0;
     }
     __syncthreads();
-    solve_system<TF>(W, n, ipiv, Cx, n, nrhs, Xs, perm);
-    for (int idx = tid; idx < n * nrhs; idx += NT) {
-      int i = idx % n, c = idx / n;
-      X[i + (long long)c * ldx] += ldexp((double)Cx[i + c * n], s_exp[c]);
+    // initial residual r = b (x = 0)
+    double sr = residual_system(A, lda, n, B, ldb, X, ldx, nrhs, Rs, s_red);
+    int steps = 0;
+    if (tid == 0) s_ok = 0;
+    __syncthreads();
+    for (int it = 0; it <= kMaxIr; ++it) {
+      if (it > 0 && sr <= a.tol) { if (tid == 0) s_ok = 1; break; }
+      if (it == kMaxIr) break;
+      // correction: scale each residual column by a power of two into FP32, solve
+      __shared__ int s_exp[kBMaxRhs];
+      if (tid < nrhs) {
+        double mx = 0.0;
+        for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(Rs[i + tid * n]));
+        int e = 0;
+        if (mx > 0.0 && isfinite(mx)) frexp(mx, &e);
+        s_exp[tid] = e;
+      }
+      __syncthreads();
+      // copy the scaled residual into an FP32 buffer laid out like X (ld = n)
+      TF* Cx = Xs + n * nrhs;  // second half of the Xs region (n*nrhs <= 4096 floats)
+      for (int idx = tid; idx < n * nrhs; idx += NT) {
+        int i = idx % n, c = idx / n;
+        Cx[i + c * n] = (TF)ldexp(Rs[i + c * n], -s_exp[c]);
+      }
+      __syncthreads();
+      solve_system<TF>(W, n, ipiv, Cx, n, nrhs, Xs, perm);
+      for (int idx = tid; idx < n * nrhs; idx += NT) {
+        int i = idx % n, c = idx / n;
+        X[i + (long long)c * ldx] += ldexp((double)Cx[i + c * n], s_exp[c]);
+      }
+      __syncthreads();
+      ++steps;
+      sr = residual_system(A, lda, n, B, ldb, X, ldx, nrhs, Rs, s_red);
+    }
+    if (s_ok) {
+      if (tid == 0) {
+        a.info[sys] = 0;
+        a.iters[sys] = steps;
+        a.sresid[sys] = sr;
+      }
+    } else if (tid == 0) {
+      int slot = atomicAdd(&a.queue[2], 1);
+      a.fallback_list[slot] = sys;
     }
     __syncthreads();
-    ++steps;
-    sr = residual_system(A, lda, n, B, ldb, X, ldx, nrhs, Rs, s_red);
   }
-  if (s_ok) {
-    if (tid == 0) {
-      a.info[sys] = 0;
-      a.iters[sys] = steps;
-      a.sresid[sys] = sr;
-    }
-  } else if (tid == 0) {
-    int slot = atomicAdd(&a.queue[2], 1);
-    a.fallback_list[slot] = sys;
-  }
-  __syncthreads();
 }
 
 template <typename TF, int CH>

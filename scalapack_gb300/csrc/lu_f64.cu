@@ -33,6 +33,15 @@ static_assert(kPanelCandDoubles == (size_t)2 * PMAXG * (PW + 2) + 2 * PW, "slot 
 // rounded down to a multiple of 8: 768 rows; one CTA per SM.
 int panel_max_rows() { return num_sms() * 768; }
 
+static int g_panel_min_rows = 64;
+int panel_min_rows() { return g_panel_min_rows; }
+void set_panel_min_rows(int rows) { g_panel_min_rows = rows < 8 ? 8 : (rows > 768 ? 768 : rows); }
+
+SplitKScratch& splitk_scratch() {
+  static SplitKScratch sc;
+  return sc;
+}
+
 // dst[i] = src[i] + delta (pivot base conversion at the C ABI).
 __global__ void ipiv_shift_kernel(const int* __restrict__ src, int* dst, int n, int delta) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -288,6 +288,149 @@ trsv_warp_kernel(int w, int ncols, const T* __restrict__ Tm, long long ldt, T* B
   }
 }
 
+// Single-launch blocked triangular solve for few right-hand sides (nrhs <=
+// NRM): FORWARD solves with the unit-lower L, otherwise with the non-unit
+// upper U, of an n x n LU factor, X (n x nrhs) overwritten in place.
+//
+// Each CTA takes the next 64-row block (in solve order) from an atomic
+// ticket, so every block it depends on belongs to a CTA that has already
+// started: the waits below always end (no residency assumption). It stages
+// its diagonal block in shared memory, then consumes the solved blocks in
+// order as their flags reach `epoch`: the block's x is read through L2 and the
+// 64x64 off-diagonal block of the factor is applied by 4 thread groups of 64
+// rows x 16 columns. The diagonal solve is one warp per right-hand side with
+// shuffles. Waits are bounded (kSpinLimit); on timeout the CTA records
+// kFlagTimeout in *status and stops.
+template <typename T, bool FORWARD, int NRM>
+__global__ void __launch_bounds__(256)
+trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long ldx, int nrhs,
+                  int* ticket, int* flags, int epoch, int* status) {
+  constexpr int KB = 64;
+  __shared__ T Ds[KB][KB + 1];          // diagonal block, Ds[r][i] = A(r0+r, r0+i)
+  __shared__ T xs[8 * KB][NRM];         // x of the dependency blocks being applied
+  __shared__ T part[4][KB][NRM];        // partial sums of the 4 column groups
+  __shared__ int s_b, s_fail;
+  const int tid = threadIdx.x;
+  const int nblk = (n + KB - 1) / KB;
+  if (tid == 0) { s_b = atomicAdd(ticket, 1); s_fail = 0; }
+  __syncthreads();
+  const int sidx = s_b;
+  if (sidx >= nblk) return;
+  const int b = FORWARD ? sidx : nblk - 1 - sidx;
+  const int r0 = b * KB, rb = min(KB, n - r0);
+  for (int idx = tid; idx < KB * KB; idx += 256) {
+    int r = idx % KB, i = idx / KB;
+    Ds[r][i] = (r < rb && i < rb) ? A[(r0 + r) + (long long)(r0 + i) * lda] : (T)0;
+  }
+  const int r = tid & (KB - 1), q = tid >> 6;
+  T acc[NRM];
+#pragma unroll
+  for (int c = 0; c < NRM; ++c) acc[c] = (T)0;
+  // Consume the solved blocks in solve order, as many at a time as have
+  // already been published (up to kChunk), so a late CTA streams through the
+  // finished part of the factor with few synchronizations.
+  constexpr int kChunk = 8;
+  __shared__ int s_avail;
+  int t = 0;
+  while (t < sidx) {
+    if (tid == 0) {
+      const int kb0 = FORWARD ? t : nblk - 1 - t;
+      long long spins = 0;
+      while (ld_acquire_gpu(&flags[kb0]) != epoch) {
+        if (++spins > kSpinLimit) { atomicExch(status, (int)kFlagTimeout); s_fail = 1; break; }
+        if (spins > 32) __nanosleep(32);
+      }
+      int av = 1;
+      while (!s_fail && av < kChunk && t + av < sidx) {
+        const int kbn = FORWARD ? t + av : nblk - 1 - (t + av);
+        if (ld_acquire_gpu(&flags[kbn]) != epoch) break;
+        ++av;
+      }
+      s_avail = av;
+    }
+    __syncthreads();
+    if (s_fail) return;
+    const int av = s_avail;
+    // rows of X covered by the chunk: blocks t..t+av-1 in solve order are
+    // contiguous in the matrix (increasing for forward, decreasing backward)
+    const int kfirst = FORWARD ? t : nblk - 1 - (t + av - 1);
+    const int k0 = kfirst * KB;
+    const int kn = min(av * KB, n - k0);
+    for (int idx = tid; idx < kn * nrhs; idx += 256) {
+      int i = idx % kn, c = idx / kn;
+      xs[i][c] = __ldcg(&X[(k0 + i) + (long long)c * ldx]);
+    }
+    __syncthreads();
+    if (r < rb) {
+      // thread group q takes every 4th group of 16 columns of the chunk
+      for (int g0 = q * 16; g0 < kn; g0 += 64) {
+        const int g1 = min(g0 + 16, kn);
+        for (int kk = g0; kk < g1; ++kk) {
+          const T a = A[(r0 + r) + (long long)(k0 + kk) * lda];
+#pragma unroll
+          for (int c = 0; c < NRM; ++c)
+            if (c < nrhs) acc[c] = fma(a, xs[kk][c], acc[c]);
+        }
+      }
+    }
+    __syncthreads();
+    t += av;
+  }
+#pragma unroll
+  for (int c = 0; c < NRM; ++c) part[q][r][c] = acc[c];
+  __syncthreads();
+  // v = b - sum of the partials, diagonal solve: warp c owns column c, lanes own rows lane, lane+32
+  const int warp = tid >> 5, lane = tid & 31;
+  for (int c = warp; c < nrhs; c += 8) {
+    T x0 = (T)0, x1 = (T)0;
+    if (lane < rb)
+      x0 = X[(r0 + lane) + (long long)c * ldx] - (part[0][lane][c] + part[1][lane][c] + part[2][lane][c] + part[3][lane][c]);
+    if (lane + 32 < rb)
+      x1 = X[(r0 + lane + 32) + (long long)c * ldx] -
+           (part[0][lane + 32][c] + part[1][lane + 32][c] + part[2][lane + 32][c] + part[3][lane + 32][c]);
+    for (int s = 0; s < rb; ++s) {
+      const int i = FORWARD ? s : rb - 1 - s;
+      const int li = i & 31;
+      const bool hi = i >= 32;
+      if (!FORWARD && lane == li) {
+        if (hi) x1 = x1 / Ds[i][i];
+        else x0 = x0 / Ds[i][i];
+      }
+      const T xi = __shfl_sync(0xffffffffu, hi ? x1 : x0, li);
+      if (FORWARD) {
+        if (lane > i) x0 = fma(-Ds[lane][i], xi, x0);
+        if (lane + 32 > i) x1 = fma(-Ds[lane + 32][i], xi, x1);
+      } else {
+        if (lane < i) x0 = fma(-Ds[lane][i], xi, x0);
+        if (lane + 32 < i) x1 = fma(-Ds[lane + 32][i], xi, x1);
+      }
+    }
+    if (lane < rb) X[(r0 + lane) + (long long)c * ldx] = x0;
+    if (lane + 32 < rb) X[(r0 + lane + 32) + (long long)c * ldx] = x1;
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) st_release_gpu(&flags[b], epoch);
+}
+
+// Launch the chained solve; `sync` holds 1 ticket int followed by one flag per
+// 64-row block (flags start at 0; epoch must differ from every earlier one).
+template <typename T, bool FORWARD>
+inline cudaError_t trsv_chain(const T* A, long long lda, int n, T* X, long long ldx, int nrhs,
+                              int* sync, int epoch, int* status, cudaStream_t s) {
+  if (n <= 0 || nrhs <= 0) return cudaSuccess;
+  const int nblk = (n + 63) / 64;
+  SL_TRY(cudaMemsetAsync(sync, 0, sizeof(int), s));
+  if (nrhs <= 1)
+    trsv_chain_kernel<T, FORWARD, 1><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, sync, sync + 1, epoch, status);
+  else if (nrhs <= 4)
+    trsv_chain_kernel<T, FORWARD, 4><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, sync, sync + 1, epoch, status);
+  else
+    trsv_chain_kernel<T, FORWARD, 8><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, sync, sync + 1, epoch, status);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 // dst(i, c) = src(perm[i], c) (forward) or dst(perm[i], c) = src(i, c) (inverse).
 template <typename TS, typename TD>
 __global__ void permute_rows_kernel(const TS* __restrict__ src, long long lds, TD* dst,
@@ -345,8 +488,11 @@ inline cudaError_t launch_panel(T* A, long long lda, int m, int r0, int c0, int 
                                 const LuWork& ws, cudaStream_t s) {
   const int R = m - r0;
   const int nsm = num_sms();
+  // Rows per CTA: at least kPanelMinRows so that the per-column grid barrier
+  // and the candidate exchange involve few CTAs (the panel is latency-bound:
+  // a column's arithmetic is small next to one barrier round trip).
   int rpc = (R + nsm - 1) / nsm;
-  if (rpc < 64) rpc = 64;
+  if (rpc < panel_min_rows()) rpc = panel_min_rows();
   rpc = (rpc + 7) & ~7;
   const int G = (R + rpc - 1) / rpc;
   const size_t smem = sizeof(T) * (size_t)rpc * PLD;
@@ -405,12 +551,91 @@ inline cudaError_t launch_skinny(int m, int n, int k, T alpha, const T* A, long 
   return cudaGetLastError();
 }
 
+// Split-K form for long k (matrix-vector products of the refinement): CTA
+// (bx, by) computes rows 256*bx.. of op(A)[:, kslice(by)] * B into its own
+// partial slot; gemm_skinny_reduce adds the ksplit partials in a fixed order.
+template <typename T, int NC>
+__global__ void __launch_bounds__(256)
+gemm_skinny_splitk_kernel(int m, int n, int k, int kslice, const T* __restrict__ A, long long lda,
+                          const T* __restrict__ B, long long ldb, T* part) {
+  __shared__ T Bs[64][NC];
+  const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int kbeg = blockIdx.y * kslice, kend = min(k, kbeg + kslice);
+  T acc[2][NC];
+#pragma unroll
+  for (int j = 0; j < NC; ++j) { acc[0][j] = (T)0; acc[1][j] = (T)0; }
+  for (int k0 = kbeg; k0 < kend; k0 += 64) {
+    const int kc = min(64, kend - k0);
+    __syncthreads();
+    for (int c = threadIdx.x; c < 64 * NC; c += blockDim.x) {
+      int kk = c % 64, nn = c / 64;
+      Bs[kk][nn] = (kk < kc && nn < n) ? B[(k0 + kk) + (long long)nn * ldb] : (T)0;
+    }
+    __syncthreads();
+    if (row < m) {
+      int kk = 0;
+      for (; kk + 1 < kc; kk += 2) {  // two independent accumulator chains
+        const T a0 = A[row + (long long)(k0 + kk) * lda];
+        const T a1 = A[row + (long long)(k0 + kk + 1) * lda];
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+          acc[0][j] = fma(a0, Bs[kk][j], acc[0][j]);
+          acc[1][j] = fma(a1, Bs[kk + 1][j], acc[1][j]);
+        }
+      }
+      if (kk < kc) {
+        const T a0 = A[row + (long long)(k0 + kk) * lda];
+#pragma unroll
+        for (int j = 0; j < NC; ++j) acc[0][j] = fma(a0, Bs[kk][j], acc[0][j]);
+      }
+    }
+  }
+  if (row < m) {
+#pragma unroll
+    for (int j = 0; j < NC; ++j)
+      if (j < n) part[((long long)blockIdx.y * n + j) * m + row] = acc[0][j] + acc[1][j];
+  }
+}
+
+template <typename T>
+__global__ void gemm_skinny_reduce_kernel(int m, int n, int ksplit, T alpha, const T* part, T* C,
+                                          long long ldc) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)m * n) return;
+  const int row = (int)(idx % m), j = (int)(idx / m);
+  T s = (T)0;
+  for (int q = 0; q < ksplit; ++q) s += part[((long long)q * n + j) * m + row];
+  C[row + (long long)j * ldc] += alpha * s;
+}
+
 // C += alpha * op(A) * B for n <= 16 columns.
 template <typename T>
 inline cudaError_t gemm_skinny(bool transa, int m, int n, int k, T alpha, const T* A,
                                long long lda, const T* B, long long ldb, T* C, long long ldc,
                                cudaStream_t s) {
   if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
+  if (!transa && n <= 4 && k >= 4096) {
+    // long products: spread k over ksplit CTA columns so every SM works
+    const int rb = (m + 255) / 256;
+    int ksplit = (4 * num_sms() + rb - 1) / rb;
+    if (ksplit > 32) ksplit = 32;
+    if (ksplit > 1) {
+      SplitKScratch& sc = splitk_scratch();
+      const size_t need = sizeof(T) * (size_t)ksplit * n * m;
+      if (sc.ptr && sc.bytes >= need) {
+        const int kslice = ((k + ksplit - 1) / ksplit + 63) / 64 * 64;
+        ksplit = (k + kslice - 1) / kslice;
+        dim3 grid(rb, ksplit);
+        T* part = reinterpret_cast<T*>(sc.ptr);
+        if (n == 1) gemm_skinny_splitk_kernel<T, 1><<<grid, 256, 0, s>>>(m, n, k, kslice, A, lda, B, ldb, part);
+        else gemm_skinny_splitk_kernel<T, 4><<<grid, 256, 0, s>>>(m, n, k, kslice, A, lda, B, ldb, part);
+        const long long tot = (long long)m * n;
+        gemm_skinny_reduce_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(m, n, ksplit, alpha, part, C, ldc);
+        count_launches(2);
+        return cudaGetLastError();
+      }
+    }
+  }
 #define SL_SK(NC)                                                                              \
   return transa ? launch_skinny<T, true, NC>(m, n, k, alpha, A, lda, B, ldb, C, ldc, s)        \
                 : launch_skinny<T, false, NC>(m, n, k, alpha, A, lda, B, ldb, C, ldc, s)

@@ -275,11 +275,19 @@ cudaError_t sgetrf_mixed_device(int n, float* F, long long ldf, int* dipiv, int 
 }
 
 // Solve with the FP32 factors: Xf (n x nrhs, ld n) overwritten in place.
+// Up to 8 right-hand sides use the single-launch chained solves.
 static cudaError_t sgetrs_inplace(int n, int nrhs, const float* F, long long ldf, const int* perm,
-                                  float* Xf, float* tmp, cudaStream_t s) {
+                                  float* Xf, float* tmp, const MixedWork& mw, cudaStream_t s) {
   SL_TRY((permute_rows<float, float>(Xf, n, tmp, n, perm, n, nrhs, 0, s)));
-  SL_TRY(tri_solve<float>(true, false, true, n, nrhs, F, ldf, tmp, n, s));
-  SL_TRY(tri_solve<float>(false, false, false, n, nrhs, F, ldf, tmp, n, s));
+  if (nrhs <= 8 && mw.chain && mw.epoch) {
+    *mw.epoch += 1;
+    SL_TRY((trsv_chain<float, true>(F, ldf, n, tmp, n, nrhs, mw.chain, *mw.epoch, mw.status, s)));
+    *mw.epoch += 1;
+    SL_TRY((trsv_chain<float, false>(F, ldf, n, tmp, n, nrhs, mw.chain, *mw.epoch, mw.status, s)));
+  } else {
+    SL_TRY(tri_solve<float>(true, false, true, n, nrhs, F, ldf, tmp, n, s));
+    SL_TRY(tri_solve<float>(false, false, false, n, nrhs, F, ldf, tmp, n, s));
+  }
   return cudaMemcpyAsync(Xf, tmp, sizeof(float) * (size_t)n * nrhs, cudaMemcpyDeviceToDevice, s);
 }
 
@@ -288,14 +296,16 @@ static cudaError_t sgetrs_inplace(int n, int nrhs, const float* F, long long ldf
 static cudaError_t precond_apply(int n, int ncols, const double* r, long long ldr, double beta,
                                  double* out, long long ldo, const float* F, long long ldf,
                                  const MixedWork& mw, cudaStream_t s) {
+  phase_begin(kPhPrecond, s);
   colmax_abs_kernel<<<ncols, 1024, 0, s>>>(r, ldr, n, mw.colmax);
   scale_to_float_kernel<<<blocks_for((long long)n * ncols), 256, 0, s>>>(r, ldr, n, ncols,
                                                                          mw.colmax, mw.Xf, n);
   count_launches(2);
-  SL_TRY(sgetrs_inplace(n, ncols, F, ldf, mw.perm, mw.Xf, mw.Xtmp, s));
+  SL_TRY(sgetrs_inplace(n, ncols, F, ldf, mw.perm, mw.Xf, mw.Xtmp, mw, s));
   float_scaled_add_kernel<<<blocks_for((long long)n * ncols), 256, 0, s>>>(mw.Xf, n, n, ncols,
                                                                            mw.colmax, beta, out, ldo);
   count_launches(1);
+  phase_end(kPhPrecond, s, 2.0 * (double)n * n * ncols, 4.0 * (double)n * n);
   return cudaGetLastError();
 }
 
@@ -303,9 +313,12 @@ static cudaError_t precond_apply(int n, int ncols, const double* r, long long ld
 static cudaError_t residual(int n, int ncols, const double* A, long long lda, const double* B,
                             long long ldb, const double* X, long long ldx, double* R,
                             cudaStream_t s) {
+  phase_begin(kPhResidual, s);
   SL_TRY(cudaMemcpy2DAsync(R, n * sizeof(double), B, ldb * sizeof(double), n * sizeof(double),
                            ncols, cudaMemcpyDeviceToDevice, s));
-  return gemm_update<double>(false, n, ncols, n, -1.0, A, lda, X, ldx, R, n, s);
+  SL_TRY(gemm_update<double>(false, n, ncols, n, -1.0, A, lda, X, ldx, R, n, s));
+  phase_end(kPhResidual, s, 2.0 * (double)n * n * ncols, 8.0 * (double)n * n);
+  return cudaSuccess;
 }
 
 // Scaled residual per column (host): ||r||/(||A|| ||x|| n eps).
@@ -352,8 +365,10 @@ static cudaError_t gmres_column(int n, const double* A, long long lda, const dou
   int k = 0;
   for (; k < mmax; ++k) {
     // w = M^-1 A v_k
+    phase_begin(kPhResidual, s);
     SL_TRY(cudaMemsetAsync(mw.Ax, 0, sizeof(double) * n, s));
     SL_TRY(gemm_update<double>(false, n, 1, n, 1.0, A, lda, V + (long long)k * ldv, ldv, mw.Ax, n, s));
+    phase_end(kPhResidual, s, 2.0 * (double)n * n, 8.0 * (double)n * n);
     SL_TRY(precond_apply(n, 1, mw.Ax, n, 0.0, w, n, F, ldf, mw, s));
     // classical Gram-Schmidt, twice
     std::fill(hcol.begin(), hcol.end(), 0.0);
@@ -496,6 +511,12 @@ cudaError_t dgesv_ir_device(int n, int nrhs, double* dA, long long lda, const do
     }
   }
   phase_end(kPhRefine, s, 0.0, 0.0);
+  if (mw.status) {
+    int cst = 0;
+    SL_TRY(cudaMemcpyAsync(&cst, mw.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SL_TRY(cudaStreamSynchronize(s));
+    if (cst != 0) { st->dev_status = cst; return cudaSuccess; }
+  }
   if (!converged) {
     // FP64 fallback with the DMMA path: on a copy of A when one was provided
     // (A preserved, the residual is reported), else in place as LAPACK DSGESV

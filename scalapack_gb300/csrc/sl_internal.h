@@ -26,7 +26,9 @@ enum Phase {
   kPhMixedPanel = 6, // FP32 panel, swaps and solves of the mixed factorization
   kPhRefine = 7,     // FP64 residuals, corrections and GMRES of the refinement
   kPhBatched = 8,    // batched solver
-  kNumPhases = 9
+  kPhResidual = 9,   // FP64 residuals and matrix-vector products of the refinement
+  kPhPrecond = 10,   // low-precision solves applied during the refinement
+  kNumPhases = 11
 };
 void count_launches(int n);
 void phase_begin(int phase, cudaStream_t s);
@@ -34,6 +36,14 @@ void phase_end(int phase, cudaStream_t s, double flops, double bytes);
 void prof_enable(bool on);
 bool prof_read(int phase, long long* launches, double* ms, double* flops, double* bytes);
 long long launch_count();
+
+// Scratch for the split-K partials of long skinny products (grown by the
+// library with the refinement workspace; a null pointer disables split-K).
+struct SplitKScratch {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+SplitKScratch& splitk_scratch();
 
 // Register-only DMMA throughput loop (FP64 tensor peak calibration), TFLOP/s.
 double dmma_peak_tflops(cudaStream_t s);
@@ -62,6 +72,9 @@ size_t panel_cand_doubles();
 constexpr size_t kPanelCandDoubles = (size_t)2 * 1024 * (32 + 2) + 2 * 32;
 // Largest M the FP64 panel supports on this device (rows held in shared memory).
 int panel_max_rows();
+// Smallest row slice per CTA of the cooperative panel (tunable, default 512).
+int panel_min_rows();
+void set_panel_min_rows(int rows);
 // Block size used when a caller passes nb <= 0.
 int default_nb();
 // While an instance lives on a thread, phase timers record nothing on it
@@ -116,6 +129,9 @@ struct MixedWork {
   double* h = nullptr;         // gmres_m + 8
   double* Acopy = nullptr;     // optional FP64 copy of A for the fallback (keeps A)
   long long ldacopy = 0;
+  int* chain = nullptr;        // ticket + per-block flags of the chained solves (n/64 + 8)
+  int* epoch = nullptr;        // host-side counter of chained-solve epochs
+  int* status = nullptr;       // device status word
 };
 struct IrOptions {
   int fmt = 0;              // 0: BF16 trailing update, 1: FP16, 2: BF16x3 split
