@@ -46,6 +46,27 @@ void pdgesv_(const int* N, const int* NRHS, double* A, const int* IA, const int*
              const int* DESCA, int* IPIV, double* B, const int* IB, const int* JB,
              const int* DESCB, int* INFO);
 
+/* ---- Routines on the LU factors ------------------------------------------ */
+
+/* Replaces PDLANGE, SRC/pdlange.f:1: 'M' max |a|, '1'/'O' max column sum,
+ * 'I' max row sum, 'F'/'E' Frobenius norm of sub(A), computed on the GPU
+ * (NaN if no GPU is usable). */
+double pdlange_(const char* NORM, const int* M, const int* N, const double* A, const int* IA,
+                const int* JA, const int* DESCA, double* WORK, size_t NORM_len);
+
+/* Replaces PDGECON, SRC/pdgecon.f:1-2: reciprocal condition number estimate
+ * (1-norm or infinity-norm) from the LU factors of PDGETRF, with the same
+ * validation, workspace query (LWORK/LIWORK = -1) and quick returns. */
+void pdgecon_(const char* NORM, const int* N, const double* A, const int* IA, const int* JA,
+              const int* DESCA, const double* ANORM, double* RCOND, double* WORK,
+              const int* LWORK, int* IWORK, const int* LIWORK, int* INFO, size_t NORM_len);
+
+/* Replaces PDGETRI, SRC/pdgetri.f:1-2: inverse of sub(A) from the LU factors
+ * and pivots of PDGETRF; INFO = i > 0 when U(i,i) is exactly zero. */
+void pdgetri_(const int* N, double* A, const int* IA, const int* JA, const int* DESCA,
+              const int* IPIV, double* WORK, const int* LWORK, int* IWORK, const int* LIWORK,
+              int* INFO);
+
 /* ---- TOOLS used by callers of the LU path ------------------------------- */
 
 /* Replaces DESCINIT, TOOLS/descinit.f:1-192. */
@@ -143,6 +164,13 @@ void sl1x1_batch_plan_destroy(sl1x1_batch_plan plan);
  * M above 152 SMs x 768 rows is rejected with -30000 before any launch. */
 int sl1x1_dgetrf_noalloc(int m, int n, double* dA, long long ldda, int* dipiv, int nb,
                          void* stream);
+
+/* Device forms of PDLANGE, PDGECON and PDGETRI (dipiv 1-based, as returned
+ * by sl1x1_dgetrf_dev). dgecon/dgetri return INFO. */
+double sl1x1_dlange_dev(char norm, int m, int n, const double* dA, long long ldda, void* stream);
+int sl1x1_dgecon_dev(char norm, int n, const double* dLU, long long ldda, double anorm,
+                     double* rcond, void* stream);
+int sl1x1_dgetri_dev(int n, double* dA, long long ldda, const int* dipiv, void* stream);
 
 /* ---- Library control ----------------------------------------------------- */
 /* Free every device buffer the library holds (also done by blacs_exit_). */

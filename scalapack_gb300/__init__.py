@@ -91,6 +91,20 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_batch_plan_results.restype = C.c_int
     L.sl1x1_batch_plan_shape.argtypes = [vp, vp, vp, vp]
     L.sl1x1_batch_plan_destroy.argtypes = [vp]
+    L.pdlange_.argtypes = [C.c_char_p, ip, ip, vp, ip, ip, ip, vp, C.c_size_t]
+    L.pdlange_.restype = C.c_double
+    L.pdgecon_.argtypes = [C.c_char_p, ip, vp, ip, ip, ip, C.POINTER(C.c_double),
+                           C.POINTER(C.c_double), vp, ip, vp, ip, ip, C.c_size_t]
+    L.pdgecon_.restype = None
+    L.pdgetri_.argtypes = [ip, vp, ip, ip, ip, vp, vp, ip, vp, ip, ip]
+    L.pdgetri_.restype = None
+    L.sl1x1_dlange_dev.argtypes = [C.c_char, C.c_int, C.c_int, vp, C.c_longlong, vp]
+    L.sl1x1_dlange_dev.restype = C.c_double
+    L.sl1x1_dgecon_dev.argtypes = [C.c_char, C.c_int, vp, C.c_longlong, C.c_double,
+                                   C.POINTER(C.c_double), vp]
+    L.sl1x1_dgecon_dev.restype = C.c_int
+    L.sl1x1_dgetri_dev.argtypes = [C.c_int, vp, C.c_longlong, vp, vp]
+    L.sl1x1_dgetri_dev.restype = C.c_int
     L.sl1x1_finalize.argtypes = []
     L.sl1x1_set_default_nb.argtypes = [C.c_int]
     L.sl1x1_set_panel_rows.argtypes = [C.c_int]
@@ -185,6 +199,43 @@ def pdgesv(n, nrhs, a, ia, ja, desca, ipiv, b, ib, jb, descb) -> int:
                   ipiv.ctypes.data_as(C.c_void_p), _arr(b, np.float64), _i(ib), _i(jb), dbp,
                   C.byref(info))
     return info.value
+
+
+def pdlange(norm, m, n, a, ia, ja, desca) -> float:
+    """PDLANGE(NORM, M, N, A, IA, JA, DESCA, WORK)."""
+    d, dp = _desc(desca)
+    work = np.zeros(max(1, m + n), dtype=np.float64)
+    return lib().pdlange_(norm.encode()[:1], _i(m), _i(n), _arr(a, np.float64), _i(ia), _i(ja), dp,
+                          work.ctypes.data_as(C.c_void_p), 1)
+
+
+def pdgecon(norm, n, a, ia, ja, desca, anorm, lwork=None, liwork=None):
+    """PDGECON: returns (rcond, info, work0, iwork0); lwork/liwork = -1 queries."""
+    d, dp = _desc(desca)
+    lw = 5 * n + 2 * max(1, int(desca[5])) + 16 if lwork is None else lwork
+    liw = max(1, n) + 8 if liwork is None else liwork
+    work = np.zeros(max(1, lw if lw > 0 else 1), dtype=np.float64)
+    iwork = np.zeros(max(1, liw if liw > 0 else 1), dtype=np.int32)
+    rc = C.c_double()
+    info = C.c_int()
+    lib().pdgecon_(norm.encode()[:1], _i(n), _arr(a, np.float64), _i(ia), _i(ja), dp,
+                   C.byref(C.c_double(anorm)), C.byref(rc), work.ctypes.data_as(C.c_void_p), _i(lw),
+                   iwork.ctypes.data_as(C.c_void_p), _i(liw), C.byref(info), 1)
+    return rc.value, info.value, work[0], int(iwork[0])
+
+
+def pdgetri(n, a, ia, ja, desca, ipiv, lwork=None, liwork=None):
+    """PDGETRI: returns (info, work0, iwork0); A overwritten by inv(A)."""
+    d, dp = _desc(desca)
+    lw = max(1, (n + 64) * int(desca[5])) if lwork is None else lwork
+    liw = int(desca[3]) + int(desca[5]) + 8 if liwork is None else liwork
+    work = np.zeros(max(1, lw if lw > 0 else 1), dtype=np.float64)
+    iwork = np.zeros(max(1, liw if liw > 0 else 1), dtype=np.int32)
+    info = C.c_int()
+    lib().pdgetri_(_i(n), _arr(a, np.float64), _i(ia), _i(ja), dp, ipiv.ctypes.data_as(C.c_void_p),
+                   work.ctypes.data_as(C.c_void_p), _i(lw), iwork.ctypes.data_as(C.c_void_p), _i(liw),
+                   C.byref(info))
+    return info.value, work[0], int(iwork[0])
 
 
 # ------------------------------------------------------------ phase timers

@@ -11,6 +11,7 @@
 // INFO <= -10000.
 #include <cuda_runtime.h>
 #include <climits>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -154,6 +155,7 @@ struct DevState {
   double* dAcopy = nullptr; size_t capAcopy = 0;
   int* dchain = nullptr; size_t capChain = 0;
   double* dsplitk = nullptr; size_t capSplitk = 0;
+  double* daux = nullptr; size_t capAux = 0;
   int chain_epoch = 0;
   unsigned short* dA16 = nullptr; size_t capA16 = 0;
   unsigned short* dB16 = nullptr; size_t capB16 = 0;
@@ -204,7 +206,7 @@ void release_all() {
   cudaFree(g_dev.dF); cudaFree(g_dev.dpermx); cudaFree(g_dev.dR); cudaFree(g_dev.dD);
   cudaFree(g_dev.dXf); cudaFree(g_dev.dXt); cudaFree(g_dev.dcm); cudaFree(g_dev.dV);
   cudaFree(g_dev.dw); cudaFree(g_dev.dAx); cudaFree(g_dev.dh); cudaFree(g_dev.dAcopy);
-  cudaFree(g_dev.dchain); cudaFree(g_dev.dsplitk);
+  cudaFree(g_dev.dchain); cudaFree(g_dev.dsplitk); cudaFree(g_dev.daux);
   sl::splitk_scratch() = sl::SplitKScratch();
   if (g_dev.stream) cudaStreamDestroy(g_dev.stream);
   g_dev = DevState();
@@ -752,6 +754,212 @@ int sl1x1_batch_plan_shape(sl1x1_batch_plan plan, int* threads, int* chunk, int*
 
 void sl1x1_batch_plan_destroy(sl1x1_batch_plan plan) {
   sl::batch_plan_destroy(reinterpret_cast<sl::BatchPlan*>(plan));
+}
+
+// ------------------------------------------------------ norms / rcond / inverse
+static char upc(char c) { return (c >= 'a' && c <= 'z') ? (char)(c - 32) : c; }
+
+double sl1x1_dlange_dev(char norm, int m, int n, const double* dA, long long ldda, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (m <= 0 || n <= 0) return 0.0;
+  if (!ensure_device()) return NAN;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = grow(&g_dev.daux, &g_dev.capAux, (size_t)(m > n ? m : n) + 8);
+  double v = NAN;
+  if (e == cudaSuccess)
+    e = sl::dlange_device(norm, m, n, dA, ldda, g_dev.daux, g_dev.daux + (m > n ? m : n) + 4, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&v, g_dev.daux + (m > n ? m : n) + 4, sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    std::fprintf(stderr, "sl1x1_dlange_dev: CUDA error %d\n", (int)e);
+    return NAN;
+  }
+  return v;
+}
+
+// PDLANGE (SRC/pdlange.f:1): the norm of sub(A), computed on the GPU.
+double pdlange_(const char* NORM, const int* M, const int* N, const double* A, const int* IA,
+                const int* JA, const int* DESCA, double* WORK, size_t NORM_len) {
+  (void)WORK; (void)NORM_len;
+  const int m = *M, n = *N;
+  if (m <= 0 || n <= 0) return 0.0;
+  double* dA = nullptr;
+  long long ldda = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!ensure_device()) {
+      std::fprintf(stderr, "pdlange_: no usable sm_103 GPU\n");
+      return NAN;
+    }
+    ldda = round_ld(m);
+    if (grow(&g_dev.dA, &g_dev.capA, (size_t)ldda * n) != cudaSuccess) return NAN;
+    const long long lld = DESCA[LLD_];
+    if (cudaMemcpy2DAsync(g_dev.dA, ldda * sizeof(double), A + (*IA - 1) + (long long)(*JA - 1) * lld,
+                          lld * sizeof(double), (size_t)m * sizeof(double), n,
+                          cudaMemcpyHostToDevice, g_dev.stream) != cudaSuccess)
+      return NAN;
+    dA = g_dev.dA;
+  }
+  return sl1x1_dlange_dev(NORM[0], m, n, dA, ldda, g_dev.stream);
+}
+
+int sl1x1_dgecon_dev(char norm, int n, const double* dLU, long long ldda, double anorm,
+                     double* rcond, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  const char u = upc(norm);
+  const bool onenrm = (u == '1' || u == 'O');
+  if (!onenrm && u != 'I') return -1;
+  if (n < 0) return -2;
+  if (ldda < (n > 1 ? n : 1)) return -4;
+  if (anorm < 0.0) return -5;
+  if (!ensure_device()) return cuda_info(cudaErrorNoDevice);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = grow(&g_dev.daux, &g_dev.capAux, 3 * (size_t)n + 16);
+  if (e != cudaSuccess) return cuda_info(e);
+  e = sl::dgecon_device(onenrm, n, dLU, ldda, anorm, rcond, g_dev.daux,
+                        reinterpret_cast<int*>(g_dev.daux + 3 * (size_t)n + 8), s);
+  return e == cudaSuccess ? 0 : cuda_info(e);
+}
+
+// PDGECON (SRC/pdgecon.f): validation, workspace query and quick returns as
+// the reference; the estimate is computed on the GPU from the LU factors.
+void pdgecon_(const char* NORM, const int* N, const double* A, const int* IA, const int* JA,
+              const int* DESCA, const double* ANORM, double* RCOND, double* WORK,
+              const int* LWORK, int* IWORK, const int* LIWORK, int* INFO, size_t NORM_len) {
+  (void)NORM_len;
+  int nprow, npcol, myrow, mycol;
+  gridinfo(DESCA[CTXT_], &nprow, &npcol, &myrow, &mycol);
+  int info = 0;
+  const int n = *N, ia = *IA, ja = *JA;
+  const char u = upc(NORM[0]);
+  const bool onenrm = (NORM[0] == '1' || u == 'O');
+  bool lquery = false;
+  if (nprow == -1) {
+    info = -(600 + FCTXT);
+  } else {
+    chk1mat(n, 2, n, 2, ia, ja, DESCA, 6, &info);
+    if (info == 0) {
+      const int npmod = numroc(n + (ia - 1) % DESCA[MB_], DESCA[MB_], 0, 0, 1);
+      const int nqmod = numroc(n + (ja - 1) % DESCA[NB_], DESCA[NB_], 0, 0, 1);
+      const int nb = DESCA[NB_];
+      int inner = nb > nqmod + nb ? nb : nqmod + nb;
+      const int lwmin = 2 * npmod + 2 * nqmod + (inner > 2 ? inner : 2);
+      const int liwmin = npmod > 1 ? npmod : 1;
+      WORK[0] = (double)lwmin;
+      IWORK[0] = liwmin;
+      lquery = (*LWORK == -1 || *LIWORK == -1);
+      if (!onenrm && u != 'I') info = -1;
+      else if (*ANORM < 0.0) info = -7;
+      else if (*LWORK < lwmin && !lquery) info = -10;
+      else if (*LIWORK < liwmin && !lquery) info = -12;
+    }
+  }
+  *INFO = info;
+  if (info != 0) { pxerbla(DESCA[CTXT_], "PDGECON", -info); return; }
+  if (lquery) return;
+  *RCOND = 0.0;
+  if (n == 0) { *RCOND = 1.0; return; }
+  if (*ANORM == 0.0) return;
+  if (n == 1) { *RCOND = 1.0; return; }
+  double* dA = nullptr;
+  long long ldda = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!ensure_device()) { *INFO = cuda_info(cudaErrorNoDevice); return; }
+    ldda = round_ld(n);
+    cudaError_t e = grow(&g_dev.dA, &g_dev.capA, (size_t)ldda * n);
+    const long long lld = DESCA[LLD_];
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(g_dev.dA, ldda * sizeof(double), A + (ia - 1) + (long long)(ja - 1) * lld,
+                            lld * sizeof(double), (size_t)n * sizeof(double), n,
+                            cudaMemcpyHostToDevice, g_dev.stream);
+    if (e != cudaSuccess) { *INFO = cuda_info(e); return; }
+    dA = g_dev.dA;
+  }
+  *INFO = sl1x1_dgecon_dev(NORM[0], n, dA, ldda, *ANORM, RCOND, g_dev.stream);
+}
+
+int sl1x1_dgetri_dev(int n, double* dA, long long ldda, const int* dipiv, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (n < 0) return -1;
+  if (ldda < (n > 1 ? n : 1)) return -3;
+  if (n == 0) return 0;
+  if (!ensure_device()) return cuda_info(cudaErrorNoDevice);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = grow(&g_dev.dipiv, &g_dev.capP, (size_t)n);
+  if (e == cudaSuccess) e = ensure_solve_ws(n, n);
+  if (e == cudaSuccess) e = grow(&g_dev.daux, &g_dev.capAux, (size_t)n * n + 8);
+  if (e != cudaSuccess) return cuda_info(e);
+  e = sl::ipiv_shift(dipiv, g_dev.dipiv, n, -1, s);
+  if (e != cudaSuccess) return cuda_info(e);
+  int info = 0;
+  sl::LuWork w = make_work();
+  e = sl::dgetri_device(n, dA, ldda, g_dev.dipiv, g_dev.daux, w,
+                        reinterpret_cast<int*>(g_dev.daux + (size_t)n * n), &info, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? info : cuda_info(e);
+}
+
+// PDGETRI (SRC/pdgetri.f): validation and workspace query as the reference,
+// inverse computed on the GPU from the LU factors and pivots of PDGETRF.
+void pdgetri_(const int* N, double* A, const int* IA, const int* JA, const int* DESCA,
+              const int* IPIV, double* WORK, const int* LWORK, int* IWORK, const int* LIWORK,
+              int* INFO) {
+  int nprow, npcol, myrow, mycol;
+  gridinfo(DESCA[CTXT_], &nprow, &npcol, &myrow, &mycol);
+  int info = 0;
+  const int n = *N, ia = *IA, ja = *JA;
+  bool lquery = false;
+  if (nprow == -1) {
+    info = -(500 + FCTXT);
+  } else {
+    chk1mat(n, 1, n, 1, ia, ja, DESCA, 5, &info);
+    if (info == 0) {
+      const int iroff = (ia - 1) % DESCA[MB_], icoff = (ja - 1) % DESCA[NB_];
+      const int np = numroc(n + iroff, DESCA[MB_], 0, 0, 1);
+      const int lwmin = np * DESCA[NB_];
+      const int nq = numroc(DESCA[N_], DESCA[NB_], 0, 0, 1);
+      const int liwmin = nq + DESCA[NB_];  // NPROW == NPCOL on a 1x1 grid
+      WORK[0] = (double)lwmin;
+      IWORK[0] = liwmin;
+      lquery = (*LWORK == -1 || *LIWORK == -1);
+      if (iroff != icoff || iroff != 0) info = -4;
+      else if (DESCA[MB_] != DESCA[NB_]) info = -(500 + FNB);
+      else if (*LWORK < lwmin && !lquery) info = -8;
+      else if (*LIWORK < liwmin && !lquery) info = -10;
+    }
+  }
+  *INFO = info;
+  if (info != 0) { pxerbla(DESCA[CTXT_], "PDGETRI", -info); return; }
+  if (lquery || n == 0) return;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!ensure_device()) { *INFO = cuda_info(cudaErrorNoDevice); return; }
+  const long long lld = DESCA[LLD_];
+  const long long ldda = round_ld(n);
+  cudaStream_t s = g_dev.stream;
+  cudaError_t e = grow(&g_dev.dA, &g_dev.capA, (size_t)ldda * n);
+  if (e == cudaSuccess) e = grow(&g_dev.dipiv, &g_dev.capP, (size_t)n);
+  if (e == cudaSuccess) e = ensure_solve_ws(n, n);
+  if (e == cudaSuccess) e = grow(&g_dev.daux, &g_dev.capAux, (size_t)n * n + 8);
+  if (e != cudaSuccess) { *INFO = cuda_info(e); return; }
+  double* hA = A + (ia - 1) + (long long)(ja - 1) * lld;
+  std::vector<int> hp((size_t)n);
+  for (int k = 0; k < n; ++k) hp[k] = IPIV[ia - 1 + k] - ia;
+  e = cudaMemcpy2DAsync(g_dev.dA, ldda * sizeof(double), hA, lld * sizeof(double),
+                        (size_t)n * sizeof(double), n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(g_dev.dipiv, hp.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
+  int dinfo = 0;
+  sl::LuWork w = make_work();
+  if (e == cudaSuccess)
+    e = sl::dgetri_device(n, g_dev.dA, ldda, g_dev.dipiv, g_dev.daux, w,
+                          reinterpret_cast<int*>(g_dev.daux + (size_t)n * n), &dinfo, s);
+  if (e == cudaSuccess && dinfo == 0)
+    e = cudaMemcpy2DAsync(hA, lld * sizeof(double), g_dev.dA, ldda * sizeof(double),
+                          (size_t)n * sizeof(double), n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  *INFO = (e == cudaSuccess) ? dinfo : cuda_info(e);
 }
 
 void sl1x1_finalize(void) {

@@ -11,10 +11,34 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "common.cuh"
 #include "sl_internal.h"
 
 namespace sl {
+
+namespace {
+// Dynamic shared-memory opt-in, once per kernel and translation unit. Kernels
+// are registered per translation unit, so the record of which kernels were
+// raised must not be shared between units: it lives in an unnamed namespace.
+inline cudaError_t smem_attr_once(const void* kern, int bytes) {
+  static std::mutex mu;
+  static const void* done_k[64];
+  static int done_b[64];
+  static int ndone = 0;
+  std::lock_guard<std::mutex> lk(mu);
+  for (int i = 0; i < ndone; ++i)
+    if (done_k[i] == kern && done_b[i] >= bytes) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess && ndone < 64) {
+    done_k[ndone] = kern;
+    done_b[ndone] = bytes;
+    ++ndone;
+  }
+  return e;
+}
+}  // namespace
 
 constexpr int PW = 32;       // sub-panel width held in shared memory
 constexpr int PMAXG = 1024;  // max CTAs of the panel kernel
@@ -497,13 +521,7 @@ inline cudaError_t launch_panel(T* A, long long lda, int m, int r0, int c0, int 
   const int G = (R + rpc - 1) / rpc;
   const size_t smem = sizeof(T) * (size_t)rpc * PLD;
   if (smem > 200 * 1024 || G > PMAXG) return cudaErrorInvalidValue;  // M beyond the panel limit
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(panel_kernel<T>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  SL_TRY(smem_attr_once((const void*)panel_kernel<T>, 200 * 1024));
   cudaError_t e = cudaMemsetAsync(ws.bar, 0, 2 * sizeof(int), s);
   if (e != cudaSuccess) return e;
   void* args[] = {&A, &lda, &m, &r0, &c0, &w, (void*)&rpc, &ipiv, (void*)&ws.info_col,
@@ -529,13 +547,7 @@ inline cudaError_t trsm_strip(int w, int ncols, const T* Tm, long long ldt, T* B
   if (w <= 0 || ncols <= 0) return cudaSuccess;
   const size_t smem = sizeof(T) * (size_t)w * (NC + 1);
   auto kern = trsm_strip_kernel<T, UPPER, TRANS, UNIT, NC>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         100 * 1024);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  SL_TRY(smem_attr_once((const void*)kern, 100 * 1024));
   dim3 grid((ncols + NC - 1) / NC);
   kern<<<grid, 256, smem, s>>>(w, ncols, Tm, ldt, B, ldb);
   count_launches(1);
@@ -676,13 +688,7 @@ inline cudaError_t diag_solve(int kb, int nrhs, const T* Td, long long lda, T* X
   if (kb <= 128 && nrhs <= 16) {
     // Few right-hand sides: one warp per column, the block in shared memory.
     auto kern = trsv_warp_kernel<T, UPPER, TRANS, UNIT>;
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           140 * 1024);
-      if (e != cudaSuccess) return e;
-      attr_set = true;
-    }
+    SL_TRY(smem_attr_once((const void*)kern, 140 * 1024));
     const size_t smem = sizeof(T) * (size_t)kb * (kb + 1);
     kern<<<(nrhs + 3) / 4, 128, smem, s>>>(kb, nrhs, Td, lda, X, ldx);
     count_launches(1);

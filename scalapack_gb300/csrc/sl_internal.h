@@ -167,6 +167,14 @@ cudaError_t batch_plan_results(BatchPlan* p, int* info, int* iters, double* sres
 void batch_plan_shape(const BatchPlan* p, int* threads, int* chunk, int* ctas);
 void batch_plan_destroy(BatchPlan* p);
 
+// ---- norms, condition estimate, inverse (aux.cu) ----
+cudaError_t dlange_device(char norm, int m, int n, const double* A, long long lda, double* work,
+                          double* result, cudaStream_t s);
+cudaError_t dgecon_device(bool onenrm, int n, const double* LU, long long lda, double anorm,
+                          double* rcond, double* work, int* iw, cudaStream_t s);
+cudaError_t dgetri_device(int n, double* dA, long long lda, const int* dipiv, double* X,
+                          const LuWork& ws, int* dflag, int* info, cudaStream_t s);
+
 // perm[i] = original row ending in row i after the n interchanges i <-> ipiv[i].
 cudaError_t perm_compose(const int* dipiv, int n, int* perm, cudaStream_t s);
 

@@ -206,3 +206,42 @@ def test_valid_call_without_gpu_fails_loudly(sl, ctx):
     d = _desc(ctx)
     info = _getrf_info(sl, 8, 8, 1, 1, d)
     assert info <= -10000  # never a silent CPU fallback
+
+
+def test_pdgecon_validation_and_query(sl, ctx):
+    # SRC/pdgecon.f:218-275: NORM -> -1, ANORM < 0 -> -7, LWORK -> -10, LIWORK -> -12
+    n, nb = 8, 4
+    d = _desc(ctx)
+    a = np.zeros((8, 8), order="F")
+    rc, info, w0, iw0 = sl.pdgecon("X", n, a, 1, 1, d, 1.0)
+    assert info == -1
+    rc, info, w0, iw0 = sl.pdgecon("1", n, a, 1, 1, d, -1.0)
+    assert info == -7
+    # workspace query: LWMIN = 2*NP + 2*NQ + max(2, NQ + NB), LIWMIN = max(1, NP)
+    rc, info, w0, iw0 = sl.pdgecon("1", n, a, 1, 1, d, 1.0, lwork=-1)
+    assert info == 0 and w0 == 2 * 8 + 2 * 8 + (8 + nb) and iw0 == 8
+    rc, info, w0, iw0 = sl.pdgecon("I", n, a, 1, 1, d, 1.0, lwork=3)
+    assert info == -10
+    rc, info, w0, iw0 = sl.pdgecon("I", n, a, 1, 1, d, 1.0, liwork=1)
+    assert info == -12
+    # quick returns need no GPU: ANORM = 0 -> RCOND = 0
+    rc, info, _, _ = sl.pdgecon("1", n, a, 1, 1, d, 0.0)
+    assert info == 0 and rc == 0.0
+
+
+def test_pdgetri_validation_and_query(sl, ctx):
+    # SRC/pdgetri.f: IA/JA misaligned -> -4, MB != NB -> -506, LWORK -> -8, LIWORK -> -10
+    d = _desc(ctx)
+    a = np.zeros((8, 8), order="F")
+    ip = np.arange(1, 17, dtype=np.int32)
+    info, w0, iw0 = sl.pdgetri(4, a, 2, 1, d, ip)
+    assert info == -4
+    info, w0, iw0 = sl.pdgetri(8, a, 1, 1, _desc(ctx, mb=4, nb=2), ip)
+    assert info == -506
+    info, w0, iw0 = sl.pdgetri(8, a, 1, 1, d, ip, lwork=-1)
+    assert info == 0 and w0 == 8 * 4 and iw0 == 8 + 4  # LWMIN = NP*NB, LIWMIN = NQ + NB
+    info, w0, iw0 = sl.pdgetri(8, a, 1, 1, d, ip, lwork=1)
+    assert info == -8
+    info, w0, iw0 = sl.pdgetri(8, a, 1, 1, d, ip, liwork=1)
+    assert info == -10
+    assert sl.pdgetri(0, a, 1, 1, d, ip)[0] == 0

@@ -179,3 +179,62 @@ def test_config_n2048_nb64(sl, orc, ctx):
     assert bad == 0, ties
     assert orc.fresid(LU, rel, A0) < RESID_THRESH
     assert orc.sresid(A0, B0, X) < RESID_THRESH
+
+
+@pytest.mark.parametrize("norm", ["M", "1", "O", "I", "F", "E"])
+def test_pdlange_norms(sl, orc, ctx, norm):
+    m, n = 300, 170
+    A = orc.matgen(m, n, 100)
+    Ab = padded(A, ia=5, ja=3)
+    d = np.array([1, ctx, Ab.shape[0], Ab.shape[1], 4, 4, 0, 0, Ab.shape[0]], np.int32)
+    v = sl.pdlange(norm, m, n, Ab, 5, 3, d)
+    ref = {"M": np.abs(A).max(), "1": np.abs(A).sum(0).max(), "O": np.abs(A).sum(0).max(),
+           "I": np.abs(A).sum(1).max(), "F": np.linalg.norm(A), "E": np.linalg.norm(A)}[norm]
+    assert abs(v - ref) <= 1e-13 * ref
+
+
+@pytest.mark.parametrize("norm", ["1", "I"])
+@pytest.mark.parametrize("n", [2, 77, 600])
+def test_pdgecon_brackets_true_rcond(sl, orc, ctx, norm, n):
+    A0, _ = system(orc, n, 1)
+    A = np.asfortranarray(A0.copy())
+    nb = 32
+    d = np.array([1, ctx, n, n, nb, nb, 0, 0, n], np.int32)
+    ipiv = np.zeros(n + nb, dtype=np.int32)
+    anorm = sl.pdlange(norm, n, n, A, 1, 1, d)
+    assert sl.pdgetrf(n, n, A, 1, 1, d, ipiv) == 0
+    rc, info, _, _ = sl.pdgecon(norm, n, A, 1, 1, d, anorm)
+    assert info == 0
+    inv = np.linalg.inv(A0)
+    true = 1.0 / (anorm * (np.abs(inv).sum(0).max() if norm == "1" else np.abs(inv).sum(1).max()))
+    # the estimate of ||inv(A)|| never exceeds the true norm, and is rarely far below it
+    assert true * (1 - 1e-10) <= rc <= 10.0 * true, (rc, true)
+
+
+@pytest.mark.parametrize("n,nb", [(1, 1), (5, 2), (200, 32), (1000, 64)])
+def test_pdgetri_inverse(sl, orc, ctx, n, nb):
+    A0, _ = system(orc, n, 1)
+    A = np.asfortranarray(A0.copy())
+    d = np.array([1, ctx, n, n, nb, nb, 0, 0, n], np.int32)
+    ipiv = np.zeros(n + nb, dtype=np.int32)
+    assert sl.pdgetrf(n, n, A, 1, 1, d, ipiv) == 0
+    info, _, _ = sl.pdgetri(n, A, 1, 1, d, ipiv)
+    assert info == 0
+    R = A0 @ A - np.eye(n)
+    eps = 2.0 ** -53
+    assert np.abs(R).sum(1).max() / (np.abs(A0).sum(1).max() * np.abs(A).sum(1).max() * n * eps) < 16
+
+
+def test_pdgetri_singular_info(sl, orc, ctx):
+    n, nb = 50, 8
+    A0, _ = system(orc, n, 1)
+    A0[:, 20] = 0.0
+    A = np.asfortranarray(A0.copy())
+    d = np.array([1, ctx, n, n, nb, nb, 0, 0, n], np.int32)
+    ipiv = np.zeros(n + nb, dtype=np.int32)
+    k = sl.pdgetrf(n, n, A, 1, 1, d, ipiv)
+    assert k == 21
+    before = A.copy()
+    info, _, _ = sl.pdgetri(n, A, 1, 1, d, ipiv)
+    assert info == 21
+    np.testing.assert_array_equal(A, before)  # inverse not computed
