@@ -177,6 +177,9 @@ int sl1x1_dgetri_dev(int n, double* dA, long long ldda, const int* dipiv, void* 
 void sl1x1_finalize(void);
 /* Block size NB used by the device entry points when nb <= 0 (default 256). */
 void sl1x1_set_default_nb(int nb);
+/* Look-ahead in the factorizations (default on): the next panel is factored
+ * on a second stream while the trailing update runs. Same results either way. */
+void sl1x1_set_lookahead(int on);
 /* Smallest row slice per CTA of the cooperative panel kernel (8..768,
  * default 64, i.e. one CTA per SM for tall panels): larger slices mean fewer
  * CTAs per per-column grid barrier but more serial work per CTA. Changes only

@@ -133,6 +133,8 @@ struct DevState {
   bool ok = false;
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t aux = nullptr;       // look-ahead stream (higher priority)
+  cudaEvent_t ev_next = nullptr, ev_panel = nullptr;
   double* dA = nullptr; size_t capA = 0;
   double* dB = nullptr; size_t capB = 0;
   int* dipiv = nullptr; size_t capP = 0;
@@ -163,6 +165,7 @@ struct DevState {
 };
 DevState g_dev;
 int g_default_nb = 256;
+bool g_lookahead = true;
 
 int cuda_info(cudaError_t e) { return -10000 - (int)e; }
 
@@ -180,6 +183,13 @@ bool ensure_device() {
     return false;
   }
   if (cudaStreamCreateWithFlags(&g_dev.stream, cudaStreamNonBlocking) != cudaSuccess) return false;
+  {
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (cudaStreamCreateWithPriority(&g_dev.aux, cudaStreamNonBlocking, hi) != cudaSuccess) return false;
+    if (cudaEventCreateWithFlags(&g_dev.ev_next, cudaEventDisableTiming) != cudaSuccess) return false;
+    if (cudaEventCreateWithFlags(&g_dev.ev_panel, cudaEventDisableTiming) != cudaSuccess) return false;
+  }
   if (cudaMalloc(&g_dev.dsmall, 16 * sizeof(int)) != cudaSuccess) return false;
   if (cudaMalloc(&g_dev.dcand, sl::panel_cand_doubles() * sizeof(double)) != cudaSuccess) return false;
   g_dev.ok = true;
@@ -209,6 +219,9 @@ void release_all() {
   cudaFree(g_dev.dchain); cudaFree(g_dev.dsplitk); cudaFree(g_dev.daux);
   sl::splitk_scratch() = sl::SplitKScratch();
   if (g_dev.stream) cudaStreamDestroy(g_dev.stream);
+  if (g_dev.aux) cudaStreamDestroy(g_dev.aux);
+  if (g_dev.ev_next) cudaEventDestroy(g_dev.ev_next);
+  if (g_dev.ev_panel) cudaEventDestroy(g_dev.ev_panel);
   g_dev = DevState();
 }
 
@@ -222,6 +235,11 @@ sl::LuWork make_work() {
   w.bswap = g_dev.dbswap;
   w.perm_len = g_dev.capPerm;
   w.bswap_len = g_dev.capBs;
+  if (g_lookahead) {
+    w.aux = g_dev.aux;
+    w.ev_next = g_dev.ev_next;
+    w.ev_panel = g_dev.ev_panel;
+  }
   return w;
 }
 
@@ -965,6 +983,11 @@ void pdgetri_(const int* N, double* A, const int* IA, const int* JA, const int* 
 void sl1x1_finalize(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   release_all();
+}
+
+void sl1x1_set_lookahead(int on) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_lookahead = (on != 0);
 }
 
 void sl1x1_set_panel_rows(int rows) {

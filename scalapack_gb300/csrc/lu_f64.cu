@@ -93,6 +93,42 @@ cudaError_t perm_compose(const int* dipiv, int n, int* perm, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// PDGETF2 on columns [j, j+jb), rows [j, m): 32-wide cooperative sub-panels,
+// each followed by its row interchanges on the rest of the panel, the U solve
+// and the GEMM update of the panel's remaining columns.
+static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, int j, int jb,
+                                const LuWork& ws, cudaStream_t s) {
+  auto Ap = [&](long long i, long long c) { return dA + i + c * ldda; };
+  phase_begin(kPhPanel, s);
+  double pflops = 0.0;
+  for (int c = 0; c < jb; c += PW) {
+    const int w = (jb - c) < PW ? (jb - c) : PW;
+    const int r0 = j + c;
+    SL_TRY(launch_panel<double>(dA, ldda, m, r0, r0, w, dipiv, ws, s));
+    const int kw = (m - r0) < w ? (m - r0) : w;
+    for (int k = 0; k < kw; ++k) pflops += 2.0 * (double)(m - r0 - k - 1) * (w - k - 1) + (m - r0 - k - 1);
+    SL_TRY(laswp<double>(dA, ldda, r0, r0 + kw, dipiv, j, r0, r0 + w, j + jb, s));
+    if (c + w < jb) {
+      SL_TRY((trsm_strip<double, false, false, true>(kw, jb - c - w, Ap(r0, r0), ldda,
+                                                      Ap(r0, r0 + w), ldda, s)));
+      pflops += (double)kw * kw * (jb - c - w);
+      if (r0 + kw < m) {
+        SL_TRY(dgemm(false, m - r0 - kw, jb - c - w, kw, -1.0, Ap(r0 + kw, r0), ldda,
+                     Ap(r0, r0 + w), ldda, 1.0, Ap(r0 + kw, r0 + w), ldda, s));
+        pflops += 2.0 * (double)(m - r0 - kw) * (jb - c - w) * kw;
+      }
+    }
+  }
+  phase_end(kPhPanel, s, pflops, 16.0 * (double)(m - j) * jb);
+  return cudaSuccess;
+}
+
+// Right-looking blocked LU. With look-ahead resources in `ws`, the panel of
+// step j+1 is factored on ws.aux while the trailing update of step j runs on
+// s: the columns of the next panel are updated first (event ev_next), the
+// next panel starts as soon as they are ready, and step j+1 waits for it
+// (event ev_panel). Panel and update touch disjoint columns, and each element
+// is accumulated in the same order either way, so the factors are the same.
 cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, int nb,
                           const LuWork& ws, cudaStream_t s) {
   SL_TRY(cudaMemsetAsync(ws.status, 0, sizeof(int), s));
@@ -100,51 +136,57 @@ cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, 
   const int mn = m < n ? m : n;
   if (nb > 1024) nb = 1024;
   auto Ap = [&](long long i, long long j) { return dA + i + j * ldda; };
+  const bool lookahead = ws.aux && ws.ev_next && ws.ev_panel && mn > 2 * nb;
+  if (mn > 0) SL_TRY(factor_panel(m, dA, ldda, dipiv, 0, (mn < nb ? mn : nb), ws, s));
+  bool panel_on_aux = false;
   for (int j = 0; j < mn; j += nb) {
     const int jb = (mn - j) < nb ? (mn - j) : nb;
-    // ---- panel (PDGETF2) as 32-wide sub-panels ----
-    phase_begin(kPhPanel, s);
-    double pflops = 0.0;
-    for (int c = 0; c < jb; c += PW) {
-      const int w = (jb - c) < PW ? (jb - c) : PW;
-      const int r0 = j + c;
-      SL_TRY(launch_panel<double>(dA, ldda, m, r0, r0, w, dipiv, ws, s));
-      const int kw = (m - r0) < w ? (m - r0) : w;
-      for (int k = 0; k < kw; ++k) pflops += 2.0 * (double)(m - r0 - k - 1) * (w - k - 1) + (m - r0 - k - 1);
-      SL_TRY(laswp<double>(dA, ldda, r0, r0 + kw, dipiv, j, r0, r0 + w, j + jb, s));
-      if (c + w < jb) {
-        SL_TRY((trsm_strip<double, false, false, true>(kw, jb - c - w, Ap(r0, r0), ldda,
-                                                        Ap(r0, r0 + w), ldda, s)));
-        pflops += (double)kw * kw * (jb - c - w);
-        if (r0 + kw < m) {
-          SL_TRY(dgemm(false, m - r0 - kw, jb - c - w, kw, -1.0, Ap(r0 + kw, r0), ldda,
-                       Ap(r0, r0 + w), ldda, 1.0, Ap(r0 + kw, r0 + w), ldda, s));
-          pflops += 2.0 * (double)(m - r0 - kw) * (jb - c - w) * kw;
-        }
-      }
-    }
-    phase_end(kPhPanel, s, pflops, 16.0 * (double)(m - j) * jb);
+    if (panel_on_aux) SL_TRY(cudaStreamWaitEvent(s, ws.ev_panel, 0));
+    panel_on_aux = false;
     // ---- PDLASWP on the left and right column blocks ----
     phase_begin(kPhLaswp, s);
     SL_TRY(laswp<double>(dA, ldda, j, j + jb, dipiv, 0, j, j + jb, n, s));
     phase_end(kPhLaswp, s, 0.0, 32.0 * jb * (double)(n - jb));
-    if (j + jb < n) {
+    const int jn = j + jb;                                   // next panel's first column
+    const int jb2 = jn < mn ? ((mn - jn) < nb ? (mn - jn) : nb) : 0;
+    if (jn < n) {
       // ---- PDTRSM: U12 = L11^{-1} A12 ----
-      const double nr = (double)(n - j - jb);
+      const double nr = (double)(n - jn);
       phase_begin(kPhTrsm, s);
-      SL_TRY((trsm_strip<double, false, false, true>(jb, n - j - jb, Ap(j, j), ldda, Ap(j, j + jb),
-                                                      ldda, s)));
+      SL_TRY((trsm_strip<double, false, false, true>(jb, n - jn, Ap(j, j), ldda, Ap(j, jn), ldda, s)));
       phase_end(kPhTrsm, s, (double)jb * jb * nr, 8.0 * (0.5 * jb * jb + 2.0 * jb * nr));
       // ---- PDGEMM: A22 -= L21 * U12 ----
-      if (j + jb < m) {
-        const double mr = (double)(m - j - jb);
-        phase_begin(kPhGemm, s);
-        SL_TRY(dgemm(false, m - j - jb, n - j - jb, jb, -1.0, Ap(j + jb, j), ldda, Ap(j, j + jb),
-                     ldda, 1.0, Ap(j + jb, j + jb), ldda, s));
-        phase_end(kPhGemm, s, 2.0 * mr * nr * jb, 8.0 * (mr * jb + jb * nr + 2.0 * mr * nr));
+      if (jn < m) {
+        const double mr = (double)(m - jn);
+        if (lookahead && jb2 > 0) {
+          // next panel's columns first, then the panel on the look-ahead stream
+          phase_begin(kPhGemm, s);
+          SL_TRY(dgemm(false, m - jn, jb2, jb, -1.0, Ap(jn, j), ldda, Ap(j, jn), ldda, 1.0,
+                       Ap(jn, jn), ldda, s));
+          phase_end(kPhGemm, s, 2.0 * mr * jb2 * jb, 8.0 * (mr * jb + (double)jb * jb2 + 2.0 * mr * jb2));
+          SL_TRY(cudaEventRecord(ws.ev_next, s));
+          SL_TRY(cudaStreamWaitEvent(ws.aux, ws.ev_next, 0));
+          SL_TRY(factor_panel(m, dA, ldda, dipiv, jn, jb2, ws, ws.aux));
+          SL_TRY(cudaEventRecord(ws.ev_panel, ws.aux));
+          panel_on_aux = true;
+          const int rest = n - jn - jb2;
+          if (rest > 0) {
+            phase_begin(kPhGemm, s);
+            SL_TRY(dgemm(false, m - jn, rest, jb, -1.0, Ap(jn, j), ldda, Ap(j, jn + jb2), ldda, 1.0,
+                         Ap(jn, jn + jb2), ldda, s));
+            phase_end(kPhGemm, s, 2.0 * mr * rest * jb, 8.0 * (mr * jb + (double)jb * rest + 2.0 * mr * rest));
+          }
+        } else {
+          phase_begin(kPhGemm, s);
+          SL_TRY(dgemm(false, m - jn, n - jn, jb, -1.0, Ap(jn, j), ldda, Ap(j, jn), ldda, 1.0,
+                       Ap(jn, jn), ldda, s));
+          phase_end(kPhGemm, s, 2.0 * mr * nr * jb, 8.0 * (mr * jb + jb * nr + 2.0 * mr * nr));
+        }
       }
     }
+    if (jb2 > 0 && !panel_on_aux) SL_TRY(factor_panel(m, dA, ldda, dipiv, jn, jb2, ws, s));
   }
+  if (panel_on_aux) SL_TRY(cudaStreamWaitEvent(s, ws.ev_panel, 0));
   return cudaGetLastError();
 }
 

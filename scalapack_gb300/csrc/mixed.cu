@@ -230,6 +230,33 @@ static unsigned blocks_for(long long n, int t = 256) {
 }
 
 // ---------------------------------------------------- FP32 factorization
+// PDGETF2 in FP32 on columns [j, j+jb), rows [j, n).
+static cudaError_t factor_panel_f32(int n, float* F, long long ldf, int* dipiv, int j, int jb,
+                                    const LuWork& ws, cudaStream_t s) {
+  auto Fp = [&](long long i, long long c) { return F + i + c * ldf; };
+  const int m = n;
+  phase_begin(kPhMixedPanel, s);
+  for (int c = 0; c < jb; c += PW) {
+    const int w = (jb - c) < PW ? (jb - c) : PW;
+    const int r0 = j + c;
+    SL_TRY(launch_panel<float>(F, ldf, m, r0, r0, w, dipiv, ws, s));
+    const int kw = (m - r0) < w ? (m - r0) : w;
+    SL_TRY(laswp<float>(F, ldf, r0, r0 + kw, dipiv, j, r0, r0 + w, j + jb, s));
+    if (c + w < jb) {
+      SL_TRY((trsm_strip<float, false, false, true>(kw, jb - c - w, Fp(r0, r0), ldf,
+                                                     Fp(r0, r0 + w), ldf, s)));
+      if (r0 + kw < m)
+        SL_TRY(sgemm_simt(false, m - r0 - kw, jb - c - w, kw, -1.f, Fp(r0 + kw, r0), ldf,
+                          Fp(r0, r0 + w), ldf, Fp(r0 + kw, r0 + w), ldf, s));
+    }
+  }
+  phase_end(kPhMixedPanel, s, 0.0, 0.0);
+  return cudaSuccess;
+}
+
+// Low-precision right-looking LU of the FP32 working matrix, with the same
+// look-ahead as the FP64 path (next panel on ws.aux while the tcgen05 update
+// of the remaining columns runs).
 cudaError_t sgetrf_mixed_device(int n, float* F, long long ldf, int* dipiv, int nb, int fmt,
                                 const LuWork& ws, const MixedWork& mw, cudaStream_t s) {
   SL_TRY(cudaMemsetAsync(ws.status, 0, sizeof(int), s));
@@ -237,40 +264,50 @@ cudaError_t sgetrf_mixed_device(int n, float* F, long long ldf, int* dipiv, int 
   const int m = n, mn = n;
   if (nb > 1024) nb = 1024;
   auto Fp = [&](long long i, long long j) { return F + i + j * ldf; };
+  const bool lookahead = ws.aux && ws.ev_next && ws.ev_panel && mn > 2 * nb;
+  if (mn > 0) SL_TRY(factor_panel_f32(n, F, ldf, dipiv, 0, (mn < nb ? mn : nb), ws, s));
+  bool panel_on_aux = false;
   for (int j = 0; j < mn; j += nb) {
     const int jb = (mn - j) < nb ? (mn - j) : nb;
+    if (panel_on_aux) SL_TRY(cudaStreamWaitEvent(s, ws.ev_panel, 0));
+    panel_on_aux = false;
+    const int jn = j + jb;
+    const int jb2 = jn < mn ? ((mn - jn) < nb ? (mn - jn) : nb) : 0;
     phase_begin(kPhMixedPanel, s);
-    for (int c = 0; c < jb; c += PW) {
-      const int w = (jb - c) < PW ? (jb - c) : PW;
-      const int r0 = j + c;
-      SL_TRY(launch_panel<float>(F, ldf, m, r0, r0, w, dipiv, ws, s));
-      const int kw = (m - r0) < w ? (m - r0) : w;
-      SL_TRY(laswp<float>(F, ldf, r0, r0 + kw, dipiv, j, r0, r0 + w, j + jb, s));
-      if (c + w < jb) {
-        SL_TRY((trsm_strip<float, false, false, true>(kw, jb - c - w, Fp(r0, r0), ldf,
-                                                       Fp(r0, r0 + w), ldf, s)));
-        if (r0 + kw < m)
-          SL_TRY(sgemm_simt(false, m - r0 - kw, jb - c - w, kw, -1.f, Fp(r0 + kw, r0), ldf,
-                            Fp(r0, r0 + w), ldf, Fp(r0 + kw, r0 + w), ldf, s));
+    SL_TRY(laswp<float>(F, ldf, j, j + jb, dipiv, 0, j, j + jb, n, s));
+    if (jn < n)
+      SL_TRY((trsm_strip<float, false, false, true>(jb, n - jn, Fp(j, j), ldf, Fp(j, jn), ldf, s)));
+    phase_end(kPhMixedPanel, s, 0.0, 0.0);
+    if (jn < n && jn < m) {
+      const int mr = m - jn, nr = n - jn;
+      const int kp = lowp_kpad(jb) * lowp_kmult(fmt);
+      phase_begin(kPhMixedGemm, s);
+      SL_TRY(lowp_pack(fmt, Fp(jn, j), ldf, mr, Fp(j, jn), ldf, nr, jb, mw.A16, mw.B16, mw.col_exp, s));
+      if (lookahead && jb2 > 0) {
+        SL_TRY(lowp_gemm(fmt, mr, jb2, jb, mw.A16, mw.B16, mw.col_exp, Fp(jn, jn), ldf, ws.status, s));
+        phase_end(kPhMixedGemm, s, 2.0 * mr * (double)jb2 * jb, 8.0 * (double)mr * jb2);
+        SL_TRY(cudaEventRecord(ws.ev_next, s));
+        SL_TRY(cudaStreamWaitEvent(ws.aux, ws.ev_next, 0));
+        SL_TRY(factor_panel_f32(n, F, ldf, dipiv, jn, jb2, ws, ws.aux));
+        SL_TRY(cudaEventRecord(ws.ev_panel, ws.aux));
+        panel_on_aux = true;
+        const int rest = nr - jb2;
+        if (rest > 0) {
+          phase_begin(kPhMixedGemm, s);
+          SL_TRY(lowp_gemm(fmt, mr, rest, jb, mw.A16, mw.B16 + (long long)jb2 * kp, mw.col_exp + jb2,
+                           Fp(jn, jn + jb2), ldf, ws.status, s));
+          phase_end(kPhMixedGemm, s, 2.0 * mr * (double)rest * jb,
+                    8.0 * (double)mr * rest + 2.0 * ((double)mr + rest) * kp);
+        }
+      } else {
+        SL_TRY(lowp_gemm(fmt, mr, nr, jb, mw.A16, mw.B16, mw.col_exp, Fp(jn, jn), ldf, ws.status, s));
+        phase_end(kPhMixedGemm, s, 2.0 * mr * (double)nr * jb,
+                  8.0 * (double)mr * nr + 2.0 * ((double)mr + nr) * kp);
       }
     }
-    SL_TRY(laswp<float>(F, ldf, j, j + jb, dipiv, 0, j, j + jb, n, s));
-    if (j + jb < n)
-      SL_TRY((trsm_strip<float, false, false, true>(jb, n - j - jb, Fp(j, j), ldf, Fp(j, j + jb),
-                                                     ldf, s)));
-    phase_end(kPhMixedPanel, s, 0.0, 0.0);
-    if (j + jb < n && j + jb < m) {
-      const int mr = m - j - jb, nr = n - j - jb;
-      phase_begin(kPhMixedGemm, s);
-      SL_TRY(lowp_pack(fmt, Fp(j + jb, j), ldf, mr, Fp(j, j + jb), ldf, nr, jb, mw.A16, mw.B16,
-                       mw.col_exp, s));
-      SL_TRY(lowp_gemm(fmt, mr, nr, jb, mw.A16, mw.B16, mw.col_exp, Fp(j + jb, j + jb), ldf,
-                       ws.status, s));
-      const int kp = lowp_kpad(jb) * lowp_kmult(fmt);
-      phase_end(kPhMixedGemm, s, 2.0 * mr * (double)nr * jb,
-                8.0 * (double)mr * nr + 2.0 * ((double)mr + nr) * kp);
-    }
+    if (jb2 > 0 && !panel_on_aux) SL_TRY(factor_panel_f32(n, F, ldf, dipiv, jn, jb2, ws, s));
   }
+  if (panel_on_aux) SL_TRY(cudaStreamWaitEvent(s, ws.ev_panel, 0));
   return cudaGetLastError();
 }
 

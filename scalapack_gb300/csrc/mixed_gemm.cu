@@ -12,7 +12,7 @@
 // Blackwell-native structure, one 128 x 256 output tile per CTA (4 warps):
 //   * warp 0 allocates 256 TMEM columns (the FP32 accumulator, lane = row);
 //   * one thread issues TMA loads (cp.async.bulk.tensor, 128-byte swizzle) of
-//     the 128x64 A and 256x64 B k-blocks into a 4-stage shared-memory ring,
+//     the 128x64 A and 256x64 B k-blocks into a 3-stage shared-memory ring,
 //     completion tracked by mbarrier transaction counts;
 //   * one thread issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=256,
 //     K=16) per 16-wide k-slice and frees each stage with tcgen05.commit;
@@ -36,7 +36,7 @@ namespace {
 constexpr int BM = 128;
 constexpr int BN = 256;
 constexpr int BK = 64;       // 64 x 16-bit = 128 bytes: one swizzle row
-constexpr int STAGES = 4;
+constexpr int STAGES = 3;   // leaves room on each SM for the look-ahead panel's CTAs
 constexpr int A_STAGE_BYTES = BM * BK * 2;  // 16 KB
 constexpr int B_STAGE_BYTES = BN * BK * 2;  // 32 KB
 constexpr int TMEM_COLS = 256;

@@ -64,6 +64,11 @@ struct LuWork {
   double* bswap;     // n * nrhs doubles: gathered right-hand sides (solve)
   size_t perm_len;
   size_t bswap_len;
+  // Look-ahead resources (null: the factorization runs on the caller's
+  // stream only): a high-priority stream for the next panel and two events.
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_next = nullptr;
+  cudaEvent_t ev_panel = nullptr;
 };
 
 size_t panel_cand_doubles();
