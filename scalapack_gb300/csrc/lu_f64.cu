@@ -26,8 +26,8 @@
 
 namespace sl {
 
-size_t panel_cand_doubles() { return (size_t)2 * PMAXG * (PW + 2) + 2 * PW; }
-static_assert(kPanelCandDoubles == (size_t)2 * PMAXG * (PW + 2) + 2 * PW, "slot layout");
+size_t panel_cand_doubles() { return kPanelCandDoubles; }
+static_assert(kPanelCandDoubles == (size_t)2 * PMAXG * (PW + 2) + 2 * PW + PW + PW / 2, "slot layout");
 
 // Rows per CTA are capped by 200 KB of shared memory (rpc * 33 doubles),
 // rounded down to a multiple of 8: 768 rows; one CTA per SM.

@@ -62,12 +62,13 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
              int* info_col, double* cand, int* bar, int* status) {
   extern __shared__ __align__(16) unsigned char panel_smem[];
   T* tile = reinterpret_cast<T*>(panel_smem);  // [rpc][PLD]
-  __shared__ double s_U[PW], s_D[PW];
+  __shared__ double s_U[PW];
   __shared__ double s_wk[PT / 32];
   __shared__ int s_wr[PT / 32];
   __shared__ int s_row;
   __shared__ int s_piv;
-  __shared__ double s_gmax;
+  __shared__ int s_fail;
+  __shared__ double s_gkey;
 
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
@@ -76,10 +77,15 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
   const int lo = b * rpc;                   // first local row (relative to r0)
   const int nr = max(0, min(rpc, R - lo));  // rows owned
   double* diag = cand + (size_t)2 * PMAXG * (PW + 2);
+  // per-column election words and arrival counters (zeroed before the launch)
+  unsigned long long* elect = reinterpret_cast<unsigned long long*>(diag + 2 * PW);
+  int* arrive = reinterpret_cast<int*>(elect + PW);
+  (void)bar;
 
   for (int c = 0; c < w; ++c)
     for (int r = tid; r < nr; r += PT)
       tile[r * PLD + c] = A[(long long)(r0 + lo + r) + (long long)(c0 + c) * lda];
+  if (tid == 0) s_fail = 0;
   __syncthreads();
 
   for (int k = 0; k < kw; ++k) {
@@ -99,70 +105,95 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
       key = lane < PT / 32 ? s_wk[lane] : -2.0;
       row = lane < PT / 32 ? s_wr[lane] : INT_MAX;
       warp_amax(key, row);
-      if (lane == 0) {
-        s_row = row;
-        double* slot = cand + ((size_t)par * PMAXG + b) * (PW + 2);
-        slot[0] = key;
-        slot[1] = (double)row;
-      }
-    }
-    __syncthreads();
-    {
-      double* slot = cand + ((size_t)par * PMAXG + b) * (PW + 2);
-      int lr = s_row;
-      if (tid < w && lr != INT_MAX) slot[2 + tid] = (double)tile[(lr - lo) * PLD + tid];
-      if (d >= lo && d < lo + nr && tid < w) diag[par * PW + tid] = (double)tile[(d - lo) * PLD + tid];
-    }
-    __threadfence();
-    if (!grid_barrier(bar, G, status)) return;
-
-    // --- global winner (largest |x|, lowest row on ties) ---
-    key = -2.0;
-    row = INT_MAX;
-    for (int q = tid; q < G; q += PT) {
-      const double* slot = cand + ((size_t)par * PMAXG + q) * (PW + 2);
-      double k2 = __ldcg(slot);
-      double r2 = __ldcg(slot + 1);
-      int ri = (r2 >= (double)INT_MAX) ? INT_MAX : (int)r2;
-      amax_combine(key, row, k2, ri);
-    }
-    warp_amax(key, row);
-    if (lane == 0) { s_wk[warp] = key; s_wr[warp] = row; }
-    __syncthreads();
-    if (warp == 0) {
-      key = lane < PT / 32 ? s_wk[lane] : -2.0;
-      row = lane < PT / 32 ? s_wr[lane] : INT_MAX;
-      warp_amax(key, row);
       if (lane == 0) { s_row = row; s_wk[0] = key; }
     }
     __syncthreads();
-    const int grow = s_row;
-    const double gkey = s_wk[0];
-    if (tid < w) s_D[tid] = __ldcg(diag + par * PW + tid);
+    {
+      // publish this CTA's candidate row (and the diagonal row if owned)
+      double* slot = cand + ((size_t)par * PMAXG + b) * (PW + 2);
+      const int lr = s_row;
+      if (tid < w && lr != INT_MAX) slot[2 + tid] = (double)tile[(lr - lo) * PLD + tid];
+      if (d >= lo && d < lo + nr && tid < w) diag[par * PW + tid] = (double)tile[(d - lo) * PLD + tid];
+      if (tid == 0) {
+        slot[0] = s_wk[0];
+        slot[1] = (double)lr;
+        if (sizeof(T) == 4 && lr != INT_MAX) {
+          // FP32: elect the winner with one 64-bit atomicMax on (|x| bits, ~row):
+          // larger |x| wins, ties go to the lower row; NaN (key -1) ranks lowest.
+          const float kf = s_wk[0] >= 0.0 ? (float)s_wk[0] : 0.0f;
+          const unsigned long long hi = s_wk[0] >= 0.0 ? (unsigned long long)__float_as_uint(kf) + 1ULL : 0ULL;
+          const unsigned long long packed = (hi << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)lr);
+          atomicMax(&elect[k], packed);
+        }
+      }
+    }
+    // --- arrive at this column's counter and wait for all CTAs (bounded) ---
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      atomicAdd(&arrive[k], 1);
+      long long spins = 0;
+      while (ld_acquire_gpu(&arrive[k]) < G) {
+        if (++spins > kSpinLimit) { atomicExch(status, (int)kBarrierTimeout); s_fail = 1; break; }
+        if (spins > 32) __nanosleep(32);
+      }
+      __threadfence();
+    }
+    __syncthreads();
+    if (s_fail) return;
+
+    // --- global winner (largest |x|, lowest row on ties) ---
+    if (sizeof(T) == 4) {
+      if (tid == 0) {
+        const unsigned long long e = __ldcg(&elect[k]);
+        const unsigned hi = (unsigned)(e >> 32);
+        s_row = (int)(0xFFFFFFFFu - (unsigned)(e & 0xFFFFFFFFu));
+        s_gkey = hi == 0 ? -1.0 : (double)__uint_as_float(hi - 1);
+      }
+    } else {
+      key = -2.0;
+      row = INT_MAX;
+      for (int q = tid; q < G; q += PT) {
+        const double* slot = cand + ((size_t)par * PMAXG + q) * (PW + 2);
+        double k2 = __ldcg(slot);
+        double r2 = __ldcg(slot + 1);
+        int ri = (r2 >= (double)INT_MAX) ? INT_MAX : (int)r2;
+        amax_combine(key, row, k2, ri);
+      }
+      warp_amax(key, row);
+      if (lane == 0) { s_wk[warp] = key; s_wr[warp] = row; }
+      __syncthreads();
+      if (warp == 0) {
+        key = lane < PT / 32 ? s_wk[lane] : -2.0;
+        row = lane < PT / 32 ? s_wr[lane] : INT_MAX;
+        warp_amax(key, row);
+        if (lane == 0) { s_row = row; s_gkey = key; }
+      }
+    }
     __syncthreads();
     if (tid == 0) {
       // IDAMAX keeps the first element when it is NaN; AMAX == 0 selects the
       // diagonal row (PBLAS/SRC/pdamax_.c:486).
-      int piv = grow;
-      double dv = s_D[k];
-      if (dv != dv || gkey == 0.0) piv = d;
+      int piv = s_row;
+      const double dv = __ldcg(diag + par * PW + k);
+      if (dv != dv || s_gkey == 0.0) piv = d;
       s_piv = piv;
     }
     __syncthreads();
     const int piv = s_piv;
+    // U = the pivot row (from its owner's slot, or the diagonal row)
     if (tid < w) {
-      if (piv == d) s_U[tid] = s_D[tid];
+      if (piv == d) s_U[tid] = __ldcg(diag + par * PW + tid);
       else s_U[tid] = __ldcg(cand + ((size_t)par * PMAXG + piv / rpc) * (PW + 2) + 2 + tid);
     }
     __syncthreads();
-    if (tid == 0) s_gmax = s_U[k];
     // --- row interchange inside the sub-panel (PDSWAP, pdgetf2.f:218) ---
     if (piv != d && tid < w) {
       if (d >= lo && d < lo + nr) tile[(d - lo) * PLD + tid] = (T)s_U[tid];
-      if (piv >= lo && piv < lo + nr) tile[(piv - lo) * PLD + tid] = (T)s_D[tid];
+      if (piv >= lo && piv < lo + nr) tile[(piv - lo) * PLD + tid] = (T)__ldcg(diag + par * PW + tid);
     }
     __syncthreads();
-    const T gmax = (T)s_gmax;
+    const T gmax = (T)s_U[k];
     if (b == 0 && tid == 0) {
       ipiv[c0 + k] = r0 + piv;
       if (gmax == (T)0) atomicMin(info_col, c0 + k);
@@ -522,7 +553,9 @@ inline cudaError_t launch_panel(T* A, long long lda, int m, int r0, int c0, int 
   const size_t smem = sizeof(T) * (size_t)rpc * PLD;
   if (smem > 200 * 1024 || G > PMAXG) return cudaErrorInvalidValue;  // M beyond the panel limit
   SL_TRY(smem_attr_once((const void*)panel_kernel<T>, 200 * 1024));
-  cudaError_t e = cudaMemsetAsync(ws.bar, 0, 2 * sizeof(int), s);
+  // election words (PW x 8 bytes) and arrival counters (PW x 4 bytes) after the slots
+  cudaError_t e = cudaMemsetAsync(ws.cand + (size_t)2 * PMAXG * (PW + 2) + 2 * PW, 0,
+                                  (size_t)PW * (sizeof(unsigned long long) + sizeof(int)), s);
   if (e != cudaSuccess) return e;
   void* args[] = {&A, &lda, &m, &r0, &c0, &w, (void*)&rpc, &ipiv, (void*)&ws.info_col,
                   (void*)&ws.cand, (void*)&ws.bar, (void*)&ws.status};

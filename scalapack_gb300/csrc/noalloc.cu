@@ -32,8 +32,9 @@
 namespace {
 
 // Stated maximum of the static scratch: 1 MiB. It holds 4 ints at offset 0
-// (barrier arrival count and generation, status word, first zero-pivot column)
-// and the panel's candidate slots from offset 256.
+// (two words kept for the panel's synchronization, status word, first
+// zero-pivot column) and from offset 256 the panel's candidate slots, per-column
+// election words and arrival counters.
 constexpr size_t kScratchBytes = (size_t)1 << 20;
 constexpr size_t kCandOffset = 256;
 static_assert(kCandOffset + sl::kPanelCandDoubles * sizeof(double) <= kScratchBytes,

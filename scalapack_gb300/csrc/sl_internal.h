@@ -73,8 +73,9 @@ struct LuWork {
 
 size_t panel_cand_doubles();
 // Candidate-slot doubles the panel kernel needs (2 parities x 1024 CTAs x
-// (key, row, 32 values) + 2 diagonal rows); panel_cand_doubles() returns it.
-constexpr size_t kPanelCandDoubles = (size_t)2 * 1024 * (32 + 2) + 2 * 32;
+// (key, row, 32 values) + 2 diagonal rows + 32 election words + 32 arrival
+// counters); panel_cand_doubles() returns it.
+constexpr size_t kPanelCandDoubles = (size_t)2 * 1024 * (32 + 2) + 2 * 32 + 32 + 16;
 // Largest M the FP64 panel supports on this device (rows held in shared memory).
 int panel_max_rows();
 // Smallest row slice per CTA of the cooperative panel (tunable, default 512).
