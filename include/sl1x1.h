@@ -180,11 +180,17 @@ void sl1x1_set_default_nb(int nb);
 /* Look-ahead in the factorizations (default on): the next panel is factored
  * on a second stream while the trailing update runs. Same results either way. */
 void sl1x1_set_lookahead(int on);
-/* Smallest row slice per CTA of the cooperative panel kernel (8..768,
- * default 64, i.e. one CTA per SM for tall panels): larger slices mean fewer
- * CTAs per per-column grid barrier but more serial work per CTA. Changes only
- * the speed, not the results. */
+/* Smallest row slice per CTA of the cooperative panel kernel (8..768; 0, the
+ * default, picks 256 rows for the FP32 panel and 128 for the FP64 one, with
+ * about 64 CTAs for tall panels): larger slices mean fewer CTAs in each
+ * column's pivot exchange but a longer rank-1 update per CTA. Changes only the
+ * speed, not the results. */
 void sl1x1_set_panel_rows(int rows);
+/* Pipeline depth of the tcgen05 low-precision update used by the mixed
+ * factorization and sl1x1_lowp_update_dev: 3 (default; one CTA per SM) or 2
+ * (two CTAs per SM, one's epilogue overlapping the other's main loop). Changes
+ * only the speed, not the results. */
+void sl1x1_set_lowp_stages(int stages);
 /* 1 if the library found a usable sm_103 device, else 0. */
 int sl1x1_device_ok(void);
 /* Version string. */

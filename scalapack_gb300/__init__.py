@@ -108,6 +108,7 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_finalize.argtypes = []
     L.sl1x1_set_default_nb.argtypes = [C.c_int]
     L.sl1x1_set_panel_rows.argtypes = [C.c_int]
+    L.sl1x1_set_lowp_stages.argtypes = [C.c_int]
     L.sl1x1_set_lookahead.argtypes = [C.c_int]
     L.sl1x1_device_ok.restype = C.c_int
     L.sl1x1_version.restype = C.c_char_p

@@ -995,6 +995,11 @@ void sl1x1_set_panel_rows(int rows) {
   sl::set_panel_min_rows(rows);
 }
 
+void sl1x1_set_lowp_stages(int stages) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  sl::lowp_set_stages(stages);
+}
+
 void sl1x1_set_default_nb(int nb) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (nb > 0) g_default_nb = nb;

@@ -27,15 +27,15 @@
 namespace sl {
 
 size_t panel_cand_doubles() { return kPanelCandDoubles; }
-static_assert(kPanelCandDoubles == (size_t)2 * PMAXG * (PW + 2) + 2 * PW + PW + PW / 2, "slot layout");
+static_assert(kPanelCandDoubles == (size_t)PX_WORDS, "exchange area layout");
 
 // Rows per CTA are capped by 200 KB of shared memory (rpc * 33 doubles),
 // rounded down to a multiple of 8: 768 rows; one CTA per SM.
 int panel_max_rows() { return num_sms() * 768; }
 
-static int g_panel_min_rows = 64;
+static int g_panel_min_rows = 0;  // 0: automatic (FP32 256, FP64 128)
 int panel_min_rows() { return g_panel_min_rows; }
-void set_panel_min_rows(int rows) { g_panel_min_rows = rows < 8 ? 8 : (rows > 768 ? 768 : rows); }
+void set_panel_min_rows(int rows) { g_panel_min_rows = rows <= 0 ? 0 : (rows < 8 ? 8 : (rows > 768 ? 768 : rows)); }
 
 SplitKScratch& splitk_scratch() {
   static SplitKScratch sc;

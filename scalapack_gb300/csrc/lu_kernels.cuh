@@ -7,6 +7,7 @@
 //   permute_rows_kernel<T>, gemm_skinny_kernel<T>  PDLAPIV and the narrow
 //                        off-diagonal updates of PDGETRS
 #pragma once
+#include <algorithm>
 #include <climits>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -41,7 +42,16 @@ inline cudaError_t smem_attr_once(const void* kern, int bytes) {
 }  // namespace
 
 constexpr int PW = 32;       // sub-panel width held in shared memory
-constexpr int PMAXG = 1024;  // max CTAs of the panel kernel
+constexpr int PMAXG = 224;   // max CTAs of the panel kernel (warp 7 reads the diagonal row)
+// Exchange area of the panel kernel, in 8-byte tagged words: the diagonal
+// rows [2 parities][2*PW], the candidate keys [2 parities][PMAXG][4] (|x| key
+// lo, key hi, row, spare: one 32-byte sector per CTA, so that CTAs do not
+// write into each other's sectors) and the candidate rows
+// [PMAXG][2 parities][2*PW].
+constexpr int PX_DIAG = 0;
+constexpr int PX_KEYS = 4 * PW;
+constexpr int PX_VALS = PX_KEYS + 8 * PMAXG;
+constexpr int PX_WORDS = PX_VALS + PMAXG * 2 * 2 * PW;
 constexpr int PT = 256;      // threads per panel CTA
 constexpr int PLD = PW + 1;  // shared row stride: conflict-free row and column walks
 
@@ -56,19 +66,114 @@ constexpr int PLD = PW + 1;  // shared row stride: conflict-free row and column 
 // (reciprocal then multiply, SRC/pdgetf2.f:224) and applies the rank-1 update
 // with lanes = columns. Writes ipiv[c0+k] = r0 + pivot (0-based rows of A) for
 // k < min(w, m-r0) and the first exactly-zero pivot column into *info_col.
+// Tagged 8-byte words {32-bit payload, 32-bit tag} carry the per-column
+// exchange between the panel's CTAs: a word is valid once its tag equals the
+// column's tag, so readers poll the data itself and no separate grid barrier
+// or fence is needed (each aligned 8-byte access is single-copy atomic).
+__device__ __forceinline__ void st_tagged(unsigned long long* p, uint32_t v, uint32_t tag) {
+  const unsigned long long wd = ((unsigned long long)tag << 32) | v;
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(wd) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_tagged(const unsigned long long* p) {
+  unsigned long long wd;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(wd) : "l"(p) : "memory");
+  return wd;
+}
+__device__ __forceinline__ void ld_tagged2(const unsigned long long* p, unsigned long long& a,
+                                           unsigned long long& b) {
+  asm volatile("ld.relaxed.gpu.global.v2.b64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
+}
+__device__ __forceinline__ bool tag_ok(unsigned long long wd, uint32_t tag) {
+  return (uint32_t)(wd >> 32) == tag;
+}
+__device__ __forceinline__ uint32_t payload(unsigned long long wd) { return (uint32_t)wd; }
+__device__ __forceinline__ unsigned long long join(unsigned long long lo, unsigned long long hi) {
+  return ((unsigned long long)payload(hi) << 32) | payload(lo);
+}
+
+// Value v of a row as tagged words (FP32: one word, FP64: two).
+template <typename T>
+__device__ __forceinline__ void st_value(unsigned long long* p, int j, T v, uint32_t tag) {
+  if constexpr (sizeof(T) == 4) {
+    st_tagged(p + j, __float_as_uint(v), tag);
+  } else {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    st_tagged(p + 2 * j, (uint32_t)b, tag);
+    st_tagged(p + 2 * j + 1, (uint32_t)(b >> 32), tag);
+  }
+}
+
+// Polls value j of a published row until its tag matches; false on timeout.
+template <typename T>
+__device__ __forceinline__ bool ld_value(const unsigned long long* p, int j, uint32_t tag, T& v) {
+  for (long long spins = 0; spins <= kSpinLimit; ++spins) {
+    if constexpr (sizeof(T) == 4) {
+      const unsigned long long a = ld_tagged(p + j);
+      if (tag_ok(a, tag)) { v = __uint_as_float(payload(a)); return true; }
+    } else {
+      unsigned long long a0, a1;
+      ld_tagged2(p + 2 * j, a0, a1);
+      if (tag_ok(a0, tag) && tag_ok(a1, tag)) { v = __longlong_as_double((long long)join(a0, a1)); return true; }
+    }
+  }
+  return false;
+}
+
+// IDAMAX key of a value: the bit pattern of |x| as an integer (monotonic in
+// |x| for IEEE formats, +0 and -0 equal), -1 for NaN so that NaN never wins.
+// Integer keys keep the pivot search off the FP64 pipe.
+__device__ __forceinline__ long long amax_ikey(double v) {
+  const long long b = __double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFLL;
+  return b > 0x7FF0000000000000LL ? -1LL : b;
+}
+__device__ __forceinline__ long long amax_ikey(float v) {
+  const int b = __float_as_int(v) & 0x7FFFFFFF;
+  return b > 0x7F800000 ? -1LL : (long long)b;
+}
+// Larger key wins, ties go to the lower row (IDAMAX returns the first max).
+__device__ __forceinline__ void ikey_combine(long long& k, int& r, long long k2, int r2) {
+  if (k2 > k || (k2 == k && r2 < r)) { k = k2; r = r2; }
+}
+__device__ __forceinline__ void warp_ikey(long long& k, int& r) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const long long k2 = __shfl_xor_sync(0xffffffffu, k, off);
+    const int r2 = __shfl_xor_sync(0xffffffffu, r, off);
+    ikey_combine(k, r, k2, r2);
+  }
+}
+
+// Cooperative unblocked LU of a sub-panel (PDGETF2, SRC/pdgetf2.f:206-237)
+// over rows r0..m-1 and columns c0..c0+w-1 of A, w <= PW. CTA b owns rows
+// r0 + b*rpc .. +rpc-1 in shared memory. Per column k:
+//   1. each CTA's IDAMAX candidate (first max, NaN never wins --
+//      PBLAS/SRC/pdamax_.c:414-486 through idamax_) is published as tagged
+//      words: its key and row, and the candidate row itself; the owner of the
+//      diagonal row publishes that row too;
+//   2. every CTA polls all keys (thread q reads CTA q's sector) until the
+//      tags match, reduces to the global winner (largest |x|, lowest row on
+//      ties) and then reads the pivot row from the winner's slot;
+//   3. rows d and piv are exchanged inside the sub-panel, the column is scaled
+//      by the reciprocal of the pivot and the rank-1 update is applied
+//      (PDSWAP/PDSCAL/PDGER, pdgetf2.f:218-233) with one thread per row, which
+//      also forms the next column's IDAMAX key.
+// Column k's words carry tag k+1 and the launch zeroes the area first. A word
+// of parity k&1 is rewritten only at column k+2, after every CTA has read
+// column k+1 -- which it can only do after finishing column k -- so two
+// parities suffice. Every poll is bounded.
 template <typename T>
 __global__ void __launch_bounds__(PT)
 panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ipiv,
-             int* info_col, double* cand, int* bar, int* status) {
+             int* info_col, double* cand, int* status) {
   extern __shared__ __align__(16) unsigned char panel_smem[];
   T* tile = reinterpret_cast<T*>(panel_smem);  // [rpc][PLD]
-  __shared__ double s_U[PW];
-  __shared__ double s_wk[PT / 32];
+  __shared__ T s_U[PW];
+  __shared__ T s_D[PW];
+  __shared__ long long s_wk[PT / 32];
   __shared__ int s_wr[PT / 32];
-  __shared__ int s_row;
-  __shared__ int s_piv;
-  __shared__ int s_fail;
-  __shared__ double s_gkey;
+  __shared__ int s_lrow, s_row, s_fail, s_scale;
+  __shared__ long long s_lkey, s_gkey;
+  __shared__ T s_rinv;
 
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
@@ -76,166 +181,177 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
   const int kw = min(w, R);
   const int lo = b * rpc;                   // first local row (relative to r0)
   const int nr = max(0, min(rpc, R - lo));  // rows owned
-  double* diag = cand + (size_t)2 * PMAXG * (PW + 2);
-  // per-column election words and arrival counters (zeroed before the launch)
-  unsigned long long* elect = reinterpret_cast<unsigned long long*>(diag + 2 * PW);
-  int* arrive = reinterpret_cast<int*>(elect + PW);
-  (void)bar;
+  unsigned long long* words = reinterpret_cast<unsigned long long*>(cand);
+  unsigned long long* diagw = words + PX_DIAG;
+  unsigned long long* keyw = words + PX_KEYS;
+  unsigned long long* valw = words + PX_VALS;
 
-  for (int c = 0; c < w; ++c)
-    for (int r = tid; r < nr; r += PT)
-      tile[r * PLD + c] = A[(long long)(r0 + lo + r) + (long long)(c0 + c) * lda];
+  // Sub-panel rows into shared memory, all w columns' loads in flight at once.
+  for (int r = tid; r < nr; r += PT) {
+    const T* src = A + (long long)(r0 + lo + r) + (long long)c0 * lda;
+    T v[PW];
+#pragma unroll
+    for (int c = 0; c < PW; ++c) v[c] = (c < w) ? src[(long long)c * lda] : (T)0;
+#pragma unroll
+    for (int c = 0; c < PW; ++c)
+      if (c < w) tile[r * PLD + c] = v[c];
+  }
   if (tid == 0) s_fail = 0;
+
+  // Per-warp IDAMAX candidates of column 0; those of column k+1 come out of
+  // column k's rank-1 update.
+  {
+    long long key = -2;
+    int row = INT_MAX;
+    for (int r = tid; r < nr; r += PT) ikey_combine(key, row, amax_ikey(tile[r * PLD]), lo + r);  // own rows
+    warp_ikey(key, row);
+    if (lane == 0) { s_wk[warp] = key; s_wr[warp] = row; }
+  }
   __syncthreads();
 
   for (int k = 0; k < kw; ++k) {
     const int d = k;  // diagonal row relative to r0
     const int par = k & 1;
-    // --- local IDAMAX over owned rows >= d ---
-    double key = -2.0;
-    int row = INT_MAX;
-    for (int r = tid; r < nr; r += PT) {
-      int gr = lo + r;
-      if (gr >= d) amax_combine(key, row, amax_key((double)tile[r * PLD + k]), gr);
-    }
-    warp_amax(key, row);
-    if (lane == 0) { s_wk[warp] = key; s_wr[warp] = row; }
-    __syncthreads();
+    const uint32_t tag = (uint32_t)(k + 1);
+    // --- this CTA's candidate: IDAMAX over its rows >= d ---
     if (warp == 0) {
-      key = lane < PT / 32 ? s_wk[lane] : -2.0;
-      row = lane < PT / 32 ? s_wr[lane] : INT_MAX;
-      warp_amax(key, row);
-      if (lane == 0) { s_row = row; s_wk[0] = key; }
+      long long key = lane < PT / 32 ? s_wk[lane] : -2;
+      int row = lane < PT / 32 ? s_wr[lane] : INT_MAX;
+      warp_ikey(key, row);
+      if (lane == 0) { s_lrow = row; s_lkey = key; }
     }
     __syncthreads();
     {
-      // publish this CTA's candidate row (and the diagonal row if owned)
-      double* slot = cand + ((size_t)par * PMAXG + b) * (PW + 2);
-      const int lr = s_row;
-      if (tid < w && lr != INT_MAX) slot[2 + tid] = (double)tile[(lr - lo) * PLD + tid];
-      if (d >= lo && d < lo + nr && tid < w) diag[par * PW + tid] = (double)tile[(d - lo) * PLD + tid];
+      // publish the candidate row, the diagonal row (if owned) and the key
+      const int lr = s_lrow;
+      if (tid < w)
+        st_value<T>(valw + ((size_t)b * 2 + par) * 2 * PW, tid,
+                    lr != INT_MAX ? tile[(lr - lo) * PLD + tid] : (T)0, tag);
+      if (d >= lo && d < lo + nr && tid < w)
+        st_value<T>(diagw + par * 2 * PW, tid, tile[(d - lo) * PLD + tid], tag);
       if (tid == 0) {
-        slot[0] = s_wk[0];
-        slot[1] = (double)lr;
-        if (sizeof(T) == 4 && lr != INT_MAX) {
-          // FP32: elect the winner with one 64-bit atomicMax on (|x| bits, ~row):
-          // larger |x| wins, ties go to the lower row; NaN (key -1) ranks lowest.
-          const float kf = s_wk[0] >= 0.0 ? (float)s_wk[0] : 0.0f;
-          const unsigned long long hi = s_wk[0] >= 0.0 ? (unsigned long long)__float_as_uint(kf) + 1ULL : 0ULL;
-          const unsigned long long packed = (hi << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)lr);
-          atomicMax(&elect[k], packed);
-        }
+        const unsigned long long kb = (unsigned long long)s_lkey;
+        unsigned long long* kw4 = keyw + ((size_t)par * PMAXG + b) * 4;
+        st_tagged(kw4 + 0, (uint32_t)kb, tag);
+        st_tagged(kw4 + 1, (uint32_t)(kb >> 32), tag);
+        st_tagged(kw4 + 2, (uint32_t)lr, tag);
       }
     }
-    // --- arrive at this column's counter and wait for all CTAs (bounded) ---
-    __syncthreads();
-    if (tid == 0) {
-      __threadfence();
-      atomicAdd(&arrive[k], 1);
+
+    // --- poll every CTA's key (thread q <- CTA q) and the diagonal row (warp 7);
+    //     the polls spin without sleeping (a sleep costs more than it saves
+    //     here), bounded by kSpinLimit ---
+    long long key = -2;
+    int row = INT_MAX;
+    if (tid < G) {
       long long spins = 0;
-      while (ld_acquire_gpu(&arrive[k]) < G) {
-        if (++spins > kSpinLimit) { atomicExch(status, (int)kBarrierTimeout); s_fail = 1; break; }
-        if (spins > 32) __nanosleep(32);
+      for (;;) {
+        unsigned long long w0, w1, w2, w3;
+        ld_tagged2(keyw + ((size_t)tid + (size_t)par * PMAXG) * 4, w0, w1);
+        ld_tagged2(keyw + ((size_t)tid + (size_t)par * PMAXG) * 4 + 2, w2, w3);
+        if (tag_ok(w0, tag) && tag_ok(w1, tag) && tag_ok(w2, tag)) {
+          key = (long long)join(w0, w1);
+          const uint32_t rr = payload(w2);
+          row = rr >= (uint32_t)INT_MAX ? INT_MAX : (int)rr;
+          break;
+        }
+        if (++spins > kSpinLimit) { atomicExch(status, (int)kFlagTimeout); s_fail = 1; break; }
       }
-      __threadfence();
+    } else if (warp == PT / 32 - 1 && lane < w) {
+      T v;
+      if (ld_value<T>(diagw + par * 2 * PW, lane, tag, v)) s_D[lane] = v;
+      else { atomicExch(status, (int)kFlagTimeout); s_fail = 1; }
+    }
+    warp_ikey(key, row);
+    if (lane == 0) { s_wk[warp] = key; s_wr[warp] = row; }
+    __syncthreads();
+    if (s_fail) return;
+    if (warp == 0) {
+      key = lane < PT / 32 ? s_wk[lane] : -2;
+      row = lane < PT / 32 ? s_wr[lane] : INT_MAX;
+      warp_ikey(key, row);
+      if (lane == 0) { s_row = row; s_gkey = key; }
+    }
+    __syncthreads();
+    // IDAMAX keeps the first element when it is NaN; AMAX == 0 selects the
+    // diagonal row (PBLAS/SRC/pdamax_.c:486).
+    const int piv = (amax_ikey(s_D[k]) < 0 || s_gkey == 0) ? d : s_row;
+    // U = the pivot row: the diagonal row, or the winner's published row
+    if (tid < w) {
+      if (piv == d) {
+        s_U[tid] = s_D[tid];
+      } else {
+        T v;
+        if (ld_value<T>(valw + ((size_t)(piv / rpc) * 2 + par) * 2 * PW, tid, tag, v)) s_U[tid] = v;
+        else { atomicExch(status, (int)kFlagTimeout); s_fail = 1; }
+      }
     }
     __syncthreads();
     if (s_fail) return;
-
-    // --- global winner (largest |x|, lowest row on ties) ---
-    if (sizeof(T) == 4) {
-      if (tid == 0) {
-        const unsigned long long e = __ldcg(&elect[k]);
-        const unsigned hi = (unsigned)(e >> 32);
-        s_row = (int)(0xFFFFFFFFu - (unsigned)(e & 0xFFFFFFFFu));
-        s_gkey = hi == 0 ? -1.0 : (double)__uint_as_float(hi - 1);
-      }
-    } else {
-      key = -2.0;
-      row = INT_MAX;
-      for (int q = tid; q < G; q += PT) {
-        const double* slot = cand + ((size_t)par * PMAXG + q) * (PW + 2);
-        double k2 = __ldcg(slot);
-        double r2 = __ldcg(slot + 1);
-        int ri = (r2 >= (double)INT_MAX) ? INT_MAX : (int)r2;
-        amax_combine(key, row, k2, ri);
-      }
-      warp_amax(key, row);
-      if (lane == 0) { s_wk[warp] = key; s_wr[warp] = row; }
-      __syncthreads();
-      if (warp == 0) {
-        key = lane < PT / 32 ? s_wk[lane] : -2.0;
-        row = lane < PT / 32 ? s_wr[lane] : INT_MAX;
-        warp_amax(key, row);
-        if (lane == 0) { s_row = row; s_gkey = key; }
-      }
-    }
-    __syncthreads();
-    if (tid == 0) {
-      // IDAMAX keeps the first element when it is NaN; AMAX == 0 selects the
-      // diagonal row (PBLAS/SRC/pdamax_.c:486).
-      int piv = s_row;
-      const double dv = __ldcg(diag + par * PW + k);
-      if (dv != dv || s_gkey == 0.0) piv = d;
-      s_piv = piv;
-    }
-    __syncthreads();
-    const int piv = s_piv;
-    // U = the pivot row (from its owner's slot, or the diagonal row)
-    if (tid < w) {
-      if (piv == d) s_U[tid] = __ldcg(diag + par * PW + tid);
-      else s_U[tid] = __ldcg(cand + ((size_t)par * PMAXG + piv / rpc) * (PW + 2) + 2 + tid);
-    }
-    __syncthreads();
     // --- row interchange inside the sub-panel (PDSWAP, pdgetf2.f:218) ---
     if (piv != d && tid < w) {
-      if (d >= lo && d < lo + nr) tile[(d - lo) * PLD + tid] = (T)s_U[tid];
-      if (piv >= lo && piv < lo + nr) tile[(piv - lo) * PLD + tid] = (T)__ldcg(diag + par * PW + tid);
+      if (d >= lo && d < lo + nr) tile[(d - lo) * PLD + tid] = s_U[tid];
+      if (piv >= lo && piv < lo + nr) tile[(piv - lo) * PLD + tid] = s_D[tid];
+    }
+    if (tid == 0) {
+      const T gmax = s_U[k];
+      s_scale = (gmax != (T)0);
+      s_rinv = (gmax != (T)0) ? (T)1 / gmax : (T)0;  // ONE/GMAX (pdgetf2.f:224)
+      if (b == 0) {
+        ipiv[c0 + k] = r0 + piv;
+        if (gmax == (T)0) atomicMin(info_col, c0 + k);
+      }
     }
     __syncthreads();
-    const T gmax = (T)s_U[k];
-    if (b == 0 && tid == 0) {
-      ipiv[c0 + k] = r0 + piv;
-      if (gmax == (T)0) atomicMin(info_col, c0 + k);
-    }
-    // --- scale by ONE/GMAX (PDSCAL, pdgetf2.f:224) and rank-1 update (PDGER) ---
-    const bool scale = (gmax != (T)0);
-    const T rinv = scale ? (T)1 / gmax : (T)0;
-    const T u = (lane < w) ? (T)s_U[lane] : (T)0;
-    for (int r = warp; r < nr; r += PT / 32) {
-      int gr = lo + r;
-      if (gr <= d) continue;
-      T l = tile[r * PLD + k];
+    // --- scale (PDSCAL) and rank-1 update (PDGER), one thread per row; the
+    //     row's next-column entry gives its IDAMAX key for column k+1 ---
+    const bool scale = s_scale != 0;
+    const T rinv = s_rinv;
+    const int kn = k + 1;
+    long long nkey = -2;
+    int nrow = INT_MAX;
+    for (int r = max(0, d + 1 - lo) + tid; r < nr; r += PT) {
+      T* rp = tile + r * PLD;
+      T l = rp[k];
       if (scale) l *= rinv;
-      __syncwarp();
-      if (lane == k) tile[r * PLD + k] = l;
-      else if (lane > k && lane < w) tile[r * PLD + lane] = fma(-l, u, tile[r * PLD + lane]);
+      rp[k] = l;
+#pragma unroll 4
+      for (int j = kn; j < w; ++j) rp[j] = fma(-l, s_U[j], rp[j]);
+      if (kn < kw) ikey_combine(nkey, nrow, amax_ikey(rp[kn]), lo + r);
+    }
+    if (kn < kw) {
+      warp_ikey(nkey, nrow);
+      if (lane == 0) { s_wk[warp] = nkey; s_wr[warp] = nrow; }
     }
     __syncthreads();
   }
 
-  for (int c = 0; c < w; ++c)
-    for (int r = tid; r < nr; r += PT)
-      A[(long long)(r0 + lo + r) + (long long)(c0 + c) * lda] = tile[r * PLD + c];
+  for (int r = tid; r < nr; r += PT) {
+    T* dst = A + (long long)(r0 + lo + r) + (long long)c0 * lda;
+    T v[PW];
+#pragma unroll
+    for (int c = 0; c < PW; ++c) v[c] = (c < w) ? tile[r * PLD + c] : (T)0;
+#pragma unroll
+    for (int c = 0; c < PW; ++c)
+      if (c < w) dst[(long long)c * lda] = v[c];
+  }
 }
 
 // Sequential row interchanges k1..k2-1 (rows i <-> ipiv[i]) on the columns
 // [cb1,ce1) and [cb2,ce2); one thread per column (PDLASWP 'Forward','Rows').
+// Used when the interchanges outnumber the composite form's table.
 template <typename T>
 __global__ void __launch_bounds__(256)
-laswp_kernel(T* A, long long lda, int k1, int k2, const int* __restrict__ ipiv, int cb1, int ce1,
-             int cb2, int ce2) {
-  __shared__ int s_piv[1024];
+laswp_seq_kernel(T* A, long long lda, int k1, int k2, const int* __restrict__ ipiv, int cb1,
+                 int ce1, int cb2, int ce2) {
   const int npiv = k2 - k1;
-  for (int i = threadIdx.x; i < npiv && i < 1024; i += blockDim.x) s_piv[i] = ipiv[k1 + i];
-  __syncthreads();
   const long long n1 = ce1 - cb1, n2 = ce2 - cb2;
   long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n1 + n2) return;
   long long col = idx < n1 ? cb1 + idx : cb2 + (idx - n1);
   T* a = A + col * lda;
   for (int i = 0; i < npiv; ++i) {
-    int p = i < 1024 ? s_piv[i] : ipiv[k1 + i];
+    int p = ipiv[k1 + i];
     int r = k1 + i;
     if (p != r) {
       T t = a[r];
@@ -245,17 +361,100 @@ laswp_kernel(T* A, long long lda, int k1, int k2, const int* __restrict__ ipiv, 
   }
 }
 
+// The same interchanges applied as one composite permutation (PDLASWP
+// 'Forward','Rows', SRC/pdlaswp.f:163-172): warp 0 of each CTA replays the
+// swaps on row labels in shared memory -- entries for rows k1..k2-1 plus the
+// pivot rows below them -- giving, for every touched row, the row whose
+// original content ends up there. Then one warp per column loads all moved
+// values at once and stores them, so a column costs one round trip instead of
+// k2-k1 dependent ones. The result is bitwise that of the sequential swaps.
+constexpr int LSW_MAXP = 256;
+template <typename T>
+__global__ void __launch_bounds__(256)
+laswp_kernel(T* A, long long lda, int k1, int k2, const int* __restrict__ ipiv, int cb1, int ce1,
+             int cb2, int ce2) {
+  __shared__ int s_piv[LSW_MAXP];
+  __shared__ int s_row[2 * LSW_MAXP];  // touched row of entry e
+  __shared__ int s_src[2 * LSW_MAXP];  // row whose original content lands in s_row[e]
+  __shared__ int s_cnt;
+  const int npiv = k2 - k1;  // <= LSW_MAXP (checked by the launcher)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < npiv; i += blockDim.x) {
+    s_piv[i] = ipiv[k1 + i];
+    s_row[i] = k1 + i;
+    s_src[i] = k1 + i;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    int cnt = npiv;
+    for (int i = 0; i < npiv; ++i) {
+      const int p = s_piv[i];
+      if (p == k1 + i) continue;
+      int e;
+      if (p >= k1 && p < k2) {
+        e = p - k1;
+      } else {
+        e = -1;
+        for (int base = npiv; base < cnt && e < 0; base += 32) {
+          const int q = base + lane;
+          const unsigned hit = __ballot_sync(0xffffffffu, q < cnt && s_row[q] == p);
+          if (hit) e = base + __ffs(hit) - 1;
+        }
+        if (e < 0) {
+          e = cnt++;
+          if (lane == 0) { s_row[e] = p; s_src[e] = p; }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) {
+        const int t = s_src[i];
+        s_src[i] = s_src[e];
+        s_src[e] = t;
+      }
+      __syncwarp();
+    }
+    if (lane == 0) s_cnt = cnt;
+  }
+  __syncthreads();
+  const int cnt = s_cnt;
+  const long long n1 = ce1 - cb1, ncols = n1 + (ce2 - cb2);
+  constexpr int PER = 2 * LSW_MAXP / 32;
+  for (long long ci = (long long)blockIdx.x * 8 + warp; ci < ncols; ci += (long long)gridDim.x * 8) {
+    const long long col = ci < n1 ? cb1 + ci : cb2 + (ci - n1);
+    T* a = A + col * lda;
+    T v[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int e = lane + 32 * q;
+      v[q] = (e < cnt && s_src[e] != s_row[e]) ? a[s_src[e]] : (T)0;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int e = lane + 32 * q;
+      if (e < cnt && s_src[e] != s_row[e]) a[s_row[e]] = v[q];
+    }
+  }
+}
+
 // op(T) X = B for a w x w triangle (w <= 256) and a strip of NC columns of B
 // per CTA, held in shared memory. FORWARD solves top-down (lower, or upper^T),
-// otherwise bottom-up. Non-unit diagonals divide (reference DTRSM semantics).
+// otherwise bottom-up. The triangle is staged in shared memory eb (<= 32)
+// columns at a time (all loads of a block in flight together), so the w
+// dependent steps read only shared memory. Non-unit diagonals divide
+// (reference DTRSM semantics).
+constexpr int TRSM_EB = 32;
 template <typename T, bool UPPER, bool TRANS, bool UNIT, int NC>
 __global__ void __launch_bounds__(256)
-trsm_strip_kernel(int w, int ncols, const T* __restrict__ Tm, long long ldt, T* B, long long ldb) {
+trsm_strip_kernel(int w, int ncols, int eb, const T* __restrict__ Tm, long long ldt, T* B,
+                  long long ldb) {
   constexpr bool FORWARD = (UPPER == TRANS);
   constexpr int RG = 256 / NC;  // row groups
   extern __shared__ __align__(16) unsigned char strip_smem[];
   T* Bs = reinterpret_cast<T*>(strip_smem);  // [w][NC+1]
   const int LD = NC + 1;
+  T* Es = Bs + (size_t)w * LD;                // [eb][w+1]: Es[ii*(w+1) + r] = op(T)(r, i(ii))
+  const int LE = w + 1;
   const int tid = threadIdx.x;
   const int c = tid % NC, rg = tid / NC;
   const long long col0 = (long long)blockIdx.x * NC;
@@ -264,23 +463,32 @@ trsm_strip_kernel(int w, int ncols, const T* __restrict__ Tm, long long ldt, T* 
     int r = i % w, cc = i / w;
     Bs[r * LD + cc] = cc < nc ? B[r + (col0 + cc) * ldb] : (T)0;
   }
-  __syncthreads();
-  auto E = [&](int i, int j) -> T {
-    return TRANS ? Tm[j + (long long)i * ldt] : Tm[i + (long long)j * ldt];
-  };
-  for (int s = 0; s < w; ++s) {
-    const int i = FORWARD ? s : w - 1 - s;
-    if (!UNIT) {
-      if (tid < NC) Bs[i * LD + tid] = Bs[i * LD + tid] / E(i, i);
-      __syncthreads();
-    }
-    const T xi = Bs[i * LD + c];
-    if (FORWARD) {
-      for (int r = i + 1 + rg; r < w; r += RG) Bs[r * LD + c] = fma(-E(r, i), xi, Bs[r * LD + c]);
-    } else {
-      for (int r = rg; r < i; r += RG) Bs[r * LD + c] = fma(-E(r, i), xi, Bs[r * LD + c]);
+  for (int s0 = 0; s0 < w; s0 += eb) {
+    const int nb = min(eb, w - s0);
+    __syncthreads();  // the previous block's steps are done with Es
+    for (int idx = tid; idx < nb * w; idx += 256) {
+      int ii, r;
+      if (!TRANS) { r = idx % w; ii = idx / w; }    // coalesced along r
+      else { ii = idx % nb; r = idx / nb; }         // coalesced along i
+      const int i = FORWARD ? s0 + ii : w - 1 - (s0 + ii);
+      Es[ii * LE + r] = TRANS ? Tm[i + (long long)r * ldt] : Tm[r + (long long)i * ldt];
     }
     __syncthreads();
+    for (int ii = 0; ii < nb; ++ii) {
+      const int i = FORWARD ? s0 + ii : w - 1 - (s0 + ii);
+      const T* Ei = Es + ii * LE;
+      if (!UNIT) {
+        if (tid < NC) Bs[i * LD + tid] = Bs[i * LD + tid] / Ei[i];
+        __syncthreads();
+      }
+      const T xi = Bs[i * LD + c];
+      if (FORWARD) {
+        for (int r = i + 1 + rg; r < w; r += RG) Bs[r * LD + c] = fma(-Ei[r], xi, Bs[r * LD + c]);
+      } else {
+        for (int r = rg; r < i; r += RG) Bs[r * LD + c] = fma(-Ei[r], xi, Bs[r * LD + c]);
+      }
+      __syncthreads();
+    }
   }
   for (int i = tid; i < w * NC; i += 256) {
     int r = i % w, cc = i / w;
@@ -542,23 +750,27 @@ template <typename T>
 inline cudaError_t launch_panel(T* A, long long lda, int m, int r0, int c0, int w, int* ipiv,
                                 const LuWork& ws, cudaStream_t s) {
   const int R = m - r0;
-  const int nsm = num_sms();
-  // Rows per CTA: at least kPanelMinRows so that the per-column grid barrier
-  // and the candidate exchange involve few CTAs (the panel is latency-bound:
-  // a column's arithmetic is small next to one barrier round trip).
-  int rpc = (R + nsm - 1) / nsm;
-  if (rpc < panel_min_rows()) rpc = panel_min_rows();
+  // Rows per CTA: about 64 CTAs per panel, and at least the type's minimum
+  // (FP32 256, FP64 128, or the tuning knob). Fewer CTAs make the per-column
+  // exchange cheaper (fewer keys to poll, less cross-die skew); more rows per
+  // CTA make the rank-1 update longer -- on GB300's FP64 pipe sooner than on
+  // the FP32 one.
+  // Tall panels beyond 64 CTAs' shared memory spread over every SM instead.
+  const int rpc_max = (int)((200 * 1024) / (sizeof(T) * PLD)) & ~7;
+  int rpc = (R + 63) / 64;
+  const int lo_rows = panel_min_rows() > 0 ? panel_min_rows() : (sizeof(T) == 4 ? 256 : 128);
+  if (rpc < lo_rows) rpc = lo_rows;
+  if (rpc > rpc_max) rpc = (R + num_sms() - 1) / num_sms();
   rpc = (rpc + 7) & ~7;
   const int G = (R + rpc - 1) / rpc;
   const size_t smem = sizeof(T) * (size_t)rpc * PLD;
   if (smem > 200 * 1024 || G > PMAXG) return cudaErrorInvalidValue;  // M beyond the panel limit
   SL_TRY(smem_attr_once((const void*)panel_kernel<T>, 200 * 1024));
-  // election words (PW x 8 bytes) and arrival counters (PW x 4 bytes) after the slots
-  cudaError_t e = cudaMemsetAsync(ws.cand + (size_t)2 * PMAXG * (PW + 2) + 2 * PW, 0,
-                                  (size_t)PW * (sizeof(unsigned long long) + sizeof(int)), s);
+  // zero the diagonal rows and the G slots used (stale tags must not match)
+  cudaError_t e = cudaMemsetAsync(ws.cand, 0, sizeof(unsigned long long) * ((size_t)PX_VALS + (size_t)G * 2 * 2 * PW), s);
   if (e != cudaSuccess) return e;
   void* args[] = {&A, &lda, &m, &r0, &c0, &w, (void*)&rpc, &ipiv, (void*)&ws.info_col,
-                  (void*)&ws.cand, (void*)&ws.bar, (void*)&ws.status};
+                  (void*)&ws.cand, (void*)&ws.status};
   count_launches(1);
   return cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(PT), args, smem, s);
 }
@@ -568,8 +780,16 @@ inline cudaError_t laswp(T* A, long long lda, int k1, int k2, const int* ipiv, i
                          int cb2, int ce2, cudaStream_t s) {
   const long long ncols = (long long)(ce1 - cb1) + (ce2 - cb2);
   if (ncols <= 0 || k2 <= k1) return cudaSuccess;
-  dim3 grid((unsigned)((ncols + 255) / 256));
-  laswp_kernel<T><<<grid, 256, 0, s>>>(A, lda, k1, k2, ipiv, cb1, ce1, cb2, ce2);
+  if (k2 - k1 > LSW_MAXP) {
+    dim3 grid((unsigned)((ncols + 255) / 256));
+    laswp_seq_kernel<T><<<grid, 256, 0, s>>>(A, lda, k1, k2, ipiv, cb1, ce1, cb2, ce2);
+  } else {
+    // one warp per column, at most 4 CTAs per SM's worth of CTAs
+    const long long want = (ncols + 7) / 8;
+    const long long cap = 4LL * num_sms();
+    laswp_kernel<T><<<(unsigned)(want < cap ? want : cap), 256, 0, s>>>(A, lda, k1, k2, ipiv, cb1,
+                                                                         ce1, cb2, ce2);
+  }
   count_launches(1);
   return cudaGetLastError();
 }
@@ -578,11 +798,17 @@ template <typename T, bool UPPER, bool TRANS, bool UNIT, int NC = 8>
 inline cudaError_t trsm_strip(int w, int ncols, const T* Tm, long long ldt, T* B, long long ldb,
                               cudaStream_t s) {
   if (w <= 0 || ncols <= 0) return cudaSuccess;
-  const size_t smem = sizeof(T) * (size_t)w * (NC + 1);
+  // staged triangle columns per block: up to 32, within 200 KB of shared memory
+  constexpr size_t kBudget = 200 * 1024;
+  const size_t bbytes = sizeof(T) * (size_t)w * (NC + 1);
+  const size_t ecol = sizeof(T) * (size_t)(w + 1);
+  if (bbytes + ecol > kBudget) return cudaErrorInvalidValue;
+  const int eb = (int)std::min<size_t>(TRSM_EB, (kBudget - bbytes) / ecol);
+  const size_t smem = bbytes + (size_t)eb * ecol;
   auto kern = trsm_strip_kernel<T, UPPER, TRANS, UNIT, NC>;
-  SL_TRY(smem_attr_once((const void*)kern, 100 * 1024));
+  SL_TRY(smem_attr_once((const void*)kern, (int)kBudget));
   dim3 grid((ncols + NC - 1) / NC);
-  kern<<<grid, 256, smem, s>>>(w, ncols, Tm, ldt, B, ldb);
+  kern<<<grid, 256, smem, s>>>(w, ncols, eb, Tm, ldt, B, ldb);
   count_launches(1);
   return cudaGetLastError();
 }

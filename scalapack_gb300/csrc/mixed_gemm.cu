@@ -17,7 +17,16 @@
 //   * one thread issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=256,
 //     K=16) per 16-wide k-slice and frees each stage with tcgen05.commit;
 //   * all 4 warps read the accumulator back with tcgen05.ld (warp w owns TMEM
-//     lanes 32w..32w+31) and apply C -= acc * 2^e in a coalesced epilogue.
+//     lanes 32w..32w+31), write -acc * 2^e for 32 columns at a time into the
+//     (now idle) stage buffers, and one thread adds each 128 x 32 chunk into C
+//     with a TMA reduce (cp.reduce.async.bulk.tensor .add, FP32), so the
+//     read-modify-write of C happens in L2 without a load round trip per
+//     element. When C's base or leading dimension does not meet the TMA
+//     alignment rules (16-byte base, ldc a multiple of 4) the epilogue falls
+//     back to coalesced loads and stores of C.
+// Two variants: 3 stages with one CTA per SM, or 2 stages with two CTAs per SM
+// (each holding 256 of the SM's 512 TMEM columns) so that one tile's epilogue
+// overlaps the other's main loop.
 // Every mbarrier wait is bounded; on timeout the CTA records kFlagTimeout in
 // the status word, drains what it issued, frees its TMEM and returns.
 #include <cuda.h>
@@ -36,7 +45,6 @@ namespace {
 constexpr int BM = 128;
 constexpr int BN = 256;
 constexpr int BK = 64;       // 64 x 16-bit = 128 bytes: one swizzle row
-constexpr int STAGES = 3;   // leaves room on each SM for the look-ahead panel's CTAs
 constexpr int A_STAGE_BYTES = BM * BK * 2;  // 16 KB
 constexpr int B_STAGE_BYTES = BN * BK * 2;  // 32 KB
 constexpr int TMEM_COLS = 256;
@@ -137,17 +145,33 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// C[x.., y..] += smem box (FP32), tracked by the issuing thread's bulk group.
+__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, const void* src, int x,
+                                                  int y) {
+  asm volatile(
+      "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2}], "
+      "[%3];" ::"l"(reinterpret_cast<uint64_t>(map)),
+      "r"(x), "r"(y), "r"(smem_u32(src))
+      : "memory");
+}
+
+constexpr int kMaxStages = 3;
 struct __align__(8) GemmSmemTail {
-  uint64_t full[STAGES];
-  uint64_t empty[STAGES];
+  uint64_t full[kMaxStages];
+  uint64_t empty[kMaxStages];
   uint64_t done;
   uint32_t tmem_base;
 };
 
-__global__ void __launch_bounds__(128, 1)
+constexpr int EPI_COLS = 32;                       // columns per epilogue chunk
+constexpr int EPI_CHUNK_BYTES = BM * EPI_COLS * 4;  // 16 KB staging per chunk
+
+template <int STAGES, int MINB>
+__global__ void __launch_bounds__(128, MINB)
 lowp_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                 float* C, long long ldc, int m, int n, int k, const int* __restrict__ col_exp,
-                 uint32_t idesc, int* status) {
+                 const __grid_constant__ CUtensorMap tmC, int use_tma_c, float* C, long long ldc,
+                 int m, int n, int k, const int* __restrict__ col_exp, uint32_t idesc,
+                 int* status) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-byte alignment for the swizzled stages
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -187,6 +211,8 @@ lowp_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
     // TMA producer
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
+    if (use_tma_c)
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmC)) : "memory");
     for (int kb = 0; kb < nk; ++kb) {
       const int s = kb % STAGES;
       if (kb >= STAGES && !mbar_wait(&tail->empty[s], ((kb / STAGES) - 1) & 1)) {
@@ -226,7 +252,40 @@ lowp_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
   if (!ok) atomicExch(status, (int)kFlagTimeout);
   asm volatile("tcgen05.fence::after_thread_sync;");
   __syncthreads();
-  if (ok && !s_fail) {
+  if (ok && !s_fail && use_tma_c) {
+    // Stage buffers are idle once every MMA has completed: reuse them as a
+    // ring of 16 KB chunks, [column][row] FP32 (the TMA box's layout).
+    constexpr int NSTG = STAGES * (A_STAGE_BYTES + B_STAGE_BYTES) / EPI_CHUNK_BYTES;
+    static_assert(NSTG >= 2, "staging ring");
+    const int rloc = warp * 32 + lane;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+    for (int c = 0; c < BN / EPI_COLS; ++c) {
+      const int cb = n0 + c * EPI_COLS;
+      if (cb >= n) break;  // uniform across the CTA
+      float* stg = reinterpret_cast<float*>(base + (size_t)(c % NSTG) * EPI_CHUNK_BYTES);
+      if (c >= NSTG) {
+        // the reduce that last read this chunk must have finished reading it
+        if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(NSTG - 1) : "memory");
+        __syncthreads();
+      }
+      float v[32];
+      tmem_ld32(trow + (uint32_t)(c * EPI_COLS), v);
+      const int ncol = min(EPI_COLS, n - cb);
+#pragma unroll
+      for (int j = 0; j < EPI_COLS; ++j) {
+        const float sc = (j < ncol) ? ldexpf(1.0f, __ldg(col_exp + cb + j)) : 0.f;
+        stg[j * BM + rloc] = -v[j] * sc;
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        tma_reduce_add_2d(&tmC, stg, m0, cb);  // rows >= m and columns >= n are clipped
+        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      }
+    }
+    if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+  } else if (ok && !s_fail) {
     const int row = m0 + warp * 32 + lane;
     const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll 1
@@ -236,8 +295,7 @@ lowp_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
       tmem_ld32(trow + (uint32_t)c0, v);
       const int ncol = min(32, n - (n0 + c0));
       // Batch the 32 column scales and the 32 C loads before any store so the
-      // loads are in flight together (C may alias nothing else, but the
-      // compiler cannot know that across the stores).
+      // loads are in flight together.
       float cv[32], sc[32];
 #pragma unroll
       for (int j = 0; j < 32; ++j) sc[j] = (j < ncol) ? ldexpf(1.0f, __ldg(col_exp + n0 + c0 + j)) : 0.f;
@@ -414,11 +472,42 @@ bool make_map(CUtensorMap* map, const void* ptr, int rows, int kpad, int box_row
   return r == CUDA_SUCCESS;
 }
 
+// 2D tensor map over C (m x n FP32, column-major, leading dimension ldc) with a
+// 128 x 32 box for the epilogue's reduce; false when C does not meet the TMA
+// rules (16-byte base, 16-byte multiple stride).
+bool make_map_c(CUtensorMap* map, float* C, int m, int n, long long ldc) {
+  if ((reinterpret_cast<uintptr_t>(C) & 15) != 0 || (ldc & 3) != 0) return false;
+  auto enc = get_encode();
+  if (!enc) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)m, (cuuint64_t)n};
+  cuuint64_t strides[1] = {(cuuint64_t)ldc * 4};
+  cuuint32_t box[2] = {(cuuint32_t)BM, (cuuint32_t)EPI_COLS};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, C, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                   CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+int g_lowp_stages = 3;  // 3: one CTA per SM; 2: two CTAs per SM
+
+// Raises the kernel's dynamic shared-memory limit once per instantiation.
+template <int ST, int MB>
+cudaError_t smem_limit_once(size_t bytes) {
+  static const cudaError_t e = cudaFuncSetAttribute(
+      lowp_gemm_kernel<ST, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return e;
+}
+
+size_t smem_bytes_for(int stages) {
+  return 1024 + (size_t)stages * (A_STAGE_BYTES + B_STAGE_BYTES) + sizeof(GemmSmemTail) + 64;
+}
+
 }  // namespace
 
-size_t lowp_gemm_smem_bytes() {
-  return 1024 + (size_t)STAGES * (A_STAGE_BYTES + B_STAGE_BYTES) + sizeof(GemmSmemTail) + 64;
-}
+size_t lowp_gemm_smem_bytes() { return smem_bytes_for(g_lowp_stages); }
+
+void lowp_set_stages(int stages) { g_lowp_stages = (stages == 2) ? 2 : 3; }
 
 int lowp_kpad(int k) { return (k + BK - 1) / BK * BK; }
 
@@ -461,20 +550,24 @@ cudaError_t lowp_gemm(int fmt, int m, int n, int k, const unsigned short* A16,
   if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
   const bool bf16 = (fmt != 1);
   const int kpad = lowp_kpad(k) * lowp_kmult(fmt);
-  CUtensorMap ta, tb;
+  CUtensorMap ta, tb, tc;
   if (!make_map(&ta, A16, m, kpad, BM) || !make_map(&tb, B16, n, kpad, BN))
     return cudaErrorInvalidResourceHandle;
-  const size_t smem = lowp_gemm_smem_bytes();
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(lowp_gemm_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  const int use_tma_c = make_map_c(&tc, C, m, n, ldc) ? 1 : 0;
+  if (!use_tma_c) tc = ta;  // unused by the kernel
   dim3 grid((m + BM - 1) / BM, (n + BN - 1) / BN);
-  lowp_gemm_kernel<<<grid, 128, smem, s>>>(ta, tb, C, ldc, m, n, kpad, col_exp, make_idesc(bf16),
-                                           status);
+  const uint32_t idesc = make_idesc(bf16);
+  if (g_lowp_stages == 2) {
+    const size_t smem = smem_bytes_for(2);
+    SL_TRY((smem_limit_once<2, 2>(smem)));
+    lowp_gemm_kernel<2, 2><<<grid, 128, smem, s>>>(ta, tb, tc, use_tma_c, C, ldc, m, n, kpad,
+                                                   col_exp, idesc, status);
+  } else {
+    const size_t smem = smem_bytes_for(3);
+    SL_TRY((smem_limit_once<3, 1>(smem)));
+    lowp_gemm_kernel<3, 1><<<grid, 128, smem, s>>>(ta, tb, tc, use_tma_c, C, ldc, m, n, kpad,
+                                                   col_exp, idesc, status);
+  }
   count_launches(1);
   return cudaGetLastError();
 }

@@ -72,13 +72,14 @@ struct LuWork {
 };
 
 size_t panel_cand_doubles();
-// Candidate-slot doubles the panel kernel needs (2 parities x 1024 CTAs x
-// (key, row, 32 values) + 2 diagonal rows + 32 election words + 32 arrival
-// counters); panel_cand_doubles() returns it.
-constexpr size_t kPanelCandDoubles = (size_t)2 * 1024 * (32 + 2) + 2 * 32 + 32 + 16;
+// 8-byte words of the panel kernel's exchange area (2 diagonal rows of 2 x 32
+// words, 2 x 224 x 4 key words, 224 CTAs x 2 parities x 64 row words);
+// panel_cand_doubles() returns it.
+constexpr size_t kPanelCandDoubles = (size_t)4 * 32 + (size_t)8 * 224 + (size_t)224 * 2 * 2 * 32;
 // Largest M the FP64 panel supports on this device (rows held in shared memory).
 int panel_max_rows();
-// Smallest row slice per CTA of the cooperative panel (tunable, default 512).
+// Smallest row slice per CTA of the cooperative panel (tunable; 0, the
+// default, means 256 rows for FP32 and 128 for FP64).
 int panel_min_rows();
 void set_panel_min_rows(int rows);
 // Block size used when a caller passes nb <= 0.
@@ -108,6 +109,8 @@ cudaError_t dgetrs_device(char trans, int n, int nrhs, const double* dA, long lo
 int lowp_kpad(int k);
 int lowp_kmult(int fmt);
 size_t lowp_gemm_smem_bytes();
+// Pipeline depth of the tcgen05 update: 3 (one CTA per SM) or 2 (two per SM).
+void lowp_set_stages(int stages);
 cudaError_t lowp_pack(int fmt, const float* L, long long lda, int m, const float* U,
                       long long ldu, int n, int k, unsigned short* A16, unsigned short* B16,
                       int* col_exp, cudaStream_t s);

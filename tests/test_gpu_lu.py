@@ -57,8 +57,10 @@ def run_pdgesv(sl, ctx, A0, B0, nb, ia=1, ja=1):
     return info, np.asfortranarray(LU), rel, np.asfortranarray(X)
 
 
+# NB 320 exceeds the composite row-interchange table (256 pivots) and takes the
+# sequential interchange kernel for the outer swaps.
 SMALL = [(1, 1), (2, 1), (3, 2), (31, 4), (64, 64), (65, 64), (257, 64), (257, 256), (1000, 64),
-         (1000, 256), (513, 1), (100, 2)]
+         (1000, 256), (513, 1), (100, 2), (700, 320)]
 
 
 @pytest.mark.parametrize("n,nb", SMALL)

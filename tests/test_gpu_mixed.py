@@ -57,6 +57,40 @@ def test_lowp_update_matches_reference(sl, gpu_required, fmt, m, n, k):
     assert bool((err <= tol).all()), float((err / tol).max())
 
 
+@pytest.mark.parametrize("stages", [2, 3])
+@pytest.mark.parametrize("pad", [0, 1, 4])
+@pytest.mark.parametrize("fmt,m,n,k", [(2, 1000, 700, 256), (0, 129, 257, 512), (1, 300, 520, 64)])
+def test_lowp_update_stages_and_leading_dimension(sl, gpu_required, stages, pad, fmt, m, n, k):
+    """Both pipeline depths, and both epilogues: the TMA reduce into C (16-byte
+    aligned C, ldc a multiple of 4) and the load/store fallback (pad 1); rows
+    between m and ldc must stay untouched."""
+    import torch
+
+    ldc = m + pad
+    g = torch.Generator(device="cuda").manual_seed(m + 11 * n + k + pad)
+    Lt = (torch.rand((k, m), device="cuda", generator=g) - 0.5)
+    Ut = (torch.rand((n, k), device="cuda", generator=g) - 0.5) * 3.0
+    Cfull = (torch.rand((n, ldc), device="cuda", generator=g) - 0.5)
+    C0 = Cfull[:, :m].T.clone()
+    guard = Cfull[:, m:].clone()
+    ref, bound = _ref_update(torch, C0, Lt.T.float(), Ut.T.float(), fmt)
+    L = sl.lib()
+    L.sl1x1_set_lowp_stages(stages)
+    try:
+        torch.cuda.synchronize()
+        info = L.sl1x1_lowp_update_dev(fmt, m, n, k, Lt.data_ptr(), m, Ut.data_ptr(), k,
+                                       Cfull.data_ptr(), ldc, None)
+        torch.cuda.synchronize()
+    finally:
+        L.sl1x1_set_lowp_stages(3)
+    assert info == 0
+    got = Cfull[:, :m].T.double()
+    err = (got - ref).abs()
+    tol = 4.0 * k * 2.0 ** -23 * bound + 2.0 ** -22 * ref.abs() + 1e-30
+    assert bool((err <= tol).all()), float((err / tol).max())
+    assert torch.equal(Cfull[:, m:], guard)
+
+
 def _dev_colmajor(torch, M):
     return torch.from_numpy(np.ascontiguousarray(np.asarray(M).T)).cuda()
 
