@@ -688,7 +688,8 @@ int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, 
     sl::splitk_scratch().bytes = g_dev.capSplitk * sizeof(double);
   }
   {
-    const size_t need = (size_t)(n + 63) / 64 + 8;
+    // ticket (64 bytes) + n x 8 tagged 8-byte words of the chained solves
+    const size_t need = 16 + (size_t)n * 8 * 2;
     if (need > g_dev.capChain || !g_dev.dchain) {
       GROW(dchain, capChain, need);
       if (e == cudaSuccess) e = cudaMemsetAsync(g_dev.dchain, 0, sizeof(int) * g_dev.capChain, s);

@@ -552,27 +552,34 @@ trsv_warp_kernel(int w, int ncols, const T* __restrict__ Tm, long long ldt, T* B
 }
 
 // Single-launch blocked triangular solve for few right-hand sides (nrhs <=
-// NRM): FORWARD solves with the unit-lower L, otherwise with the non-unit
-// upper U, of an n x n LU factor, X (n x nrhs) overwritten in place.
+// NRM), FP32: FORWARD solves with the unit-lower L, otherwise with the
+// non-unit upper U, of an n x n LU factor, X (n x nrhs) overwritten in place.
 //
 // Each CTA takes the next 64-row block (in solve order) from an atomic
 // ticket, so every block it depends on belongs to a CTA that has already
-// started: the waits below always end (no residency assumption). It stages
-// its diagonal block in shared memory, then consumes the solved blocks in
-// order as their flags reach `epoch`: the block's x is read through L2 and the
-// 64x64 off-diagonal block of the factor is applied by 4 thread groups of 64
-// rows x 16 columns. The diagonal solve is one warp per right-hand side with
-// shuffles. Waits are bounded (kSpinLimit); on timeout the CTA records
-// kFlagTimeout in *status and stops.
+// started: the waits below always end (no residency assumption). Solved
+// blocks are published as tagged words {x bits, epoch} in xt, so a consumer
+// polls the values themselves (one round trip, no flag and no fence). A CTA
+// stages its diagonal block and the off-diagonal block of its immediate
+// predecessor in shared memory, consumes the earlier solved blocks in chunks
+// of up to 8 (2 for more than 4 right-hand sides) as they appear (4 thread groups of 64 rows x 16 columns apply
+// the 64x64 blocks of the factor), and when the predecessor's x arrives only
+// a 64x64 product from shared memory and the diagonal solve (one warp per
+// right-hand side, shuffles) remain on the chain. Waits are bounded
+// (kSpinLimit); on timeout the CTA records kFlagTimeout in *status and stops.
 template <typename T, bool FORWARD, int NRM>
 __global__ void __launch_bounds__(256)
 trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long ldx, int nrhs,
-                  int* ticket, int* flags, int epoch, int* status) {
+                  int* ticket, unsigned long long* xt, int epoch, int* status) {
+  static_assert(sizeof(T) == 4, "tagged words carry 32-bit values");
   constexpr int KB = 64;
+  constexpr int kChunk = NRM > 4 ? 2 : 8;  // keeps static shared memory under 48 KB
   __shared__ T Ds[KB][KB + 1];          // diagonal block, Ds[r][i] = A(r0+r, r0+i)
-  __shared__ T xs[8 * KB][NRM];         // x of the dependency blocks being applied
+  __shared__ T Ls[KB][KB + 1];          // predecessor block, Ls[r][i] = A(r0+r, kp*KB+i)
+  __shared__ T xs[kChunk * KB][NRM];    // x of the blocks being applied
   __shared__ T part[4][KB][NRM];        // partial sums of the 4 column groups
-  __shared__ int s_b, s_fail;
+  __shared__ int s_b, s_fail, s_bad[kChunk];
+  const uint32_t tag = (uint32_t)epoch;
   const int tid = threadIdx.x;
   const int nblk = (n + KB - 1) / KB;
   if (tid == 0) { s_b = atomicAdd(ticket, 1); s_fail = 0; }
@@ -581,53 +588,79 @@ trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long
   if (sidx >= nblk) return;
   const int b = FORWARD ? sidx : nblk - 1 - sidx;
   const int r0 = b * KB, rb = min(KB, n - r0);
+  const int kp = FORWARD ? b - 1 : b + 1;  // predecessor in solve order
+  const int wp = (sidx > 0) ? min(KB, n - kp * KB) : 0;
   for (int idx = tid; idx < KB * KB; idx += 256) {
     int r = idx % KB, i = idx / KB;
     Ds[r][i] = (r < rb && i < rb) ? A[(r0 + r) + (long long)(r0 + i) * lda] : (T)0;
+    Ls[r][i] = (r < rb && i < wp) ? A[(r0 + r) + (long long)(kp * KB + i) * lda] : (T)0;
   }
   const int r = tid & (KB - 1), q = tid >> 6;
+  const int warp = tid >> 5, lane = tid & 31;
+  // the block's right-hand side, read now rather than on the chain (warp c
+  // owns column c; only this CTA writes these rows)
+  T bx0 = (T)0, bx1 = (T)0;
+  if (warp < nrhs) {
+    if (lane < rb) bx0 = X[(r0 + lane) + (long long)warp * ldx];
+    if (lane + 32 < rb) bx1 = X[(r0 + lane + 32) + (long long)warp * ldx];
+  }
   T acc[NRM];
 #pragma unroll
   for (int c = 0; c < NRM; ++c) acc[c] = (T)0;
-  // Consume the solved blocks in solve order, as many at a time as have
-  // already been published (up to kChunk), so a late CTA streams through the
-  // finished part of the factor with few synchronizations.
-  constexpr int kChunk = 8;
-  __shared__ int s_avail;
+  // Blocks 0 .. sidx-2 in solve order: chunks of the consecutive solved blocks
+  // that are already published (at least the first one, waited for).
   int t = 0;
-  while (t < sidx) {
-    if (tid == 0) {
-      const int kb0 = FORWARD ? t : nblk - 1 - t;
-      long long spins = 0;
-      while (ld_acquire_gpu(&flags[kb0]) != epoch) {
-        if (++spins > kSpinLimit) { atomicExch(status, (int)kFlagTimeout); s_fail = 1; break; }
-        if (spins > 32) __nanosleep(32);
-      }
-      int av = 1;
-      while (!s_fail && av < kChunk && t + av < sidx) {
-        const int kbn = FORWARD ? t + av : nblk - 1 - (t + av);
-        if (ld_acquire_gpu(&flags[kbn]) != epoch) break;
-        ++av;
-      }
-      s_avail = av;
-    }
-    __syncthreads();
-    if (s_fail) return;
-    const int av = s_avail;
-    // rows of X covered by the chunk: blocks t..t+av-1 in solve order are
-    // contiguous in the matrix (increasing for forward, decreasing backward)
-    const int kfirst = FORWARD ? t : nblk - 1 - (t + av - 1);
+  long long spins = 0;
+  while (t < sidx - 1) {
+    const int want = min(kChunk, sidx - 1 - t);
+    const int kfirst = FORWARD ? t : nblk - 1 - (t + want - 1);  // lowest block of the chunk
     const int k0 = kfirst * KB;
-    const int kn = min(av * KB, n - k0);
+    const int kn = min(want * KB, n - k0);
+    if (tid == 0) {
+      // one thread watches the chunk's first block (its last word) before the
+      // whole chunk is read, so waiting CTAs do not stream through L2
+      const int kb0 = FORWARD ? t : nblk - 1 - t;
+      const unsigned long long* p = xt + kb0 * KB + min(KB, n - kb0 * KB) - 1;
+      for (long long sp = 0;; ++sp) {
+        unsigned long long wd;
+        asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(wd) : "l"(p) : "memory");
+        if ((uint32_t)(wd >> 32) == tag) break;
+        if (sp > kSpinLimit) { s_fail = 1; break; }
+      }
+    }
+    if (tid < kChunk) s_bad[tid] = 0;
+    __syncthreads();
+    if (s_fail) {
+      if (tid == 0) atomicExch(status, (int)kFlagTimeout);
+      return;
+    }
     for (int idx = tid; idx < kn * nrhs; idx += 256) {
-      int i = idx % kn, c = idx / kn;
-      xs[i][c] = __ldcg(&X[(k0 + i) + (long long)c * ldx]);
+      const int i = idx % kn, c = idx / kn;
+      unsigned long long wd;
+      asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(wd) : "l"(xt + (size_t)c * n + k0 + i) : "memory");
+      xs[i][c] = __uint_as_float((uint32_t)wd);
+      if ((uint32_t)(wd >> 32) != tag) {
+        const int blk = i / KB;                                  // chunk block, matrix order
+        s_bad[FORWARD ? blk : want - 1 - blk] = 1;               // solve order
+      }
     }
     __syncthreads();
+    int av = 0;
+    while (av < want && s_bad[av] == 0) ++av;
+    if (av == 0) {  // the watched word arrived before the rest of its block
+      if (++spins > kSpinLimit) {
+        if (tid == 0) atomicExch(status, (int)kFlagTimeout);
+        return;
+      }
+      __syncthreads();  // everyone has read s_bad before it is reset
+      continue;
+    }
+    // columns of the av complete blocks, in matrix order
+    const int c0 = FORWARD ? 0 : (want - av) * KB;
+    const int c1 = FORWARD ? min(av * KB, kn) : kn;
     if (r < rb) {
-      // thread group q takes every 4th group of 16 columns of the chunk
-      for (int g0 = q * 16; g0 < kn; g0 += 64) {
-        const int g1 = min(g0 + 16, kn);
+      for (int g0 = c0 + q * 16; g0 < c1; g0 += 64) {
+        const int g1 = min(g0 + 16, c1);
         for (int kk = g0; kk < g1; ++kk) {
           const T a = A[(r0 + r) + (long long)(k0 + kk) * lda];
 #pragma unroll
@@ -639,18 +672,45 @@ trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long
     __syncthreads();
     t += av;
   }
+  // The predecessor: poll its x (the chain's one round trip), apply Ls.
+  if (sidx > 0) {
+    for (int idx = tid; idx < wp * nrhs; idx += 256) {
+      const int i = idx % wp, c = idx / wp;
+      const unsigned long long* p = xt + (size_t)c * n + kp * KB + i;
+      unsigned long long wd;
+      for (long long sp = 0;; ++sp) {
+        asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(wd) : "l"(p) : "memory");
+        if ((uint32_t)(wd >> 32) == tag) break;
+        if (sp > kSpinLimit) { s_fail = 1; break; }
+      }
+      xs[i][c] = __uint_as_float((uint32_t)wd);
+    }
+    __syncthreads();
+    if (s_fail) {
+      if (tid == 0) atomicExch(status, (int)kFlagTimeout);
+      return;
+    }
+    if (r < rb) {
+#pragma unroll 4
+      for (int kk = q * 16; kk < q * 16 + 16; ++kk) {
+        if (kk < wp) {
+#pragma unroll
+          for (int c = 0; c < NRM; ++c)
+            if (c < nrhs) acc[c] = fma(Ls[r][kk], xs[kk][c], acc[c]);
+        }
+      }
+    }
+  }
 #pragma unroll
   for (int c = 0; c < NRM; ++c) part[q][r][c] = acc[c];
   __syncthreads();
   // v = b - sum of the partials, diagonal solve: warp c owns column c, lanes own rows lane, lane+32
-  const int warp = tid >> 5, lane = tid & 31;
-  for (int c = warp; c < nrhs; c += 8) {
+  if (warp < nrhs) {
+    const int c = warp;
     T x0 = (T)0, x1 = (T)0;
-    if (lane < rb)
-      x0 = X[(r0 + lane) + (long long)c * ldx] - (part[0][lane][c] + part[1][lane][c] + part[2][lane][c] + part[3][lane][c]);
+    if (lane < rb) x0 = bx0 - (part[0][lane][c] + part[1][lane][c] + part[2][lane][c] + part[3][lane][c]);
     if (lane + 32 < rb)
-      x1 = X[(r0 + lane + 32) + (long long)c * ldx] -
-           (part[0][lane + 32][c] + part[1][lane + 32][c] + part[2][lane + 32][c] + part[3][lane + 32][c]);
+      x1 = bx1 - (part[0][lane + 32][c] + part[1][lane + 32][c] + part[2][lane + 32][c] + part[3][lane + 32][c]);
     for (int s = 0; s < rb; ++s) {
       const int i = FORWARD ? s : rb - 1 - s;
       const int li = i & 31;
@@ -668,28 +728,36 @@ trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long
         if (lane + 32 < i) x1 = fma(-Ds[lane + 32][i], xi, x1);
       }
     }
-    if (lane < rb) X[(r0 + lane) + (long long)c * ldx] = x0;
-    if (lane + 32 < rb) X[(r0 + lane + 32) + (long long)c * ldx] = x1;
+    // publish: tagged words for the consumers, plain values for the result
+    const unsigned long long t0 = ((unsigned long long)tag << 32) | __float_as_uint(x0);
+    const unsigned long long t1 = ((unsigned long long)tag << 32) | __float_as_uint(x1);
+    if (lane < rb) {
+      asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(xt + (size_t)c * n + r0 + lane), "l"(t0) : "memory");
+      X[(r0 + lane) + (long long)c * ldx] = x0;
+    }
+    if (lane + 32 < rb) {
+      asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(xt + (size_t)c * n + r0 + lane + 32), "l"(t1) : "memory");
+      X[(r0 + lane + 32) + (long long)c * ldx] = x1;
+    }
   }
-  __threadfence();
-  __syncthreads();
-  if (tid == 0) st_release_gpu(&flags[b], epoch);
 }
 
-// Launch the chained solve; `sync` holds 1 ticket int followed by one flag per
-// 64-row block (flags start at 0; epoch must differ from every earlier one).
+// Launch the chained solve; `sync` holds 1 ticket int (64 bytes reserved)
+// followed by n x nrhs tagged 8-byte words (zeroed once; epoch must differ
+// from every earlier one).
 template <typename T, bool FORWARD>
 inline cudaError_t trsv_chain(const T* A, long long lda, int n, T* X, long long ldx, int nrhs,
                               int* sync, int epoch, int* status, cudaStream_t s) {
   if (n <= 0 || nrhs <= 0) return cudaSuccess;
   const int nblk = (n + 63) / 64;
   SL_TRY(cudaMemsetAsync(sync, 0, sizeof(int), s));
+  unsigned long long* xt = reinterpret_cast<unsigned long long*>(sync + 16);
   if (nrhs <= 1)
-    trsv_chain_kernel<T, FORWARD, 1><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, sync, sync + 1, epoch, status);
+    trsv_chain_kernel<T, FORWARD, 1><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, sync, xt, epoch, status);
   else if (nrhs <= 4)
-    trsv_chain_kernel<T, FORWARD, 4><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, sync, sync + 1, epoch, status);
+    trsv_chain_kernel<T, FORWARD, 4><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, sync, xt, epoch, status);
   else
-    trsv_chain_kernel<T, FORWARD, 8><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, sync, sync + 1, epoch, status);
+    trsv_chain_kernel<T, FORWARD, 8><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, sync, xt, epoch, status);
   count_launches(1);
   return cudaGetLastError();
 }

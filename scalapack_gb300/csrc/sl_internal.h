@@ -138,7 +138,7 @@ struct MixedWork {
   double* h = nullptr;         // gmres_m + 8
   double* Acopy = nullptr;     // optional FP64 copy of A for the fallback (keeps A)
   long long ldacopy = 0;
-  int* chain = nullptr;        // ticket + per-block flags of the chained solves (n/64 + 8)
+  int* chain = nullptr;        // chained solves: ticket (16 ints) + n x 8 tagged words
   int* epoch = nullptr;        // host-side counter of chained-solve epochs
   int* status = nullptr;       // device status word
 };
