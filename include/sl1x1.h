@@ -67,6 +67,49 @@ void pdgetri_(const int* N, double* A, const int* IA, const int* JA, const int* 
               const int* IPIV, double* WORK, const int* LWORK, int* IWORK, const int* LIWORK,
               int* INFO);
 
+/* ---- Expert driver and its parts (refinement, error bounds, scaling) ----- */
+
+/* Replaces PDGERFS, SRC/pdgerfs.f:1-4: iterative refinement of X for
+ * op(sub(A)) X = sub(B) with the factors of PDGETRF, the componentwise
+ * backward error BERR and the forward error bound FERR of every column (FERR
+ * and BERR indexed from JB, as the reference does). Same argument checks,
+ * workspace query and N <= 1 quick return; residuals, solves and the norm
+ * estimate run on the GPU. */
+void pdgerfs_(const char* TRANS, const int* N, const int* NRHS, const double* A, const int* IA,
+              const int* JA, const int* DESCA, const double* AF, const int* IAF, const int* JAF,
+              const int* DESCAF, const int* IPIV, const double* B, const int* IB, const int* JB,
+              const int* DESCB, double* X, const int* IX, const int* JX, const int* DESCX,
+              double* FERR, double* BERR, double* WORK, const int* LWORK, int* IWORK,
+              const int* LIWORK, int* INFO, size_t TRANS_len);
+
+/* Replaces PDGESVX, SRC/pdgesvx.f:1-4: FACT = 'E' equilibrates (PDGEEQU,
+ * PDLAQGE), 'N' or 'E' factors into AF, 'F' takes AF and IPIV; then RCOND
+ * (PDLANGE + PDGECON; INFO = IA+N when RCOND < eps), PDGETRS, PDGERFS and the
+ * back-transformation of X and FERR. One deliberate difference: with
+ * FACT = 'F', TRANS = 'N' and EQUED = 'C' or 'B' the reference multiplies X
+ * by a workspace that it never filled with C; this library multiplies by C. */
+void pdgesvx_(const char* FACT, const char* TRANS, const int* N, const int* NRHS, double* A,
+              const int* IA, const int* JA, const int* DESCA, double* AF, const int* IAF,
+              const int* JAF, const int* DESCAF, int* IPIV, char* EQUED, double* R, double* C,
+              double* B, const int* IB, const int* JB, const int* DESCB, double* X, const int* IX,
+              const int* JX, const int* DESCX, double* RCOND, double* FERR, double* BERR,
+              double* WORK, const int* LWORK, int* IWORK, const int* LIWORK, int* INFO,
+              size_t FACT_len, size_t TRANS_len, size_t EQUED_len);
+
+/* Replaces PDGEEQU, SRC/pdgeequ.f:1-2: row scale factors R(IA:IA+M-1) and
+ * column scale factors C(JA:JA+N-1) that bring the largest entry of every row
+ * and column of diag(R) sub(A) diag(C) to 1; INFO = i (zero row) or M+j (zero
+ * column). Computed on the GPU; bit-identical to the reference's arithmetic. */
+void pdgeequ_(const int* M, const int* N, const double* A, const int* IA, const int* JA,
+              const int* DESCA, double* R, double* C, double* ROWCND, double* COLCND,
+              double* AMAX, int* INFO);
+
+/* Replaces PDLAQGE, SRC/pdlaqge.f:1-2: scales sub(A) by R and/or C when
+ * ROWCND, COLCND and AMAX call for it (threshold 0.1) and reports EQUED. */
+void pdlaqge_(const int* M, const int* N, double* A, const int* IA, const int* JA,
+              const int* DESCA, const double* R, const double* C, const double* ROWCND,
+              const double* COLCND, const double* AMAX, char* EQUED, size_t EQUED_len);
+
 /* ---- TOOLS used by callers of the LU path ------------------------------- */
 
 /* Replaces DESCINIT, TOOLS/descinit.f:1-192. */
@@ -171,6 +214,16 @@ double sl1x1_dlange_dev(char norm, int m, int n, const double* dA, long long ldd
 int sl1x1_dgecon_dev(char norm, int n, const double* dLU, long long ldda, double anorm,
                      double* rcond, void* stream);
 int sl1x1_dgetri_dev(int n, double* dA, long long ldda, const int* dipiv, void* stream);
+/* PDGEEQU on device data: dR (m) and dC (n) device arrays, scalars on the
+ * host; returns INFO as PDGEEQU. */
+int sl1x1_dgeequ_dev(int m, int n, const double* dA, long long ldda, double* dR, double* dC,
+                     double* rowcnd, double* colcnd, double* amax, void* stream);
+/* PDGERFS on device data (dipiv 1-based as LAPACK); ferr and berr are host
+ * arrays of nrhs entries. Returns 0 or a negative INFO. */
+int sl1x1_dgerfs_dev(char trans, int n, int nrhs, const double* dA, long long ldda,
+                     const double* dAF, long long lddaf, const int* dipiv, const double* dB,
+                     long long lddb, double* dX, long long lddx, double* ferr, double* berr,
+                     void* stream);
 
 /* ---- Library control ----------------------------------------------------- */
 /* Free every device buffer the library holds (also done by blacs_exit_). */

@@ -90,6 +90,27 @@ def lib():
     L.orc_eps.restype = C.c_double
     L.orc_set_recorder.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
     L.orc_gen_conditioned.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p, C.c_int]
+    L.orc_pdgeequ.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.orc_pdgeequ.restype = C.c_int
+    L.orc_pdlaqge.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                              C.c_void_p, C.c_double, C.c_double, C.c_double]
+    L.orc_pdlaqge.restype = C.c_char
+    L.orc_pdlange.argtypes = [C.c_char, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int]
+    L.orc_pdlange.restype = C.c_double
+    L.orc_pdgecon.argtypes = [C.c_char, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double]
+    L.orc_pdgecon.restype = C.c_double
+    L.orc_pdgerfs.argtypes = [C.c_char, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                              C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                              C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                              C.c_void_p, C.c_void_p]
+    L.orc_pdgerfs.restype = None
+    L.orc_pdgesvx.argtypes = [C.c_char, C.c_char, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int,
+                              C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                              C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                              C.c_void_p, C.c_void_p]
+    L.orc_pdgesvx.restype = C.c_int
     path, prefix = find_host_blas()
     if path:
         L.orc_load_blas(path.encode(), prefix.encode())
@@ -237,3 +258,77 @@ def solve_reference(A, B, nb=64):
     if info == 0:
         pdgetrs("N", n, B.shape[1], LU, ipiv, X)
     return LU, ipiv[:n].copy(), X, info
+
+
+# ---- expert driver (PDGEEQU / PDLAQGE / PDLANGE / PDGECON / PDGERFS / PDGESVX) ----
+
+def pdgeequ(A):
+    """PDGEEQU of a Fortran-order matrix: (R, C, rowcnd, colcnd, amax, info)."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    m, n = A.shape
+    R = np.zeros(max(m, 1))
+    Cv = np.zeros(max(n, 1))
+    out = (C.c_double * 3)()
+    info = lib().orc_pdgeequ(m, n, _p(A), max(m, 1), 1, 1, _p(R), _p(Cv), C.byref(out, 0),
+                             C.byref(out, 8), C.byref(out, 16))
+    return R[:m], Cv[:n], out[0], out[1], out[2], info
+
+
+def pdlaqge(A, R, Cv, rowcnd, colcnd, amax):
+    """PDLAQGE: (scaled copy of A, EQUED)."""
+    A = np.array(A, dtype=np.float64, order="F")
+    m, n = A.shape
+    R = np.ascontiguousarray(R, dtype=np.float64)
+    Cv = np.ascontiguousarray(Cv, dtype=np.float64)
+    eq = lib().orc_pdlaqge(m, n, _p(A), max(m, 1), 1, 1, _p(R), _p(Cv), rowcnd, colcnd, amax)
+    return A, eq.decode()
+
+
+def pdlange(norm, A):
+    A = np.asfortranarray(A, dtype=np.float64)
+    return lib().orc_pdlange(norm.encode(), A.shape[0], _p(A), max(A.shape[0], 1), 1, 1)
+
+
+def pdgecon(norm, LU, anorm):
+    LU = np.asfortranarray(LU, dtype=np.float64)
+    return lib().orc_pdgecon(norm.encode(), LU.shape[0], _p(LU), max(LU.shape[0], 1), 1, 1, anorm)
+
+
+def pdgerfs(trans, A, AF, ipiv, B, X):
+    """PDGERFS with IA = IAF = IB = IX = 1: (refined X, FERR, BERR); ipiv holds
+    global 1-based rows as PDGETRF writes them."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    AF = np.asfortranarray(AF, dtype=np.float64)
+    B = np.asfortranarray(B, dtype=np.float64)
+    X = np.array(X, dtype=np.float64, order="F")
+    n, nrhs = B.shape
+    ip = np.ascontiguousarray(ipiv, dtype=np.int32)
+    ferr = np.zeros(max(nrhs, 1))
+    berr = np.zeros(max(nrhs, 1))
+    ld = max(n, 1)
+    lib().orc_pdgerfs(trans.encode(), n, nrhs, _p(A), ld, 1, 1, _p(AF), ld, 1, 1, _p(ip), _p(B), ld,
+                      1, 1, _p(X), ld, 1, 1, _p(ferr), _p(berr))
+    return X, ferr[:nrhs], berr[:nrhs]
+
+
+def pdgesvx(fact, trans, A, B, AF=None, ipiv=None, equed="N", R=None, Cv=None, nb=64):
+    """PDGESVX with IA = IAF = IB = IX = 1 on copies of the inputs; returns a
+    dict of every output (A and B as modified by equilibration)."""
+    A = np.array(A, dtype=np.float64, order="F")
+    B = np.array(B, dtype=np.float64, order="F")
+    n, nrhs = B.shape
+    ld = max(n, 1)
+    AF = np.zeros((n, n), order="F") if AF is None else np.array(AF, dtype=np.float64, order="F")
+    ip = np.zeros(max(n, 1), np.int32) if ipiv is None else np.array(ipiv, dtype=np.int32)
+    R = np.zeros(max(n, 1)) if R is None else np.array(R, dtype=np.float64)
+    Cv = np.zeros(max(n, 1)) if Cv is None else np.array(Cv, dtype=np.float64)
+    X = np.zeros((n, nrhs), order="F")
+    eq = C.create_string_buffer(equed.encode(), 2)
+    rcond = C.c_double(0.0)
+    ferr = np.zeros(max(nrhs, 1))
+    berr = np.zeros(max(nrhs, 1))
+    info = lib().orc_pdgesvx(fact.encode(), trans.encode(), n, nrhs, _p(A), ld, 1, 1, _p(AF), ld, 1,
+                             1, n, nb, _p(ip), eq, _p(R), _p(Cv), _p(B), ld, 1, 1, _p(X), ld, 1, 1,
+                             C.byref(rcond), _p(ferr), _p(berr))
+    return dict(info=info, A=A, AF=AF, ipiv=ip[:n], equed=eq.value.decode(), R=R[:n], C=Cv[:n],
+                B=B, X=X, rcond=rcond.value, ferr=ferr[:nrhs], berr=berr[:nrhs])

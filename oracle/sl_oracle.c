@@ -2,8 +2,9 @@
  * sl_oracle.c -- TEST INFRASTRUCTURE ONLY.
  *
  * CPU restatement of ScaLAPACK 2.2.3's dense LU path on a 1x1 BLACS grid
- * (PDGETRF / PDGETF2 / PDLASWP / PDTRSM / PDGEMM / PDGETRS / PDLAPIV) and of the
- * LU tester's generator and residual checks.  It is the checker that the GPU
+ * (PDGETRF / PDGETF2 / PDLASWP / PDTRSM / PDGEMM / PDGETRS / PDLAPIV), of the
+ * expert driver around it (PDGEEQU / PDLAQGE / PDLANGE / PDGECON / PDLACON /
+ * PDGERFS / PDGESVX) and of the LU tester's generator and residual checks.  It is the checker that the GPU
  * library is compared against; it is never linked into, called by, or used as
  * a fallback for the product library.  Only the test suite, the smoke check
  * and the CPU-baseline leg of the benchmark load it.
@@ -626,4 +627,328 @@ void orc_gen_conditioned(int n, int nrefl, double kappa, int seed, double* A, in
     }
   }
   free(v); free(w);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Expert driver: PDGEEQU, PDLAQGE, PDLACON, PDGECON, PDLANGE, PDGERFS,       */
+/* PDGESVX on a 1x1 grid                                                      */
+/* ------------------------------------------------------------------------- */
+#define A_AT(M, ld, i, j) ((M)[(size_t)(i) + (size_t)(j) * (size_t)(ld)])
+static const double ORC_SAFMIN = 2.2250738585072014e-308; /* 2^-1022, PDLAMCH 'S' */
+
+/* PDGEEQU (SRC/pdgeequ.f:230-340) for sub(A) = A(ia.., ja..), m x n.
+ * R[i] stands for R(IA+i) and C[j] for C(JA+j).  Returns INFO. */
+int orc_pdgeequ(int m, int n, const double* A, int lda, int ia, int ja, double* R, double* C,
+                double* rowcnd, double* colcnd, double* amax) {
+  if (m == 0 || n == 0) { *rowcnd = 1.0; *colcnd = 1.0; *amax = 0.0; return 0; }
+  const double* S = A + (ia - 1) + (size_t)(ja - 1) * lda;
+  const double smlnum = ORC_SAFMIN, bignum = 1.0 / smlnum;
+  for (int i = 0; i < m; ++i) R[i] = 0.0;
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) R[i] = fmax(R[i], fabs(A_AT(S, lda, i, j)));
+  double rcmin = bignum, rcmax = 0.0;
+  for (int i = 0; i < m; ++i) { rcmax = fmax(rcmax, R[i]); rcmin = fmin(rcmin, R[i]); }
+  *amax = rcmax;
+  if (rcmin == 0.0) {
+    for (int i = 0; i < m; ++i) if (R[i] == 0.0) return i + 1;
+  }
+  for (int i = 0; i < m; ++i) R[i] = 1.0 / fmin(fmax(R[i], smlnum), bignum);
+  *rowcnd = fmax(rcmin, smlnum) / fmin(rcmax, bignum);
+  for (int j = 0; j < n; ++j) C[j] = 0.0;
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) C[j] = fmax(C[j], fabs(A_AT(S, lda, i, j)) * R[i]);
+  rcmin = bignum; rcmax = 0.0;
+  for (int j = 0; j < n; ++j) { rcmin = fmin(rcmin, C[j]); rcmax = fmax(rcmax, C[j]); }
+  if (rcmin == 0.0) {
+    for (int j = 0; j < n; ++j) if (C[j] == 0.0) return m + j + 1;
+  }
+  for (int j = 0; j < n; ++j) C[j] = 1.0 / fmin(fmax(C[j], smlnum), bignum);
+  *colcnd = fmax(rcmin, smlnum) / fmin(rcmax, bignum);
+  return 0;
+}
+
+/* PDLAQGE (SRC/pdlaqge.f:180-260).  Returns EQUED. */
+char orc_pdlaqge(int m, int n, double* A, int lda, int ia, int ja, const double* R,
+                 const double* C, double rowcnd, double colcnd, double amax) {
+  if (m <= 0 || n <= 0) return 'N';
+  double* S = A + (ia - 1) + (size_t)(ja - 1) * lda;
+  const double small = ORC_SAFMIN / ldexp(1.0, -52); /* 'Safe minimum' / 'Precision' */
+  const double large = 1.0 / small, thresh = 0.1;
+  if (rowcnd >= thresh && amax >= small && amax <= large) {
+    if (colcnd >= thresh) return 'N';
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < m; ++i) A_AT(S, lda, i, j) = C[j] * A_AT(S, lda, i, j);
+    return 'C';
+  }
+  if (colcnd >= thresh) {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < m; ++i) A_AT(S, lda, i, j) = R[i] * A_AT(S, lda, i, j);
+    return 'R';
+  }
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) A_AT(S, lda, i, j) = C[j] * R[i] * A_AT(S, lda, i, j);
+  return 'B';
+}
+
+/* Hager/Higham 1-norm estimator as PDLACON (SRC/pdlacon.f) runs it on one
+ * process: op(1, x) overwrites x with B x, op(2, x) with B^T x. */
+typedef void (*orc_op_t)(int kase, double* x, void* ctx);
+static double orc_dlacon(int n, orc_op_t op, void* ctx) {
+  double* x = (double*)malloc(sizeof(double) * (size_t)n);
+  int* isgn = (int*)malloc(sizeof(int) * (size_t)n);
+  double est = 0.0;
+  for (int i = 0; i < n; ++i) x[i] = 1.0 / n;
+  op(1, x, ctx);
+  if (n == 1) { est = fabs(x[0]); free(x); free(isgn); return est; }
+  for (int i = 0; i < n; ++i) est += fabs(x[i]);
+  for (int i = 0; i < n; ++i) { x[i] = x[i] >= 0.0 ? 1.0 : -1.0; isgn[i] = (int)x[i]; }
+  op(2, x, ctx);
+  int j = 0;
+  for (int i = 1; i < n; ++i) if (fabs(x[i]) > fabs(x[j])) j = i;
+  int iter = 2;
+  for (;;) {
+    for (int i = 0; i < n; ++i) x[i] = 0.0;
+    x[j] = 1.0;
+    op(1, x, ctx);
+    const double estold = est;
+    est = 0.0;
+    for (int i = 0; i < n; ++i) est += fabs(x[i]);
+    int changed = 0;
+    for (int i = 0; i < n; ++i) if ((x[i] >= 0.0 ? 1 : -1) != isgn[i]) { changed = 1; break; }
+    if (!changed || est <= estold) break;
+    for (int i = 0; i < n; ++i) { x[i] = x[i] >= 0.0 ? 1.0 : -1.0; isgn[i] = (int)x[i]; }
+    op(2, x, ctx);
+    const int jlast = j;
+    j = 0;
+    for (int i = 1; i < n; ++i) if (fabs(x[i]) > fabs(x[j])) j = i;
+    if (x[jlast] == fabs(x[j]) || iter >= 5) break;
+    ++iter;
+  }
+  double altsgn = 1.0;
+  for (int i = 0; i < n; ++i) { x[i] = altsgn * (1.0 + (double)i / (double)(n - 1)); altsgn = -altsgn; }
+  op(1, x, ctx);
+  double temp = 0.0;
+  for (int i = 0; i < n; ++i) temp += fabs(x[i]);
+  temp = 2.0 * temp / (3.0 * n);
+  if (temp > est) est = temp;
+  free(x); free(isgn);
+  return est;
+}
+
+/* PDLANGE '1' (max column sum) or 'I' (max row sum) of sub(A), n x n. */
+double orc_pdlange(char norm, int n, const double* A, int lda, int ia, int ja) {
+  const double* S = A + (ia - 1) + (size_t)(ja - 1) * lda;
+  double v = 0.0;
+  if (norm == '1' || norm == 'O' || norm == 'o') {
+    for (int j = 0; j < n; ++j) {
+      double s = 0.0;
+      for (int i = 0; i < n; ++i) s += fabs(A_AT(S, lda, i, j));
+      if (s > v) v = s;
+    }
+  } else {
+    for (int i = 0; i < n; ++i) {
+      double s = 0.0;
+      for (int j = 0; j < n; ++j) s += fabs(A_AT(S, lda, i, j));
+      if (s > v) v = s;
+    }
+  }
+  return v;
+}
+
+struct orc_inv_ctx { int n; const double* LU; int ld; int onenrm; };
+static void orc_gecon_op(int kase, double* x, void* vctx) {
+  struct orc_inv_ctx* c = (struct orc_inv_ctx*)vctx;
+  const int kase1 = c->onenrm ? 1 : 2;
+  if (kase == kase1) { /* inv(U) inv(L) x */
+    trsm_lower_unit(c->n, 1, c->LU, c->ld, x, c->n);
+    trsm_upper_nonunit(c->n, 1, c->LU, c->ld, x, c->n);
+  } else {             /* inv(L)^T inv(U)^T x */
+    trsm_upperT_nonunit(c->n, 1, c->LU, c->ld, x, c->n);
+    trsm_lowerT_unit(c->n, 1, c->LU, c->ld, x, c->n);
+  }
+}
+
+/* PDGECON (SRC/pdgecon.f) with unscaled triangular solves. */
+double orc_pdgecon(char norm, int n, const double* AF, int ldaf, int iaf, int jaf, double anorm) {
+  if (n == 0) return 1.0;
+  if (anorm == 0.0) return 0.0;
+  struct orc_inv_ctx c = {n, AF + (iaf - 1) + (size_t)(jaf - 1) * ldaf, ldaf,
+                          (norm == '1' || norm == 'O' || norm == 'o')};
+  const double ainvnm = orc_dlacon(n, orc_gecon_op, &c);
+  return ainvnm != 0.0 ? (1.0 / ainvnm) / anorm : 0.0;
+}
+
+struct orc_rfs_ctx {
+  char trans, transt;
+  int n; const double* AF; int ldaf, iaf, jaf; const int* ipiv; const double* w;
+};
+static void orc_rfs_op(int kase, double* x, void* vctx) {
+  struct orc_rfs_ctx* c = (struct orc_rfs_ctx*)vctx;
+  if (kase == 1) { /* diag(W) inv(op(A))^T */
+    orc_pdgetrs(c->transt, c->n, 1, c->AF, c->ldaf, c->iaf, c->jaf, c->ipiv, x, c->n, 1, 1);
+    for (int i = 0; i < c->n; ++i) x[i] = c->w[i] * x[i];
+  } else {         /* inv(op(A)) diag(W) */
+    for (int i = 0; i < c->n; ++i) x[i] = c->w[i] * x[i];
+    orc_pdgetrs(c->trans, c->n, 1, c->AF, c->ldaf, c->iaf, c->jaf, c->ipiv, x, c->n, 1, 1);
+  }
+}
+
+/* PDGERFS (SRC/pdgerfs.f:470-887) on a 1x1 grid.  ferr[k] / berr[k] stand for
+ * FERR(JB+k) / BERR(JB+k); ferr[k] is left as it was when column k of X is 0. */
+void orc_pdgerfs(char trans, int n, int nrhs, const double* A, int lda, int ia, int ja,
+                 const double* AF, int ldaf, int iaf, int jaf, const int* ipiv, const double* B,
+                 int ldb, int ib, int jb, double* X, int ldx, int ix, int jx, double* ferr,
+                 double* berr) {
+  if (n <= 1 || nrhs == 0) {
+    for (int k = 0; k < nrhs; ++k) { ferr[k] = 0.0; berr[k] = 0.0; }
+    return;
+  }
+  const int notran = (trans == 'N' || trans == 'n');
+  const double* SA = A + (ia - 1) + (size_t)(ja - 1) * lda;
+  const int nz = n + 1;
+  const double eps = orc_eps();
+  const double safe1 = nz * ORC_SAFMIN, safe2 = safe1 / eps;
+  double* r = (double*)malloc(sizeof(double) * (size_t)n);
+  double* w = (double*)malloc(sizeof(double) * (size_t)n);
+  for (int k = 0; k < nrhs; ++k) {
+    const double* b = B + (ib - 1) + (size_t)(jb - 1 + k) * ldb;
+    double* x = X + (ix - 1) + (size_t)(jx - 1 + k) * ldx;
+    int count = 1;
+    double lstres = 3.0;
+    for (;;) {
+      /* r = b - op(A) x, w = |b| + |op(A)| |x| */
+      for (int i = 0; i < n; ++i) { r[i] = b[i]; w[i] = fabs(b[i]); }
+      if (notran) {
+        for (int j = 0; j < n; ++j)
+          for (int i = 0; i < n; ++i) {
+            r[i] -= A_AT(SA, lda, i, j) * x[j];
+            w[i] += fabs(A_AT(SA, lda, i, j)) * fabs(x[j]);
+          }
+      } else {
+        for (int j = 0; j < n; ++j) {
+          double s = 0.0, t = 0.0;
+          for (int i = 0; i < n; ++i) {
+            s += A_AT(SA, lda, i, j) * x[i];
+            t += fabs(A_AT(SA, lda, i, j)) * fabs(x[i]);
+          }
+          r[j] -= s;
+          w[j] += t;
+        }
+      }
+      double s = 0.0;
+      for (int i = 0; i < n; ++i) {
+        const double q = (w[i] > safe2) ? fabs(r[i]) / w[i] : (fabs(r[i]) + safe1) / (w[i] + safe1);
+        if (q > s) s = q;
+      }
+      berr[k] = s;
+      if (s > eps && 2.0 * s <= lstres && count <= 5) {
+        orc_pdgetrs(trans, n, 1, AF, ldaf, iaf, jaf, ipiv, r, n, 1, 1);
+        for (int i = 0; i < n; ++i) x[i] = x[i] + r[i];
+        lstres = s;
+        ++count;
+        continue;
+      }
+      break;
+    }
+    for (int i = 0; i < n; ++i)
+      w[i] = (w[i] > safe2) ? fabs(r[i]) + nz * eps * w[i] : fabs(r[i]) + nz * eps * w[i] + safe1;
+    struct orc_rfs_ctx c = {notran ? 'N' : 'T', notran ? 'T' : 'N', n, AF, ldaf, iaf, jaf, ipiv, w};
+    const double est = orc_dlacon(n, orc_rfs_op, &c);
+    double xmax = 0.0;
+    for (int i = 0; i < n; ++i) xmax = fmax(xmax, fabs(x[i]));
+    if (xmax != 0.0) ferr[k] = est / xmax;
+  }
+  free(r); free(w);
+}
+
+/* PDGESVX (SRC/pdgesvx.f:660-845) on a 1x1 grid, after argument checks.
+ * R[i] is R(i+1) and C[j] is C(j+1) (full local arrays); ferr/berr are the
+ * full FERR/BERR arrays (FERR(j) = ferr[j-1]).  With FACT = 'F', TRANS = 'N'
+ * and column equilibration, X is multiplied by C (the reference multiplies by
+ * a workspace it never filled there).  mglob_af is DESCAF(M_), nb = NB_AF.
+ * Returns INFO. */
+int orc_pdgesvx(char fact, char trans, int n, int nrhs, double* A, int lda, int ia, int ja,
+                double* AF, int ldaf, int iaf, int jaf, int mglob_af, int nb, int* ipiv,
+                char* equed, double* R, double* C, double* B, int ldb, int ib, int jb, double* X,
+                int ldx, int ix, int jx, double* rcond, double* ferr, double* berr) {
+  const int nofact = (fact == 'N'), equil = (fact == 'E'), notran = (trans == 'N');
+  int rowequ = 0, colequ = 0;
+  double rowcnd = 1.0, colcnd = 1.0;
+  const double smlnum = ORC_SAFMIN, bignum = 1.0 / smlnum;
+  if (nofact || equil) {
+    *equed = 'N';
+  } else {
+    rowequ = (*equed == 'R' || *equed == 'B');
+    colequ = (*equed == 'C' || *equed == 'B');
+    if (rowequ) {
+      double mn = bignum, mx = 0.0;
+      for (int i = 0; i < n; ++i) { mn = fmin(mn, R[ia - 1 + i]); mx = fmax(mx, R[ia - 1 + i]); }
+      rowcnd = n > 0 ? fmax(mn, smlnum) / fmin(mx, bignum) : 1.0;
+    }
+    if (colequ) {
+      double mn = bignum, mx = 0.0;
+      for (int j = 0; j < n; ++j) { mn = fmin(mn, C[ja - 1 + j]); mx = fmax(mx, C[ja - 1 + j]); }
+      colcnd = n > 0 ? fmax(mn, smlnum) / fmin(mx, bignum) : 1.0;
+    }
+  }
+  if (n == 0) {
+    *rcond = 1.0;
+    for (int k = 0; k < nrhs; ++k) { ferr[jb - 1 + k] = 0.0; berr[jb - 1 + k] = 0.0; }
+    return 0;
+  }
+  /* 1. equilibrate */
+  if (equil) {
+    double rc = 1.0, cc = 1.0, amax = 0.0;
+    const int infequ = orc_pdgeequ(n, n, A, lda, ia, ja, R + (ia - 1), C + (ja - 1), &rc, &cc, &amax);
+    if (infequ == 0) {
+      rowcnd = rc;
+      colcnd = cc;
+      *equed = orc_pdlaqge(n, n, A, lda, ia, ja, R + (ia - 1), C + (ja - 1), rowcnd, colcnd, amax);
+      rowequ = (*equed == 'R' || *equed == 'B');
+      colequ = (*equed == 'C' || *equed == 'B');
+    }
+  }
+  /* scale B: R(IB..) rows (op = N) or C(JA..) (op = T) */
+  if (notran ? rowequ : colequ) {
+    for (int k = 0; k < nrhs; ++k)
+      for (int i = 0; i < n; ++i) {
+        const double v = notran ? R[ib - 1 + i] : C[ja - 1 + i];
+        A_AT(B, ldb, ib - 1 + i, jb - 1 + k) = v * A_AT(B, ldb, ib - 1 + i, jb - 1 + k);
+      }
+  }
+  /* 2. factor */
+  if (nofact || equil) {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i)
+        A_AT(AF, ldaf, iaf - 1 + i, jaf - 1 + j) = A_AT(A, lda, ia - 1 + i, ja - 1 + j);
+    const int info = orc_pdgetrf(n, n, AF, ldaf, iaf, jaf, nb, mglob_af, ipiv);
+    if (info != 0) {
+      if (info > 0) *rcond = 0.0;
+      return info;
+    }
+  }
+  /* 3. condition estimate */
+  const char norm = notran ? '1' : 'I';
+  const double anorm = orc_pdlange(norm, n, A, lda, ia, ja);
+  *rcond = orc_pdgecon(norm, n, AF, ldaf, iaf, jaf, anorm);
+  if (*rcond < orc_eps()) return ia + n;
+  /* 4. solve, 5. refine */
+  for (int k = 0; k < nrhs; ++k)
+    for (int i = 0; i < n; ++i)
+      A_AT(X, ldx, ix - 1 + i, jx - 1 + k) = A_AT(B, ldb, ib - 1 + i, jb - 1 + k);
+  orc_pdgetrs(notran ? 'N' : 'T', n, nrhs, AF, ldaf, iaf, jaf, ipiv, X, ldx, ix, jx);
+  orc_pdgerfs(notran ? 'N' : 'T', n, nrhs, A, lda, ia, ja, AF, ldaf, iaf, jaf, ipiv, B, ldb, ib,
+              jb, X, ldx, ix, jx, ferr + (jb - 1), berr + (jb - 1));
+  /* 6. back to the original system */
+  if (notran ? colequ : rowequ) {
+    const double cnd = notran ? colcnd : rowcnd;
+    for (int k = 0; k < nrhs; ++k) {
+      for (int i = 0; i < n; ++i) {
+        const double v = notran ? C[ja - 1 + i] : R[ix - 1 + i];
+        A_AT(X, ldx, ix - 1 + i, jx - 1 + k) = v * A_AT(X, ldx, ix - 1 + i, jx - 1 + k);
+      }
+      ferr[jx - 1 + k] = ferr[jx - 1 + k] / cnd;
+    }
+  }
+  return 0;
 }

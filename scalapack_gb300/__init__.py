@@ -24,7 +24,8 @@ from . import _build
 __all__ = [
     "lib", "descinit", "numroc", "blacs_gridinit", "blacs_gridinfo", "blacs_gridexit",
     "blacs_exit", "pdgetrf", "pdgetrs", "pdgesv", "dgetrf_dev", "dgetrs_dev", "dgesv_dev",
-    "DLEN", "CTXT_", "M_", "N_", "MB_", "NB_", "LLD_",
+    "DLEN", "CTXT_", "M_", "N_", "MB_", "NB_", "LLD_", "pdgerfs", "pdgesvx", "pdgeequ", "pdlaqge",
+    "dgeequ_dev", "dgerfs_dev",
 ]
 
 DLEN = 9
@@ -105,6 +106,24 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_dgecon_dev.restype = C.c_int
     L.sl1x1_dgetri_dev.argtypes = [C.c_int, vp, C.c_longlong, vp, vp]
     L.sl1x1_dgetri_dev.restype = C.c_int
+    ip = C.POINTER(C.c_int)
+    dp_ = C.POINTER(C.c_double)
+    L.pdgerfs_.argtypes = [C.c_char_p, ip, ip, vp, ip, ip, ip, vp, ip, ip, ip, vp, vp, ip, ip, ip,
+                           vp, ip, ip, ip, vp, vp, vp, ip, vp, ip, ip, C.c_size_t]
+    L.pdgerfs_.restype = None
+    L.pdgesvx_.argtypes = [C.c_char_p, C.c_char_p, ip, ip, vp, ip, ip, ip, vp, ip, ip, ip, vp,
+                           C.c_char_p, vp, vp, vp, ip, ip, ip, vp, ip, ip, ip, dp_, vp, vp, vp, ip,
+                           vp, ip, ip, C.c_size_t, C.c_size_t, C.c_size_t]
+    L.pdgesvx_.restype = None
+    L.pdgeequ_.argtypes = [ip, ip, vp, ip, ip, ip, vp, vp, dp_, dp_, dp_, ip]
+    L.pdgeequ_.restype = None
+    L.pdlaqge_.argtypes = [ip, ip, vp, ip, ip, ip, vp, vp, dp_, dp_, dp_, C.c_char_p, C.c_size_t]
+    L.pdlaqge_.restype = None
+    L.sl1x1_dgeequ_dev.argtypes = [C.c_int, C.c_int, vp, C.c_longlong, vp, vp, dp_, dp_, dp_, vp]
+    L.sl1x1_dgeequ_dev.restype = C.c_int
+    L.sl1x1_dgerfs_dev.argtypes = [C.c_char, C.c_int, C.c_int, vp, C.c_longlong, vp, C.c_longlong,
+                                   vp, vp, C.c_longlong, vp, C.c_longlong, vp, vp, vp]
+    L.sl1x1_dgerfs_dev.restype = C.c_int
     L.sl1x1_finalize.argtypes = []
     L.sl1x1_set_default_nb.argtypes = [C.c_int]
     L.sl1x1_set_panel_rows.argtypes = [C.c_int]
@@ -240,6 +259,79 @@ def pdgetri(n, a, ia, ja, desca, ipiv, lwork=None, liwork=None):
     return info.value, work[0], int(iwork[0])
 
 
+def _vec(a):
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("expected a contiguous float64 vector")
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def pdgerfs(trans, n, nrhs, a, ia, ja, desca, af, iaf, jaf, descaf, ipiv, b, ib, jb, descb, x, ix,
+            jx, descx, ferr, berr, lwork=None, liwork=None):
+    """PDGERFS: X refined in place, FERR/BERR filled from JB; returns
+    (info, work0, iwork0). lwork/liwork = -1 queries."""
+    _, dpa = _desc(desca)
+    _, dpf = _desc(descaf)
+    _, dpb = _desc(descb)
+    _, dpx = _desc(descx)
+    lw = 3 * max(1, n) + 8 if lwork is None else lwork
+    liw = max(1, n) + 8 if liwork is None else liwork
+    work = np.zeros(max(1, lw if lw > 0 else 1), dtype=np.float64)
+    iwork = np.zeros(max(1, liw if liw > 0 else 1), dtype=np.int32)
+    info = C.c_int()
+    lib().pdgerfs_(trans.encode()[:1], _i(n), _i(nrhs), _arr(a, np.float64), _i(ia), _i(ja), dpa,
+                   _arr(af, np.float64), _i(iaf), _i(jaf), dpf, ipiv.ctypes.data_as(C.c_void_p),
+                   _arr(b, np.float64), _i(ib), _i(jb), dpb, _arr(x, np.float64), _i(ix), _i(jx), dpx,
+                   _vec(ferr), _vec(berr), work.ctypes.data_as(C.c_void_p), _i(lw),
+                   iwork.ctypes.data_as(C.c_void_p), _i(liw), C.byref(info), 1)
+    return info.value, work[0], int(iwork[0])
+
+
+def pdgesvx(fact, trans, n, nrhs, a, ia, ja, desca, af, iaf, jaf, descaf, ipiv, equed, r, c, b, ib,
+            jb, descb, x, ix, jx, descx, ferr, berr, lwork=None, liwork=None):
+    """PDGESVX: returns dict(info, equed, rcond, work0, iwork0); A, AF, IPIV,
+    R, C, B, X, FERR and BERR are updated in place as the reference does."""
+    _, dpa = _desc(desca)
+    _, dpf = _desc(descaf)
+    _, dpb = _desc(descb)
+    _, dpx = _desc(descx)
+    nb = max(1, int(desca[5]))
+    lw = 6 * max(1, n) + 4 * nb + 64 if lwork is None else lwork
+    liw = max(1, n) + 8 if liwork is None else liwork
+    work = np.zeros(max(1, lw if lw > 0 else 1), dtype=np.float64)
+    iwork = np.zeros(max(1, liw if liw > 0 else 1), dtype=np.int32)
+    info = C.c_int()
+    rcond = C.c_double(-1.0)
+    eq = C.create_string_buffer(equed.encode()[:1], 2)
+    lib().pdgesvx_(fact.encode()[:1], trans.encode()[:1], _i(n), _i(nrhs), _arr(a, np.float64),
+                   _i(ia), _i(ja), dpa, _arr(af, np.float64), _i(iaf), _i(jaf), dpf,
+                   ipiv.ctypes.data_as(C.c_void_p), eq, _vec(r), _vec(c), _arr(b, np.float64), _i(ib),
+                   _i(jb), dpb, _arr(x, np.float64), _i(ix), _i(jx), dpx, C.byref(rcond), _vec(ferr),
+                   _vec(berr), work.ctypes.data_as(C.c_void_p), _i(lw),
+                   iwork.ctypes.data_as(C.c_void_p), _i(liw), C.byref(info), 1, 1, 1)
+    return dict(info=info.value, equed=eq.value.decode(), rcond=rcond.value, work0=work[0],
+                iwork0=int(iwork[0]))
+
+
+def pdgeequ(m, n, a, ia, ja, desca, r, c):
+    """PDGEEQU: R(IA..) and C(JA..) filled; returns (info, rowcnd, colcnd, amax)."""
+    _, dp = _desc(desca)
+    rc, cc, am = C.c_double(-1.0), C.c_double(-1.0), C.c_double(-1.0)
+    info = C.c_int()
+    lib().pdgeequ_(_i(m), _i(n), _arr(a, np.float64), _i(ia), _i(ja), dp, _vec(r), _vec(c),
+                   C.byref(rc), C.byref(cc), C.byref(am), C.byref(info))
+    return info.value, rc.value, cc.value, am.value
+
+
+def pdlaqge(m, n, a, ia, ja, desca, r, c, rowcnd, colcnd, amax) -> str:
+    """PDLAQGE: sub(A) scaled in place; returns EQUED."""
+    _, dp = _desc(desca)
+    eq = C.create_string_buffer(b"?", 2)
+    lib().pdlaqge_(_i(m), _i(n), _arr(a, np.float64), _i(ia), _i(ja), dp, _vec(r), _vec(c),
+                   C.byref(C.c_double(rowcnd)), C.byref(C.c_double(colcnd)),
+                   C.byref(C.c_double(amax)), eq, 1)
+    return eq.value.decode()
+
+
 # ------------------------------------------------------------ phase timers
 PHASES = ["panel", "laswp", "trsm", "gemm", "solve", "mixed_gemm", "mixed_panel", "refine",
           "batched", "residual", "precond"]
@@ -351,6 +443,25 @@ def dgetrs_dev(trans, n, nrhs, a_ptr, ldda, ipiv_ptr, b_ptr, lddb, stream=None) 
     return lib().sl1x1_dgetrs_dev(trans.encode()[:1], n, nrhs, C.c_void_p(a_ptr), ldda,
                                   C.c_void_p(ipiv_ptr), C.c_void_p(b_ptr), lddb,
                                   _stream_ptr(stream))
+
+
+def dgeequ_dev(m, n, a_ptr, ldda, r_ptr, c_ptr, stream=None):
+    """PDGEEQU on device data: returns (info, rowcnd, colcnd, amax)."""
+    rc, cc, am = C.c_double(-1.0), C.c_double(-1.0), C.c_double(-1.0)
+    info = lib().sl1x1_dgeequ_dev(m, n, a_ptr, ldda, r_ptr, c_ptr, C.byref(rc), C.byref(cc),
+                                  C.byref(am), _stream_ptr(stream))
+    return info, rc.value, cc.value, am.value
+
+
+def dgerfs_dev(trans, n, nrhs, a_ptr, ldda, af_ptr, lddaf, ipiv_ptr, b_ptr, lddb, x_ptr, lddx,
+               stream=None):
+    """PDGERFS on device data (ipiv 1-based): returns (info, ferr, berr)."""
+    ferr = np.zeros(max(1, nrhs))
+    berr = np.zeros(max(1, nrhs))
+    info = lib().sl1x1_dgerfs_dev(trans.encode()[:1], n, nrhs, a_ptr, ldda, af_ptr, lddaf, ipiv_ptr,
+                                  b_ptr, lddb, x_ptr, lddx, ferr.ctypes.data_as(C.c_void_p),
+                                  berr.ctypes.data_as(C.c_void_p), _stream_ptr(stream))
+    return info, ferr[:nrhs], berr[:nrhs]
 
 
 def dgesv_dev(n, nrhs, a_ptr, ldda, ipiv_ptr, b_ptr, lddb, nb=0, stream=None) -> int:

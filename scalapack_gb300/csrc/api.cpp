@@ -19,14 +19,11 @@
 #include <vector>
 
 #include "../../include/sl1x1.h"
+#include "host_state.h"
 #include "sl_internal.h"
 
-namespace {
-
-// Descriptor entries (0-based C indices of the Fortran DESC(1..9)).
-enum { DTYPE_ = 0, CTXT_ = 1, M_ = 2, N_ = 3, MB_ = 4, NB_ = 5, RSRC_ = 6, CSRC_ = 7, LLD_ = 8 };
-// Fortran positions of the descriptor entries (DESC(k) has k = index + 1).
-enum { FDTYPE = 1, FCTXT = 2, FM = 3, FN = 4, FMB = 5, FNB = 6, FRSRC = 7, FCSRC = 8, FLLD = 9 };
+namespace sl {
+namespace host {
 
 std::mutex g_mu;       // device state and the LU entry points
 std::mutex g_grid_mu;  // the 1x1 BLACS shim's context table
@@ -128,41 +125,6 @@ void chk1mat(int ma, int mapos0, int na, int napos0, int ia, int ja, const int* 
 }
 
 // ------------------------------------------------------------- device state
-struct DevState {
-  bool init = false;
-  bool ok = false;
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  cudaStream_t aux = nullptr;       // look-ahead stream (higher priority)
-  cudaEvent_t ev_next = nullptr, ev_panel = nullptr;
-  double* dA = nullptr; size_t capA = 0;
-  double* dB = nullptr; size_t capB = 0;
-  int* dipiv = nullptr; size_t capP = 0;
-  int* dsmall = nullptr;      // bar[2], status, info_col
-  double* dcand = nullptr;
-  int* dperm = nullptr; size_t capPerm = 0;
-  double* dbswap = nullptr; size_t capBs = 0;
-  // mixed-precision workspace
-  float* dF = nullptr; size_t capF = 0;
-  int* dpermx = nullptr; size_t capPermx = 0;
-  double* dR = nullptr; size_t capR = 0;
-  double* dD = nullptr; size_t capD = 0;
-  float* dXf = nullptr; size_t capXf = 0;
-  float* dXt = nullptr; size_t capXt = 0;
-  double* dcm = nullptr; size_t capCm = 0;
-  double* dV = nullptr; size_t capV = 0;
-  double* dw = nullptr; size_t capW = 0;
-  double* dAx = nullptr; size_t capAx = 0;
-  double* dh = nullptr; size_t capH = 0;
-  double* dAcopy = nullptr; size_t capAcopy = 0;
-  int* dchain = nullptr; size_t capChain = 0;
-  double* dsplitk = nullptr; size_t capSplitk = 0;
-  double* daux = nullptr; size_t capAux = 0;
-  int chain_epoch = 0;
-  unsigned short* dA16 = nullptr; size_t capA16 = 0;
-  unsigned short* dB16 = nullptr; size_t capB16 = 0;
-  int* dcolexp = nullptr; size_t capCe = 0;
-};
 DevState g_dev;
 int g_default_nb = 256;
 bool g_lookahead = true;
@@ -196,18 +158,6 @@ bool ensure_device() {
   return true;
 }
 
-template <class T>
-cudaError_t grow(T** p, size_t* cap, size_t need) {
-  if (need <= *cap && *p) return cudaSuccess;
-  if (*p) cudaFree(*p);
-  *p = nullptr;
-  *cap = 0;
-  size_t n = need < 1 ? 1 : need;
-  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
-  if (e == cudaSuccess) *cap = n;
-  return e;
-}
-
 void release_all() {
   if (!g_dev.ok) return;
   cudaFree(g_dev.dA); cudaFree(g_dev.dB); cudaFree(g_dev.dipiv); cudaFree(g_dev.dsmall);
@@ -217,6 +167,8 @@ void release_all() {
   cudaFree(g_dev.dXf); cudaFree(g_dev.dXt); cudaFree(g_dev.dcm); cudaFree(g_dev.dV);
   cudaFree(g_dev.dw); cudaFree(g_dev.dAx); cudaFree(g_dev.dh); cudaFree(g_dev.dAcopy);
   cudaFree(g_dev.dchain); cudaFree(g_dev.dsplitk); cudaFree(g_dev.daux);
+  cudaFree(g_dev.dA2); cudaFree(g_dev.dX); cudaFree(g_dev.drw); cudaFree(g_dev.drc);
+  cudaFree(g_dev.dipiv2);
   sl::splitk_scratch() = sl::SplitKScratch();
   if (g_dev.stream) cudaStreamDestroy(g_dev.stream);
   if (g_dev.aux) cudaStreamDestroy(g_dev.aux);
@@ -319,10 +271,13 @@ int validate_getrf(const char* name, int m, int n, int ia, int ja, const int* de
   return info;
 }
 
-}  // namespace
+}  // namespace host
+}  // namespace sl
+
+using namespace sl::host;
 
 namespace sl {
-int default_nb() { return g_default_nb; }
+int default_nb() { return host::g_default_nb; }
 }  // namespace sl
 
 extern "C" {

@@ -192,18 +192,17 @@ static cudaError_t apply_inv(bool trans, int n, const double* LU, long long lda,
 
 // Estimate ||B||_1 with B = inv(U)inv(L) (onenrm) or its transpose (infinity
 // norm of inv(A)). work: 3*n + 8 doubles; iw: 4 ints.
-cudaError_t dgecon_device(bool onenrm, int n, const double* LU, long long lda, double anorm,
-                          double* rcond, double* work, int* iw, cudaStream_t s) {
-  *rcond = 0.0;
-  if (n == 0) { *rcond = 1.0; return cudaSuccess; }
-  if (anorm == 0.0) return cudaSuccess;
-  if (n == 1) { *rcond = 1.0; return cudaSuccess; }
+// Hager's estimate of the 1-norm of an n x n operator B given only products
+// (the reverse-communication loop of PDLACON, SRC/pdlacon.f, restated as a
+// host-driven loop): apply(true, x) overwrites x with B x, apply(false, x)
+// with B^T x. work holds 3n + 4 doubles, iw 2 ints; n >= 2.
+cudaError_t lacon_estimate(int n, const LaconApply& apply, double* work, int* iw, cudaStream_t s,
+                           double* est_out) {
   double* x = work;
   double* xi = work + n;
   double* tmp = work + 2 * (size_t)n;
-  double* scal = work + 3 * (size_t)n;  // [0] sum |y|, [1] |z_j|, [2] |z_jlast|
+  double* scal = work + 3 * (size_t)n;  // [0] sum |y|, [1] |z_j|
   const unsigned g = (unsigned)((n + 255) / 256);
-  const bool t1 = !onenrm;  // KASE 1 applies B, KASE 2 applies B^T
   auto asum = [&](const double* v, double* out) -> cudaError_t {
     rowred_abs_kernel<<<g, 256, 0, s>>>(v, n, n, 1, 0, tmp);  // |v_i| (one column)
     vec_reduce_kernel<<<1, 1024, 0, s>>>(tmp, n, 1, out);
@@ -217,7 +216,7 @@ cudaError_t dgecon_device(bool onenrm, int n, const double* LU, long long lda, d
   // x = (1/n, ..., 1/n); y = B x
   fill_kernel<<<g, 256, 0, s>>>(x, n, 1.0 / n);
   count_launches(1);
-  SL_TRY(apply_inv(t1, n, LU, lda, x, s));
+  SL_TRY(apply(true, x));
   SL_TRY(asum(x, scal));
   double est = 0.0;
   SL_TRY(read(&est, scal, sizeof(double)));
@@ -226,7 +225,7 @@ cudaError_t dgecon_device(bool onenrm, int n, const double* LU, long long lda, d
   sign_kernel<<<g, 256, 0, s>>>(x, n, xi, xi, 0, iw);
   SL_TRY(cudaMemcpyAsync(x, xi, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   count_launches(1);
-  SL_TRY(apply_inv(!t1, n, LU, lda, x, s));
+  SL_TRY(apply(false, x));
   iamax_kernel<<<1, 1024, 0, s>>>(x, n, iw + 1, scal + 1);
   count_launches(1);
   int iter = 2;
@@ -236,7 +235,7 @@ cudaError_t dgecon_device(bool onenrm, int n, const double* LU, long long lda, d
     // x = e_j; y = B x
     unit_vec_kernel<<<g, 256, 0, s>>>(x, n, iw + 1);
     count_launches(1);
-    SL_TRY(apply_inv(t1, n, LU, lda, x, s));
+    SL_TRY(apply(true, x));
     const double est_old = est;
     SL_TRY(asum(x, scal));
     SL_TRY(read(&est, scal, sizeof(double)));
@@ -248,7 +247,7 @@ cudaError_t dgecon_device(bool onenrm, int n, const double* LU, long long lda, d
     if (!changed || est <= est_old) break;  // repeated sign vector or no growth
     SL_TRY(cudaMemcpyAsync(xi, tmp, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
     SL_TRY(cudaMemcpyAsync(x, xi, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-    SL_TRY(apply_inv(!t1, n, LU, lda, x, s));
+    SL_TRY(apply(false, x));
     double zlast = 0.0;
     // |z(jlast)| of the new z, then the new argmax
     SL_TRY(cudaMemcpyAsync(&zlast, x + j, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -264,12 +263,27 @@ cudaError_t dgecon_device(bool onenrm, int n, const double* LU, long long lda, d
   // alternative estimate
   altsgn_kernel<<<g, 256, 0, s>>>(x, n);
   count_launches(1);
-  SL_TRY(apply_inv(t1, n, LU, lda, x, s));
+  SL_TRY(apply(true, x));
   SL_TRY(asum(x, scal));
   double alt = 0.0;
   SL_TRY(read(&alt, scal, sizeof(double)));
   alt = 2.0 * alt / (3.0 * n);
   if (alt > est) est = alt;
+  *est_out = est;
+  return cudaSuccess;
+}
+
+cudaError_t dgecon_device(bool onenrm, int n, const double* LU, long long lda, double anorm,
+                          double* rcond, double* work, int* iw, cudaStream_t s) {
+  *rcond = 0.0;
+  if (n == 0) { *rcond = 1.0; return cudaSuccess; }
+  if (anorm == 0.0) return cudaSuccess;
+  if (n == 1) { *rcond = 1.0; return cudaSuccess; }
+  const bool t1 = !onenrm;  // KASE 1 applies B, KASE 2 applies B^T
+  double est = 0.0;
+  SL_TRY(lacon_estimate(
+      n, [&](bool kase1, double* x) { return apply_inv(kase1 ? t1 : !t1, n, LU, lda, x, s); }, work,
+      iw, s, &est));
   if (est != 0.0 && std::isfinite(est)) *rcond = (1.0 / est) / anorm;
   return cudaSuccess;
 }

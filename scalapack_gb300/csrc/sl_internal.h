@@ -1,6 +1,8 @@
 // Internal interfaces shared by the sl1x1 translation units (not exported).
 #pragma once
 #include <cuda_runtime.h>
+
+#include <functional>
 #include <stddef.h>
 
 #ifndef SL_TRY
@@ -181,6 +183,34 @@ cudaError_t dlange_device(char norm, int m, int n, const double* A, long long ld
                           double* result, cudaStream_t s);
 cudaError_t dgecon_device(bool onenrm, int n, const double* LU, long long lda, double anorm,
                           double* rcond, double* work, int* iw, cudaStream_t s);
+// Operator of the 1-norm estimator: apply(true, x) -> B x, apply(false, x) -> B^T x.
+using LaconApply = std::function<cudaError_t(bool, double*)>;
+// PDLACON's estimate of ||B||_1 (n >= 2); work 3n + 4 doubles, iw 2 ints.
+cudaError_t lacon_estimate(int n, const LaconApply& apply, double* work, int* iw, cudaStream_t s,
+                           double* est);
+
+// ---- refinement, error bounds, equilibration (refine.cu) ----
+// Device workspace of dgerfs_device in doubles.
+size_t refine_work_doubles(int n);
+// PDGERFS on device data: X refined in place; ferr/berr are host arrays of
+// nrhs entries (ferr[k] is left unchanged when column k of X is zero, as the
+// reference does). dipiv is 0-based.
+cudaError_t dgerfs_device(char trans, int n, int nrhs, const double* A, long long lda,
+                          const double* AF, long long ldaf, const int* dipiv, const double* B,
+                          long long ldb, double* X, long long ldx, double* ferr, double* berr,
+                          const LuWork& ws, double* work, int* iw, cudaStream_t s);
+// PDGEEQU: R (m) and C (n) device arrays; scalars and INFO on the host.
+// work holds max(m, n) + 4 doubles, iw 1 int.
+cudaError_t dgeequ_device(int m, int n, const double* A, long long lda, double* R, double* C,
+                          double* rowcnd, double* colcnd, double* amax, int* info, double* work,
+                          int* iw, cudaStream_t s);
+// PDLAQGE's decision: 'N', 'R', 'C' or 'B'.
+char dlaqge_equed(double rowcnd, double colcnd, double amax);
+cudaError_t dlaqge_device(int m, int n, double* A, long long lda, const double* R, const double* C,
+                          char equed, cudaStream_t s);
+// X(i, c) *= v_i for c < ncols.
+cudaError_t scale_rows_device(int n, int ncols, double* X, long long ldx, const double* v,
+                              cudaStream_t s);
 cudaError_t dgetri_device(int n, double* dA, long long lda, const int* dipiv, double* X,
                           const LuWork& ws, int* dflag, int* info, cudaStream_t s);
 
