@@ -17,9 +17,9 @@
  *   INFO = -(i*100+j)  entry j of the i-th (array) argument is illegal
  *   INFO = K > 0   U(K,K) is exactly zero (factorization completed)
  *   INFO <= -10000 GPU failure: -10000 - cudaError_t for a CUDA runtime error,
- *                  -20000 - s for a device status s (1: a bounded grid barrier
- *                  timed out, 2: a bounded flag wait timed out), -30000 when
- *                  the problem exceeds a documented size limit of the GPU path.
+ *                  -20000 - s for a device status s (2: a bounded wait on
+ *                  data another CTA publishes timed out), -30000 when the
+ *                  problem exceeds a documented size limit of the GPU path.
  */
 #ifndef SL1X1_H
 #define SL1X1_H

@@ -179,7 +179,6 @@ void release_all() {
 
 sl::LuWork make_work() {
   sl::LuWork w;
-  w.bar = g_dev.dsmall;
   w.status = g_dev.dsmall + 2;
   w.info_col = g_dev.dsmall + 3;
   w.cand = g_dev.dcand;

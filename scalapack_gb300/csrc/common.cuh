@@ -9,13 +9,13 @@ namespace sl {
 // into INFO = -(10000 + code) by the host layer.
 enum DevStatus : int {
   kOk = 0,
-  kBarrierTimeout = 1,   // a bounded grid barrier gave up
-  kFlagTimeout = 2,      // a bounded flag wait gave up
+  kBarrierTimeout = 1,   // reserved: a bounded grid barrier gave up (no kernel uses one now)
+  kFlagTimeout = 2,      // a bounded wait on another CTA's published data gave up
   kBadArgument = 3,      // kernel-side argument check failed
 };
 
-// Upper bound on spin iterations of any device-side wait. With the
-// __nanosleep back-off below this is several seconds of waiting, after which
+// Upper bound on spin iterations of any device-side wait: each iteration is at
+// least one L2 round trip, so this is several seconds of waiting, after which
 // the kernel records an error and returns instead of hanging the GPU.
 constexpr long long kSpinLimit = 1LL << 24;
 
@@ -29,38 +29,6 @@ __device__ __forceinline__ void st_release_gpu(int* p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Grid-wide barrier for cooperatively launched kernels (all CTAs co-resident).
-// state[0] = arrival counter, state[1] = generation. The host zeroes both
-// before each launch. Every wait is bounded: on timeout the CTA sets
-// *status = kBarrierTimeout and returns false; callers then leave the kernel.
-__device__ __forceinline__ bool grid_barrier(int* state, int nblocks, int* status) {
-  __syncthreads();
-  __shared__ int s_ok;
-  if (threadIdx.x == 0) {
-    s_ok = 1;
-    int gen = ld_acquire_gpu(&state[1]);
-    __threadfence();
-    int arrived = atomicAdd(&state[0], 1) + 1;
-    if (arrived == nblocks) {
-      state[0] = 0;
-      __threadfence();
-      st_release_gpu(&state[1], gen + 1);
-    } else {
-      long long spins = 0;
-      while (ld_acquire_gpu(&state[1]) == gen) {
-        if (++spins > kSpinLimit) {
-          atomicExch(status, (int)kBarrierTimeout);
-          s_ok = 0;
-          break;
-        }
-        if (spins > 64) __nanosleep(64);
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
 
 // IDAMAX ordering key. Reference BLAS IDAMAX keeps the first maximal |x| and a
 // NaN never replaces the running maximum, so NaN entries are mapped below every

@@ -30,7 +30,7 @@ struct DevState {
   double* dA = nullptr; size_t capA = 0;
   double* dB = nullptr; size_t capB = 0;
   int* dipiv = nullptr; size_t capP = 0;
-  int* dsmall = nullptr;      // bar[2], status, info_col
+  int* dsmall = nullptr;      // [2] status, [3] first zero-pivot column, [4] mixed status
   double* dcand = nullptr;
   int* dperm = nullptr; size_t capPerm = 0;
   double* dbswap = nullptr; size_t capBs = 0;

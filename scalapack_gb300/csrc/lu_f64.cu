@@ -11,8 +11,8 @@
 //
 // The NB-wide panel is factored as 32-column sub-panels; each sub-panel is one
 // cooperative kernel whose CTAs hold disjoint row slices of the sub-panel in
-// shared memory and meet at one bounded grid barrier per column (pivot search
-// across CTAs). The remaining columns of the NB panel are brought up to date
+// shared memory and exchange each column's pivot candidates through tagged
+// words in L2 (bounded polls, no grid barrier). The remaining columns of the NB panel are brought up to date
 // with the same swap / triangular-solve / GEMM kernels, so the final factors,
 // pivots and INFO are those of the reference's column-by-column PDGETF2 in
 // exact arithmetic.

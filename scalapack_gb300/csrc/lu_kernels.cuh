@@ -55,17 +55,10 @@ constexpr int PX_WORDS = PX_VALS + PMAXG * 2 * 2 * PW;
 constexpr int PT = 256;      // threads per panel CTA
 constexpr int PLD = PW + 1;  // shared row stride: conflict-free row and column walks
 
-// Factor rows [r0, m) x columns [c0, c0+w) (w <= 32) of A in place.
-//
-// Cooperative launch, one CTA per contiguous slice of rpc rows, the slice held
-// in shared memory. Per column: warp-shuffle IDAMAX inside each CTA, each
-// CTA's best (|x|, row) and its row values published to an L2 slot array
-// (double-buffered by column parity), one bounded grid barrier, then every CTA
-// selects the same winner (largest |x|, lowest row on ties), exchanges the
-// winner and diagonal rows it owns, scales its part of the column by ONE/GMAX
-// (reciprocal then multiply, SRC/pdgetf2.f:224) and applies the rank-1 update
-// with lanes = columns. Writes ipiv[c0+k] = r0 + pivot (0-based rows of A) for
+// Factor rows [r0, m) x columns [c0, c0+w) (w <= 32) of A in place (the
+// panel kernel below): writes ipiv[c0+k] = r0 + pivot (0-based rows of A) for
 // k < min(w, m-r0) and the first exactly-zero pivot column into *info_col.
+//
 // Tagged 8-byte words {32-bit payload, 32-bit tag} carry the per-column
 // exchange between the panel's CTAs: a word is valid once its tag equals the
 // column's tag, so readers poll the data itself and no separate grid barrier

@@ -8,16 +8,17 @@
 // other entry points grow library-owned device buffers on demand; this one
 // allocates nothing.
 //
-// The factorization's only scratch -- the grid-barrier counters, the device
-// status word, the first-zero-pivot column and the panel kernel's candidate
-// slots -- lives in the file-scope array below, a fixed 1 MiB that every GPU
+// The factorization's only scratch -- the device status word, the
+// first-zero-pivot column and the panel kernel's exchange area -- lives in the
+// file-scope array below, a fixed 1 MiB that every GPU
 // which loads this library holds until the process exits. The caller passes
 // the matrix and the pivot array as usual.
 //
 // Set-up: the first call on each device looks up the device address of that
 // array (cudaGetSymbolAddress, with that device current) and caches it; make
 // that first call before any stream capture. Every call shares the one array:
-// the call re-initializes the barrier, status and zero-pivot words itself,
+// the call re-initializes the status and zero-pivot words and every panel
+// launch clears its exchange area,
 // but two calls whose GPU work overlaps (on different streams or from
 // different host threads) race on it and must not be issued.
 #include <cuda_runtime.h>
@@ -32,13 +33,12 @@
 namespace {
 
 // Stated maximum of the static scratch: 1 MiB. It holds 4 ints at offset 0
-// (two words kept for the panel's synchronization, status word, first
-// zero-pivot column) and from offset 256 the panel's candidate slots, per-column
-// election words and arrival counters.
+// (two spare words, status word, first zero-pivot column) and from offset 256
+// the panel kernel's exchange area.
 constexpr size_t kScratchBytes = (size_t)1 << 20;
 constexpr size_t kCandOffset = 256;
 static_assert(kCandOffset + sl::kPanelCandDoubles * sizeof(double) <= kScratchBytes,
-              "panel candidate slots must fit the static scratch");
+              "the panel exchange area must fit the static scratch");
 
 static __device__ __align__(256) unsigned char g_dgetrf_scratch[kScratchBytes];
 
@@ -86,9 +86,8 @@ extern "C" int sl1x1_dgetrf_noalloc(int m, int n, double* dA, long long ldda, in
   }
 
   sl::LuWork w;
-  w.bar = static_cast<int*>(base);
-  w.status = w.bar + 2;
-  w.info_col = w.bar + 3;
+  w.status = static_cast<int*>(base) + 2;
+  w.info_col = static_cast<int*>(base) + 3;
   w.cand = reinterpret_cast<double*>(static_cast<unsigned char*>(base) + kCandOffset);
   w.perm = nullptr;
   w.bswap = nullptr;
@@ -98,7 +97,7 @@ extern "C" int sl1x1_dgetrf_noalloc(int m, int n, double* dA, long long ldda, in
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   sl::ProfSuppress no_events;  // phase timers would create CUDA events
   // dgetrf_device zeroes the status word and resets the zero-pivot column,
-  // and every panel launch zeroes the barrier words, before use.
+  // and every panel launch clears its exchange area, before use.
   e = sl::dgetrf_device(m, n, dA, ldda, dipiv, nb > 0 ? nb : sl::default_nb(), w, s);
   if (e == cudaErrorInvalidValue) return -30000;
   if (e != cudaSuccess) return cuda_info(e);

@@ -58,10 +58,9 @@ cudaError_t dgemm(bool transa, int m, int n, int k, double alpha, const double* 
 // Device workspace used by the FP64 factorization / solve (sized by the
 // caller through lu_workspace_bytes).
 struct LuWork {
-  int* bar;          // 2 ints: grid barrier state
   int* status;       // 1 int: device status word (DevStatus)
   int* info_col;     // 1 int: first zero-pivot column (0-based), INT_MAX if none
-  double* cand;      // candidate slots of the panel kernel
+  double* cand;      // exchange area of the panel kernel (kPanelCandDoubles words)
   int* perm;         // n ints: composed row permutation (solve)
   double* bswap;     // n * nrhs doubles: gathered right-hand sides (solve)
   size_t perm_len;
