@@ -110,6 +110,37 @@ void pdlaqge_(const int* M, const int* N, double* A, const int* IA, const int* J
               const int* DESCA, const double* R, const double* C, const double* ROWCND,
               const double* COLCND, const double* AMAX, char* EQUED, size_t EQUED_len);
 
+/* ---- Redistribution in front of the LU (REDIST) ------------------------- */
+
+/* Replaces PDGEMR2D, REDIST/SRC/pdgemr.c:1-20 (SUBROUTINE PDGEMR2D(M, N, A,
+ * IA, JA, DESCA, B, IB, JB, DESCB, ICTXT)): copies sub(A) into sub(B). This
+ * library's contexts are 1x1 grids, so on one process it is a submatrix copy
+ * between two descriptors; a process outside a context passes CTXT = -1 for
+ * it. Between processes, the sl1x1_redist_* pieces below do the per-pair work
+ * and a transport moves the buffers. */
+void pdgemr2d_(const int* M, const int* N, const double* A, const int* IA, const int* JA,
+               const int* DESCA, double* B, const int* IB, const int* JB, const int* DESCB,
+               const int* ICTXT);
+
+/* Redistribution between two 2D block-cyclic layouts, one process pair at a
+ * time (no counterpart symbol in the reference; it is the pack / unpack step
+ * of PDGEMR2D). sub(A) = A(ia:ia+m-1, ja:ja+n-1) laid out by desca on a
+ * p0 x q0 grid, sub(B) by descb on a p1 x q1 grid; (sr, sc) is the source
+ * process in A's grid, (dr, dc) the destination in B's. The buffer holds the
+ * elements of sub(A) owned by both, column-major in submatrix coordinates.
+ * Each returns the element count (-1 for an invalid descriptor or grid). */
+long long sl1x1_redist_count(int m, int n, int ia, int ja, const int* desca, int p0, int q0,
+                             int sr, int sc, int ib, int jb, const int* descb, int p1, int q1,
+                             int dr, int dc);
+/* Copies the pair's elements from the source's local array A into buf. */
+long long sl1x1_redist_pack(int m, int n, int ia, int ja, const int* desca, int p0, int q0, int sr,
+                            int sc, int ib, int jb, const int* descb, int p1, int q1, int dr,
+                            int dc, const double* A, double* buf);
+/* Copies buf into the destination's local array B. */
+long long sl1x1_redist_unpack(int m, int n, int ia, int ja, const int* desca, int p0, int q0,
+                              int sr, int sc, int ib, int jb, const int* descb, int p1, int q1,
+                              int dr, int dc, const double* buf, double* B);
+
 /* ---- TOOLS used by callers of the LU path ------------------------------- */
 
 /* Replaces DESCINIT, TOOLS/descinit.f:1-192. */

@@ -25,7 +25,7 @@ __all__ = [
     "lib", "descinit", "numroc", "blacs_gridinit", "blacs_gridinfo", "blacs_gridexit",
     "blacs_exit", "pdgetrf", "pdgetrs", "pdgesv", "dgetrf_dev", "dgetrs_dev", "dgesv_dev",
     "DLEN", "CTXT_", "M_", "N_", "MB_", "NB_", "LLD_", "pdgerfs", "pdgesvx", "pdgeequ", "pdlaqge",
-    "dgeequ_dev", "dgerfs_dev",
+    "dgeequ_dev", "dgerfs_dev", "pdgemr2d",
 ]
 
 DLEN = 9
@@ -124,6 +124,8 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_dgerfs_dev.argtypes = [C.c_char, C.c_int, C.c_int, vp, C.c_longlong, vp, C.c_longlong,
                                    vp, vp, C.c_longlong, vp, C.c_longlong, vp, vp, vp]
     L.sl1x1_dgerfs_dev.restype = C.c_int
+    L.pdgemr2d_.argtypes = [ip, ip, vp, ip, ip, ip, vp, ip, ip, ip, ip]
+    L.pdgemr2d_.restype = None
     L.sl1x1_finalize.argtypes = []
     L.sl1x1_set_default_nb.argtypes = [C.c_int]
     L.sl1x1_set_panel_rows.argtypes = [C.c_int]
@@ -310,6 +312,14 @@ def pdgesvx(fact, trans, n, nrhs, a, ia, ja, desca, af, iaf, jaf, descaf, ipiv, 
                    iwork.ctypes.data_as(C.c_void_p), _i(liw), C.byref(info), 1, 1, 1)
     return dict(info=info.value, equed=eq.value.decode(), rcond=rcond.value, work0=work[0],
                 iwork0=int(iwork[0]))
+
+
+def pdgemr2d(m, n, a, ia, ja, desca, b, ib, jb, descb, ictxt=-1):
+    """PDGEMR2D between this process's 1x1 contexts: sub(A) copied into sub(B)."""
+    _, dpa = _desc(desca)
+    _, dpb = _desc(descb)
+    lib().pdgemr2d_(_i(m), _i(n), _arr(a, np.float64), _i(ia), _i(ja), dpa, _arr(b, np.float64),
+                    _i(ib), _i(jb), dpb, _i(ictxt))
 
 
 def pdgeequ(m, n, a, ia, ja, desca, r, c):
