@@ -100,13 +100,18 @@ __device__ __forceinline__ void block_argmax(const T* P, int ldp, int k, int m, 
 
 // Factor the n x n matrix W (column-major, ld n) in place. ipiv receives
 // 0-based rows; returns INFO (first zero pivot, 1-based) in *info.
+// stage / stage_len: shared scratch idle during the factorization, used to
+// apply each panel's row interchanges to the other columns.
 template <typename T, int CH>
-__device__ void factor_system(T* W, int n, int* ipiv, int* info, unsigned char* smem) {
+__device__ void factor_system(T* W, int n, int* ipiv, int* info, unsigned char* smem, T* stage,
+                              int stage_len) {
   T* P = reinterpret_cast<T*>(smem);               // [kBMaxN][kBPB+1] panel, row-major
-  T* Us = P + kBMaxN * (kBPB + 1);                   // [kBPB][CH] U12 chunk
+  T* Us = P + kBMaxN * (kBPB + 1);                   // [kBPB][CH+1] U12 chunk (padded rows)
+  constexpr int UL = CH + 1;
   __shared__ double s_key[32];
   __shared__ int s_row[32];
   __shared__ int s_info;
+  __shared__ int s_trow[2 * kBPB], s_tsrc[2 * kBPB], s_tcnt;
   const int tid = threadIdx.x, NT = blockDim.x;
   const int PL = kBPB + 1;
   if (tid == 0) s_info = 0;
@@ -149,20 +154,58 @@ __device__ void factor_system(T* W, int n, int* ipiv, int* info, unsigned char* 
       W[(j + r) + (long long)(j + c) * n] = P[r * PL + c];
     }
     __syncthreads();
-    // row interchanges on the other columns
-    for (int c = tid; c < n; c += NT) {
-      if (c >= j && c < j + jb) continue;
-      T* col = W + (long long)c * n;
+    // Row interchanges on the other columns (PDLASWP) as one composite
+    // permutation: warp 0 replays the jb swaps on row labels (rows j..j+jb-1
+    // and the pivot rows below), then every moved value of a chunk of
+    // columns is read into `stage` before any is written back.
+    if (tid < 32) {
+      const int lane = tid;
+      int cnt = jb;
+      for (int e = lane; e < jb; e += 32) { s_trow[e] = j + e; s_tsrc[e] = j + e; }
+      __syncwarp();
       for (int k = 0; k < jb; ++k) {
-        int p = ipiv[j + k];
-        if (p != j + k) {
-          T t = col[j + k];
-          col[j + k] = col[p];
-          col[p] = t;
+        const int p = ipiv[j + k];
+        if (p == j + k) continue;
+        int e = -1;
+        if (p < j + jb) {
+          e = p - j;
+        } else {
+          for (int base = jb; base < cnt && e < 0; base += 32) {
+            const int q = base + lane;
+            const unsigned hit = __ballot_sync(0xffffffffu, q < cnt && s_trow[q] == p);
+            if (hit) e = base + __ffs(hit) - 1;
+          }
+          if (e < 0) {
+            e = cnt++;
+            if (lane == 0) { s_trow[e] = p; s_tsrc[e] = p; }
+          }
         }
+        __syncwarp();
+        if (lane == 0) { const int t = s_tsrc[k]; s_tsrc[k] = s_tsrc[e]; s_tsrc[e] = t; }
+        __syncwarp();
       }
+      if (lane == 0) s_tcnt = cnt;
     }
     __syncthreads();
+    {
+      const int cnt = s_tcnt;
+      const int cw = stage_len / cnt;  // columns per chunk (cnt <= 64)
+      for (int c0 = 0; c0 < n; c0 += cw) {
+        const int nc = min(cw, n - c0);
+        for (int idx = tid; idx < nc * cnt; idx += NT) {
+          const int e = idx % cnt, c = c0 + idx / cnt;
+          if ((c < j || c >= j + jb) && s_tsrc[e] != s_trow[e])
+            stage[idx] = W[s_tsrc[e] + (long long)c * n];
+        }
+        __syncthreads();
+        for (int idx = tid; idx < nc * cnt; idx += NT) {
+          const int e = idx % cnt, c = c0 + idx / cnt;
+          if ((c < j || c >= j + jb) && s_tsrc[e] != s_trow[e])
+            W[s_trow[e] + (long long)c * n] = stage[idx];
+        }
+        __syncthreads();
+      }
+    }
     const int nr = n - j - jb;  // trailing columns
     if (nr > 0) {
       // U12 = L11^-1 A12, one thread per column, L11 from the shared panel
@@ -189,7 +232,7 @@ __device__ void factor_system(T* W, int n, int* ipiv, int* info, unsigned char* 
           const int cw = min(CH, n - c0);
           for (int idx = tid; idx < jb * CH; idx += NT) {
             int k = idx % jb, c = idx / jb;
-            Us[k * CH + c] = c < cw ? W[(j + k) + (long long)(c0 + c) * n] : (T)0;
+            Us[k * UL + c] = c < cw ? W[(j + k) + (long long)(c0 + c) * n] : (T)0;
           }
           __syncthreads();
           for (int r = tid; r < mr; r += NT) {
@@ -200,7 +243,7 @@ __device__ void factor_system(T* W, int n, int* ipiv, int* info, unsigned char* 
             for (int k = 0; k < jb; ++k) {
               const T a = lrow[k];
 #pragma unroll
-              for (int c = 0; c < CH; ++c) acc[c] = fma(a, Us[k * CH + c], acc[c]);
+              for (int c = 0; c < CH; ++c) acc[c] = fma(a, Us[k * UL + c], acc[c]);
             }
             T* crow = W + (j + jb + r) + (long long)c0 * n;
 #pragma unroll
@@ -217,22 +260,26 @@ __device__ void factor_system(T* W, int n, int* ipiv, int* info, unsigned char* 
   __syncthreads();
 }
 
-// Solve with the factors of factor_system: X (n x nrhs, ldx) holds the
-// right-hand sides on entry and the solution on exit. Xs: shared scratch of
-// n*nrhs values; perm: n ints of shared memory.
-template <typename T>
-__device__ void solve_system(const T* W, int n, const int* ipiv, T* X, int ldx, int nrhs, T* Xs,
-                             int* perm) {
-  const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31, warp = tid >> 5;
-  const int nw = NT >> 5;
-  for (int i = tid; i < n; i += NT) perm[i] = i;
+// The row permutation of the factorization (PDLAPIV's interchanges composed):
+// perm[i] = original row that ends up in row i. Computed once per system.
+__device__ void compose_perm(const int* ipiv, int n, int* perm) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = i;
   __syncthreads();
-  if (tid == 0)
+  if (threadIdx.x == 0)
     for (int i = 0; i < n; ++i) {
-      int q = ipiv[i];
-      if (q != i) { int t = perm[i]; perm[i] = perm[q]; perm[q] = t; }
+      const int q = ipiv[i];
+      if (q != i) { const int t = perm[i]; perm[i] = perm[q]; perm[q] = t; }
     }
   __syncthreads();
+}
+
+// Solve with the factors of factor_system: X (n x nrhs, ldx) holds the
+// right-hand sides on entry and the solution on exit. Xs: shared scratch of
+// n*nrhs values; perm: the composed permutation (shared memory).
+template <typename T>
+__device__ void solve_system(const T* W, int n, const int* perm, T* X, int ldx, int nrhs, T* Xs) {
+  const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int nw = NT >> 5;
   for (int idx = tid; idx < n * nrhs; idx += NT) {
     int i = idx % n, c = idx / n;
     Xs[i + c * n] = X[perm[i] + (long long)c * ldx];
@@ -260,7 +307,9 @@ __device__ void solve_system(const T* W, int n, const int* ipiv, T* X, int ldx, 
         for (int c = 0; c < kBMaxRhs; ++c)
           if (c < nrhs) acc[c] = fma(l, Xs[k0 + i + c * n], acc[c]);
       }
-      for (int c = 0; c < nrhs; ++c) Xs[r + c * n] -= acc[c];
+#pragma unroll
+      for (int c = 0; c < kBMaxRhs; ++c)
+        if (c < nrhs) Xs[r + c * n] -= acc[c];
     }
     __syncthreads();
   }
@@ -289,7 +338,9 @@ __device__ void solve_system(const T* W, int n, const int* ipiv, T* X, int ldx, 
         for (int c = 0; c < kBMaxRhs; ++c)
           if (c < nrhs) acc[c] = fma(u, Xs[k0 + i + c * n], acc[c]);
       }
-      for (int c = 0; c < nrhs; ++c) Xs[r + c * n] -= acc[c];
+#pragma unroll
+      for (int c = 0; c < kBMaxRhs; ++c)
+        if (c < nrhs) Xs[r + c * n] -= acc[c];
     }
     __syncthreads();
   }
@@ -300,43 +351,80 @@ __device__ void solve_system(const T* W, int n, const int* ipiv, T* X, int ldx, 
   __syncthreads();
 }
 
+// NaN-propagating maximum (a NaN, once seen, stays): the tester's norm semantics.
+__device__ __forceinline__ double nanmax(double m, double v) { return (v > m || v != v) ? v : m; }
+
 // R = B - A X (FP64) into shared Rs (n x nrhs); returns the scaled residual
 // max_c ||r_c|| / (||A|| ||x_c|| n eps) (tester semantics, LIN/pdlaschk.f).
+// X is staged in shared memory (Xsh, n*nrhs doubles) so the pass over A is the
+// only global stream, read with 8 loads in flight per thread; ||A||_inf is
+// passed in (*anorm >= 0, from the copy into the working matrix) or computed.
 __device__ double residual_system(const double* A, int lda, int n, const double* B, int ldb,
-                                  const double* X, int ldx, int nrhs, double* Rs, double* s_red) {
-  const int tid = threadIdx.x, NT = blockDim.x;
+                                  const double* X, int ldx, int nrhs, double* Rs, double* s_red,
+                                  double* Xsh, double* anorm) {
+  const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int nw = NT >> 5;
+  __shared__ double s_rm[32][kBMaxRhs], s_xm[32][kBMaxRhs];
+  for (int idx = tid; idx < n * nrhs; idx += NT) {
+    const int i = idx % n, c = idx / n;
+    Xsh[i + c * n] = X[i + (long long)c * ldx];
+  }
+  __syncthreads();
+  const bool need_norm = !(*anorm >= 0.0);
   double rowmax = 0.0;
+  double rm[kBMaxRhs], xm[kBMaxRhs];
+#pragma unroll
+  for (int c = 0; c < kBMaxRhs; ++c) { rm[c] = 0.0; xm[c] = 0.0; }
   for (int r = tid; r < n; r += NT) {
     double acc[kBMaxRhs];
 #pragma unroll
     for (int c = 0; c < kBMaxRhs; ++c) acc[c] = (c < nrhs) ? B[r + (long long)c * ldb] : 0.0;
     double rs = 0.0;
+    const double* ar = A + r;
+#pragma unroll 8
     for (int k = 0; k < n; ++k) {
-      const double a = A[r + (long long)k * lda];
-      rs += fabs(a);
+      const double a = ar[(long long)k * lda];
+      if (need_norm) rs += fabs(a);
 #pragma unroll
       for (int c = 0; c < kBMaxRhs; ++c)
-        if (c < nrhs) acc[c] = fma(-a, X[k + (long long)c * ldx], acc[c]);
+        if (c < nrhs) acc[c] = fma(-a, Xsh[k + c * n], acc[c]);
     }
     rowmax = fmax(rowmax, rs);
-    for (int c = 0; c < nrhs; ++c) Rs[r + c * n] = acc[c];
+#pragma unroll
+    for (int c = 0; c < kBMaxRhs; ++c)
+      if (c < nrhs) {
+        Rs[r + c * n] = acc[c];
+        rm[c] = nanmax(rm[c], fabs(acc[c]));
+        xm[c] = nanmax(xm[c], fabs(Xsh[r + c * n]));
+      }
   }
-  // block max of the row sums
-  for (int off = 16; off > 0; off >>= 1) rowmax = fmax(rowmax, __shfl_xor_sync(0xffffffffu, rowmax, off));
-  if ((tid & 31) == 0) s_red[tid >> 5] = rowmax;
+  // block reductions: max row sum, and per column max |r| and max |x|
+  for (int off = 16; off > 0; off >>= 1) {
+    rowmax = fmax(rowmax, __shfl_xor_sync(0xffffffffu, rowmax, off));
+#pragma unroll
+    for (int c = 0; c < kBMaxRhs; ++c) {
+      rm[c] = nanmax(rm[c], __shfl_xor_sync(0xffffffffu, rm[c], off));
+      xm[c] = nanmax(xm[c], __shfl_xor_sync(0xffffffffu, xm[c], off));
+    }
+  }
+  if (lane == 0) {
+    s_red[warp] = rowmax;
+#pragma unroll
+    for (int c = 0; c < kBMaxRhs; ++c) { s_rm[warp][c] = rm[c]; s_xm[warp][c] = xm[c]; }
+  }
   __syncthreads();
   if (tid == 0) {
-    double an = 0.0;
-    for (int w = 0; w < (NT >> 5); ++w) an = fmax(an, s_red[w]);
+    double an = *anorm;
+    if (need_norm) {
+      an = 0.0;
+      for (int w = 0; w < nw; ++w) an = fmax(an, s_red[w]);
+      *anorm = an;
+    }
     double worst = 0.0;
     for (int c = 0; c < nrhs; ++c) {
-      double rm = 0.0, xm = 0.0;
-      for (int i = 0; i < n; ++i) {
-        double rv = fabs(Rs[i + c * n]), xv = fabs(X[i + (long long)c * ldx]);
-        if (rv > rm || rv != rv) rm = rv;
-        if (xv > xm || xv != xv) xm = xv;
-      }
-      double v = rm / (xm * an * ldexp(1.0, -53) * n);
+      double r1 = 0.0, x1 = 0.0;
+      for (int w = 0; w < nw; ++w) { r1 = nanmax(r1, s_rm[w][c]); x1 = nanmax(x1, s_xm[w][c]); }
+      const double v = r1 / (x1 * an * ldexp(1.0, -53) * n);
       if (!(v <= worst)) worst = v;
     }
     s_red[32] = worst;
@@ -358,21 +446,43 @@ __device__ void run_system(const BatchArgs& a, int sys, bool fp64_pass, unsigned
   const double* B = a.B[sys];
   const int ldb = a.ldb[sys];
   // shared layout: factor scratch, then Xs (n*nrhs TF), Rs (n*nrhs double), perm (n ints)
-  unsigned char* after = smem + sizeof(TF) * (kBMaxN * (kBPB + 1) + kBPB * CH);
+  unsigned char* after = smem + sizeof(TF) * (kBMaxN * (kBPB + 1) + kBPB * (CH + 1));
   TF* Xs = reinterpret_cast<TF*>(after);
   double* Rs = reinterpret_cast<double*>(after + sizeof(double) * kBMaxN * kBMaxRhs);
   int* perm = reinterpret_cast<int*>(after + 2 * sizeof(double) * kBMaxN * kBMaxRhs);
+  double* Xsh = reinterpret_cast<double*>(after);  // X staged by residual_system (Xs is idle then)
   __shared__ double s_red[40];
+  __shared__ double s_anorm;
   __shared__ int s_info;
   __shared__ int s_ok;
-  // working copy in the factorization precision
-  for (long long idx = tid; idx < (long long)n * n; idx += NT) {
-    int r = (int)(idx % n);
-    long long c = idx / n;
-    W[idx] = (TF)A[r + c * lda];
+  // working copy in the factorization precision; one thread per row, so the
+  // same pass gives ||A||_inf (row sums of |a|)
+  {
+    double rs_max = 0.0;
+    for (int r = tid; r < n; r += NT) {
+      double rs = 0.0;
+      const double* ar = A + r;
+#pragma unroll 8
+      for (int c = 0; c < n; ++c) {
+        const double v = ar[(long long)c * lda];
+        rs += fabs(v);
+        W[r + (long long)c * n] = (TF)v;
+      }
+      rs_max = fmax(rs_max, rs);
+    }
+    for (int off = 16; off > 0; off >>= 1) rs_max = fmax(rs_max, __shfl_xor_sync(0xffffffffu, rs_max, off));
+    if ((tid & 31) == 0) s_red[tid >> 5] = rs_max;
+    __syncthreads();
+    if (tid == 0) {
+      double an = 0.0;
+      for (int w = 0; w < (NT >> 5); ++w) an = fmax(an, s_red[w]);
+      s_anorm = an;
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  factor_system<TF, CH>(W, n, ipiv, &s_info, smem);
+  // Xs and Rs are idle while factoring: they stage the row interchanges
+  factor_system<TF, CH>(W, n, ipiv, &s_info, smem, reinterpret_cast<TF*>(after),
+                        (int)(2 * sizeof(double) * kBMaxN * kBMaxRhs / sizeof(TF)));
   const int info = s_info;
   if (info != 0) {
     // Exactly singular in the factorization precision: in mode 1 hand the
@@ -390,6 +500,7 @@ __device__ void run_system(const BatchArgs& a, int sys, bool fp64_pass, unsigned
     __syncthreads();
     return;
   }
+  compose_perm(ipiv, n, perm);
   if constexpr (sizeof(TF) == 8) {
     // FP64: X = B, solve, residual
     for (int idx = tid; idx < n * nrhs; idx += NT) {
@@ -397,8 +508,8 @@ __device__ void run_system(const BatchArgs& a, int sys, bool fp64_pass, unsigned
       X[i + (long long)c * ldx] = B[i + (long long)c * ldb];
     }
     __syncthreads();
-    solve_system<TF>(W, n, ipiv, reinterpret_cast<TF*>(X), ldx, nrhs, Xs, perm);
-    double sr = residual_system(A, lda, n, B, ldb, X, ldx, nrhs, Rs, s_red);
+    solve_system<TF>(W, n, perm, reinterpret_cast<TF*>(X), ldx, nrhs, Xs);
+    double sr = residual_system(A, lda, n, B, ldb, X, ldx, nrhs, Rs, s_red, Xsh, &s_anorm);
     if (tid == 0) {
       a.info[sys] = 0;
       a.iters[sys] = fp64_pass ? -1 : 0;
@@ -413,8 +524,13 @@ __device__ void run_system(const BatchArgs& a, int sys, bool fp64_pass, unsigned
       X[i + (long long)c * ldx] = 0.0;
     }
     __syncthreads();
-    // initial residual r = b (x = 0)
-    double sr = residual_system(A, lda, n, B, ldb, X, ldx, nrhs, Rs, s_red);
+    // initial residual r = b (x = 0): no pass over A
+    for (int idx = tid; idx < n * nrhs; idx += NT) {
+      const int i = idx % n, c = idx / n;
+      Rs[i + c * n] = B[i + (long long)c * ldb];
+    }
+    __syncthreads();
+    double sr = 1.0 / 0.0;  // scaled residual of x = 0 (the loop always refines at least once)
     int steps = 0;
     if (tid == 0) s_ok = 0;
     __syncthreads();
@@ -438,14 +554,14 @@ __device__ void run_system(const BatchArgs& a, int sys, bool fp64_pass, unsigned
         Cx[i + c * n] = (TF)ldexp(Rs[i + c * n], -s_exp[c]);
       }
       __syncthreads();
-      solve_system<TF>(W, n, ipiv, Cx, n, nrhs, Xs, perm);
+      solve_system<TF>(W, n, perm, Cx, n, nrhs, Xs);
       for (int idx = tid; idx < n * nrhs; idx += NT) {
         int i = idx % n, c = idx / n;
         X[i + (long long)c * ldx] += ldexp((double)Cx[i + c * n], s_exp[c]);
       }
       __syncthreads();
       ++steps;
-      sr = residual_system(A, lda, n, B, ldb, X, ldx, nrhs, Rs, s_red);
+      sr = residual_system(A, lda, n, B, ldb, X, ldx, nrhs, Rs, s_red, Xsh, &s_anorm);
     }
     if (s_ok) {
       if (tid == 0) {
@@ -480,7 +596,7 @@ __global__ void batched_kernel(BatchArgs a, int fp64_pass) {
 
 template <typename TF, int CH>
 size_t batched_smem() {
-  return sizeof(TF) * (kBMaxN * (kBPB + 1) + kBPB * CH) + 2 * sizeof(double) * kBMaxN * kBMaxRhs +
+  return sizeof(TF) * (kBMaxN * (kBPB + 1) + kBPB * (CH + 1)) + 2 * sizeof(double) * kBMaxN * kBMaxRhs +
          sizeof(int) * kBMaxN + 64;
 }
 
