@@ -154,6 +154,7 @@ bool ensure_device() {
   }
   if (cudaMalloc(&g_dev.dsmall, 16 * sizeof(int)) != cudaSuccess) return false;
   if (cudaMalloc(&g_dev.dcand, sl::panel_cand_doubles() * sizeof(double)) != cudaSuccess) return false;
+  if (cudaMalloc(&g_dev.dplan, sl::kSwapPlanInts * sizeof(int)) != cudaSuccess) return false;
   g_dev.ok = true;
   return true;
 }
@@ -161,7 +162,7 @@ bool ensure_device() {
 void release_all() {
   if (!g_dev.ok) return;
   cudaFree(g_dev.dA); cudaFree(g_dev.dB); cudaFree(g_dev.dipiv); cudaFree(g_dev.dsmall);
-  cudaFree(g_dev.dcand); cudaFree(g_dev.dperm); cudaFree(g_dev.dbswap);
+  cudaFree(g_dev.dcand); cudaFree(g_dev.dplan); cudaFree(g_dev.dperm); cudaFree(g_dev.dbswap);
   cudaFree(g_dev.dA16); cudaFree(g_dev.dB16); cudaFree(g_dev.dcolexp);
   cudaFree(g_dev.dF); cudaFree(g_dev.dpermx); cudaFree(g_dev.dR); cudaFree(g_dev.dD);
   cudaFree(g_dev.dXf); cudaFree(g_dev.dXt); cudaFree(g_dev.dcm); cudaFree(g_dev.dV);
@@ -182,6 +183,7 @@ sl::LuWork make_work() {
   w.status = g_dev.dsmall + 2;
   w.info_col = g_dev.dsmall + 3;
   w.cand = g_dev.dcand;
+  w.swap_plan = g_dev.dplan;
   w.perm = g_dev.dperm;
   w.bswap = g_dev.dbswap;
   w.perm_len = g_dev.capPerm;

@@ -32,6 +32,7 @@ struct DevState {
   int* dipiv = nullptr; size_t capP = 0;
   int* dsmall = nullptr;      // [2] status, [3] first zero-pivot column, [4] mixed status
   double* dcand = nullptr;
+  int* dplan = nullptr;       // a panel's interchange plan (kSwapPlanInts)
   int* dperm = nullptr; size_t capPerm = 0;
   double* dbswap = nullptr; size_t capBs = 0;
   // mixed-precision workspace

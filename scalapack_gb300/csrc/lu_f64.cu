@@ -119,6 +119,10 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
       }
     }
   }
+  // the panel's interchanges in composite form, for the row interchanges of
+  // the other columns (computed here, on the panel's stream)
+  const int npiv = (m - j) < jb ? (m - j) : jb;
+  if (ws.swap_plan && npiv <= LSW_MAXP) SL_TRY(laswp_plan(j, j + npiv, dipiv, ws.swap_plan, s));
   phase_end(kPhPanel, s, pflops, 16.0 * (double)(m - j) * jb);
   return cudaSuccess;
 }
@@ -145,7 +149,7 @@ cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, 
     panel_on_aux = false;
     // ---- PDLASWP on the left and right column blocks ----
     phase_begin(kPhLaswp, s);
-    SL_TRY(laswp<double>(dA, ldda, j, j + jb, dipiv, 0, j, j + jb, n, s));
+    SL_TRY(laswp_planned<double>(dA, ldda, j, j + jb, dipiv, ws.swap_plan, 0, j, j + jb, n, s));
     phase_end(kPhLaswp, s, 0.0, 32.0 * jb * (double)(n - jb));
     const int jn = j + jb;                                   // next panel's first column
     const int jb2 = jn < mn ? ((mn - jn) < nb ? (mn - jn) : nb) : 0;

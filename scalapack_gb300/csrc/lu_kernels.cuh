@@ -430,6 +430,88 @@ laswp_kernel(T* A, long long lda, int k1, int k2, const int* __restrict__ ipiv, 
   }
 }
 
+// Plan of the interchanges k1..k2-1 (k2-k1 <= LSW_MAXP) in composite form:
+// plan[0] = number of pairs, then (row, src) pairs for every touched row whose
+// content changes (row receives the original content of src). One thread
+// replays the swaps on row labels with a hash table over the touched rows, so
+// the cost is a few shared-memory operations per interchange. Computed once
+// per panel, on the panel's stream; laswp_apply_kernel then only moves data.
+constexpr int LSW_HASH = 1024;
+static __global__ void laswp_plan_kernel(int k1, int k2, const int* __restrict__ ipiv, int* plan) {
+  __shared__ int s_row[2 * LSW_MAXP], s_src[2 * LSW_MAXP], s_tab[LSW_HASH];
+  const int npiv = k2 - k1;
+  for (int i = threadIdx.x; i < LSW_HASH; i += blockDim.x) s_tab[i] = -1;
+  for (int i = threadIdx.x; i < npiv; i += blockDim.x) { s_row[i] = k1 + i; s_src[i] = k1 + i; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int cnt = npiv;
+    for (int i = 0; i < npiv; ++i) {
+      const int p = ipiv[k1 + i];
+      if (p == k1 + i) continue;
+      int e;
+      if (p >= k1 && p < k2) {
+        e = p - k1;
+      } else {
+        int h = p & (LSW_HASH - 1);
+        while (s_tab[h] >= 0 && s_row[s_tab[h]] != p) h = (h + 1) & (LSW_HASH - 1);
+        if (s_tab[h] < 0) {  // first time this row is touched
+          e = cnt++;
+          s_row[e] = p;
+          s_src[e] = p;
+          s_tab[h] = e;
+        } else {
+          e = s_tab[h];
+        }
+      }
+      const int t = s_src[i];
+      s_src[i] = s_src[e];
+      s_src[e] = t;
+    }
+    int np = 0;
+    for (int e = 0; e < cnt; ++e)
+      if (s_src[e] != s_row[e]) {
+        plan[1 + 2 * np] = s_row[e];
+        plan[2 + 2 * np] = s_src[e];
+        ++np;
+      }
+    plan[0] = np;
+  }
+}
+
+// Applies a plan of laswp_plan_kernel to the columns [cb1,ce1) and
+// [cb2,ce2): one warp per column loads every moved value, then stores them.
+template <typename T>
+__global__ void __launch_bounds__(256)
+laswp_apply_kernel(T* A, long long lda, const int* __restrict__ plan, int cb1, int ce1, int cb2,
+                   int ce2) {
+  __shared__ int s_row[2 * LSW_MAXP], s_src[2 * LSW_MAXP];
+  const int np = plan[0];
+  for (int e = threadIdx.x; e < np; e += blockDim.x) {
+    s_row[e] = plan[1 + 2 * e];
+    s_src[e] = plan[2 + 2 * e];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long n1 = ce1 - cb1, ncols = n1 + (ce2 - cb2);
+  constexpr int PER = 2 * LSW_MAXP / 32;
+  for (long long ci = (long long)blockIdx.x * 8 + warp; ci < ncols; ci += (long long)gridDim.x * 8) {
+    const long long col = ci < n1 ? cb1 + ci : cb2 + (ci - n1);
+    T* a = A + col * lda;
+    T v[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int e = lane + 32 * q;
+      v[q] = (e < np) ? a[s_src[e]] : (T)0;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int e = lane + 32 * q;
+      if (e < np) a[s_row[e]] = v[q];
+    }
+  }
+}
+
 // op(T) X = B for a w x w triangle (w <= 256) and a strip of NC columns of B
 // per CTA, held in shared memory. FORWARD solves top-down (lower, or upper^T),
 // otherwise bottom-up. The triangle is staged in shared memory eb (<= 32)
@@ -490,27 +572,35 @@ trsm_strip_kernel(int w, int ncols, int eb, const T* __restrict__ Tm, long long 
 }
 
 // op(T) x = b for a w x w diagonal block (w <= 128) and few right-hand sides:
-// the CTA stages the block in shared memory (row stride w+1, conflict-free),
-// then each warp solves one column with its 4 rows per lane held in registers;
+// one CTA per right-hand side stages the block's triangle in shared memory
+// (row stride w+1, conflict-free) with all its warps, then warp 0 solves the
+// column with its 4 rows per lane held in registers;
 // x_i is broadcast with a shuffle, so no block-wide barrier sits on the
 // dependency chain. Non-unit diagonals divide (reference DTRSM semantics).
 template <typename T, bool UPPER, bool TRANS, bool UNIT>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
 trsv_warp_kernel(int w, int ncols, const T* __restrict__ Tm, long long ldt, T* B, long long ldb) {
   extern __shared__ __align__(16) unsigned char trsv_smem[];
   T* Ts = reinterpret_cast<T*>(trsv_smem);  // Ts[r*(w+1) + i] = op(T)(r, i)
   const int W1 = w + 1;
+  constexpr bool FORWARD = (UPPER == TRANS);
+  // stage only the triangle the solve reads (the diagonal too when non-unit),
+  // many loads in flight per thread
+#pragma unroll 8
   for (int idx = threadIdx.x; idx < w * w; idx += blockDim.x) {
     int r, i;
     if (!TRANS) { r = idx % w; i = idx / w; }  // coalesced along r
     else { i = idx % w; r = idx / w; }         // coalesced along i
-    Ts[r * W1 + i] = TRANS ? Tm[i + (long long)r * ldt] : Tm[r + (long long)i * ldt];
+    const bool need = FORWARD ? (r > i || (!UNIT && r == i)) : (r < i || (!UNIT && r == i));
+    if (need) Ts[r * W1 + i] = TRANS ? Tm[i + (long long)r * ldt] : Tm[r + (long long)i * ldt];
   }
   __syncthreads();
-  constexpr bool FORWARD = (UPPER == TRANS);
+  // one right-hand side per CTA, solved by warp 0: GB300's FP64 pipe is narrow
+  // per SM, so the columns' solves are spread over as many SMs as there are
+  // columns; the other warps only help staging
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long col = (long long)blockIdx.x * 4 + warp;
-  if (col >= ncols) return;
+  const long long col = blockIdx.x;
+  if (warp != 0 || col >= ncols) return;
   T x[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
@@ -855,6 +945,31 @@ inline cudaError_t laswp(T* A, long long lda, int k1, int k2, const int* ipiv, i
   return cudaGetLastError();
 }
 
+// Plan of a panel's interchanges (k2 - k1 <= LSW_MAXP), see laswp_plan_kernel.
+inline cudaError_t laswp_plan(int k1, int k2, const int* ipiv, int* plan, cudaStream_t s) {
+  if (k2 - k1 > LSW_MAXP) return cudaErrorInvalidValue;
+  if (k2 <= k1) return cudaMemsetAsync(plan, 0, sizeof(int), s);
+  laswp_plan_kernel<<<1, 256, 0, s>>>(k1, k2, ipiv, plan);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+// Row interchanges from a plan when one is available, else as laswp().
+template <typename T>
+inline cudaError_t laswp_planned(T* A, long long lda, int k1, int k2, const int* ipiv,
+                                 const int* plan, int cb1, int ce1, int cb2, int ce2,
+                                 cudaStream_t s) {
+  const long long ncols = (long long)(ce1 - cb1) + (ce2 - cb2);
+  if (ncols <= 0 || k2 <= k1) return cudaSuccess;
+  if (!plan || k2 - k1 > LSW_MAXP) return laswp<T>(A, lda, k1, k2, ipiv, cb1, ce1, cb2, ce2, s);
+  const long long want = (ncols + 7) / 8;
+  const long long cap = 4LL * num_sms();
+  laswp_apply_kernel<T><<<(unsigned)(want < cap ? want : cap), 256, 0, s>>>(A, lda, plan, cb1, ce1,
+                                                                            cb2, ce2);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 template <typename T, bool UPPER, bool TRANS, bool UNIT, int NC = 8>
 inline cudaError_t trsm_strip(int w, int ncols, const T* Tm, long long ldt, T* B, long long ldb,
                               cudaStream_t s) {
@@ -872,6 +987,48 @@ inline cudaError_t trsm_strip(int w, int ncols, const T* Tm, long long ldt, T* B
   kern<<<grid, 256, smem, s>>>(w, ncols, eb, Tm, ldt, B, ldb);
   count_launches(1);
   return cudaGetLastError();
+}
+
+// The same product with each row tile split across NC/4 column groups of 4
+// (64 rows per CTA for NC = 16, 128 for NC = 8): 4x more CTAs than
+// gemm_skinny_kernel, so that a product with few rows still fills every SM
+// (the off-diagonal updates of a blocked triangular solve with 8-16 right-hand
+// sides).
+template <typename T, bool TRANSA, int NC>
+__global__ void __launch_bounds__(256)
+gemm_skinny_rt_kernel(int m, int n, int k, T alpha, const T* __restrict__ A, long long lda,
+                      const T* __restrict__ B, long long ldb, T* C, long long ldc) {
+  static_assert(NC % 4 == 0 && NC >= 8, "column groups of 4");
+  constexpr int G = NC / 4;    // column groups
+  constexpr int RT = 256 / G;  // rows per CTA
+  __shared__ T Bs[64][NC];
+  const int g = threadIdx.x / RT, rl = threadIdx.x % RT;
+  const long long row = (long long)blockIdx.x * RT + rl;
+  T acc[4] = {(T)0, (T)0, (T)0, (T)0};
+  for (int k0 = 0; k0 < k; k0 += 64) {
+    const int kc = min(64, k - k0);
+    __syncthreads();
+    for (int c = threadIdx.x; c < 64 * NC; c += blockDim.x) {
+      int kk = c % 64, nn = c / 64;
+      Bs[kk][nn] = (kk < kc && nn < n) ? B[(k0 + kk) + (long long)nn * ldb] : (T)0;
+    }
+    __syncthreads();
+    if (row < m) {
+#pragma unroll 16
+      for (int kk = 0; kk < kc; ++kk) {
+        const T a = TRANSA ? A[(k0 + kk) + row * lda] : A[row + (long long)(k0 + kk) * lda];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[j] = fma(a, Bs[kk][g * 4 + j], acc[j]);
+      }
+    }
+  }
+  if (row < m) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = g * 4 + j;
+      if (c < n) C[row + (long long)c * ldc] += alpha * acc[j];
+    }
+  }
 }
 
 template <typename T, bool TA, int NC>
@@ -968,6 +1125,21 @@ inline cudaError_t gemm_skinny(bool transa, int m, int n, int k, T alpha, const 
       }
     }
   }
+  if (n > 4 && (m + 255) / 256 < 2 * num_sms()) {
+    // few rows: split each row tile over column groups so that every SM works
+    const int nc = n <= 8 ? 8 : 16;
+    const int rt = 256 / (nc / 4);
+    dim3 grid((unsigned)((m + rt - 1) / rt));
+    if (nc == 8) {
+      if (transa) gemm_skinny_rt_kernel<T, true, 8><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, C, ldc);
+      else gemm_skinny_rt_kernel<T, false, 8><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, C, ldc);
+    } else {
+      if (transa) gemm_skinny_rt_kernel<T, true, 16><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, C, ldc);
+      else gemm_skinny_rt_kernel<T, false, 16><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, C, ldc);
+    }
+    count_launches(1);
+    return cudaGetLastError();
+  }
 #define SL_SK(NC)                                                                              \
   return transa ? launch_skinny<T, true, NC>(m, n, k, alpha, A, lda, B, ldb, C, ldc, s)        \
                 : launch_skinny<T, false, NC>(m, n, k, alpha, A, lda, B, ldb, C, ldc, s)
@@ -1010,7 +1182,7 @@ inline cudaError_t diag_solve(int kb, int nrhs, const T* Td, long long lda, T* X
     auto kern = trsv_warp_kernel<T, UPPER, TRANS, UNIT>;
     SL_TRY(smem_attr_once((const void*)kern, 140 * 1024));
     const size_t smem = sizeof(T) * (size_t)kb * (kb + 1);
-    kern<<<(nrhs + 3) / 4, 128, smem, s>>>(kb, nrhs, Td, lda, X, ldx);
+    kern<<<nrhs, 256, smem, s>>>(kb, nrhs, Td, lda, X, ldx);
     count_launches(1);
     return cudaGetLastError();
   }

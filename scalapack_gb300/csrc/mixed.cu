@@ -250,6 +250,8 @@ static cudaError_t factor_panel_f32(int n, float* F, long long ldf, int* dipiv, 
                           Fp(r0, r0 + w), ldf, Fp(r0 + kw, r0 + w), ldf, s));
     }
   }
+  const int npiv = (m - j) < jb ? (m - j) : jb;
+  if (ws.swap_plan && npiv <= LSW_MAXP) SL_TRY(laswp_plan(j, j + npiv, dipiv, ws.swap_plan, s));
   phase_end(kPhMixedPanel, s, 0.0, 0.0);
   return cudaSuccess;
 }
@@ -274,7 +276,7 @@ cudaError_t sgetrf_mixed_device(int n, float* F, long long ldf, int* dipiv, int 
     const int jn = j + jb;
     const int jb2 = jn < mn ? ((mn - jn) < nb ? (mn - jn) : nb) : 0;
     phase_begin(kPhMixedPanel, s);
-    SL_TRY(laswp<float>(F, ldf, j, j + jb, dipiv, 0, j, j + jb, n, s));
+    SL_TRY(laswp_planned<float>(F, ldf, j, j + jb, dipiv, ws.swap_plan, 0, j, j + jb, n, s));
     if (jn < n)
       SL_TRY((trsm_strip<float, false, false, true>(jb, n - jn, Fp(j, j), ldf, Fp(j, jn), ldf, s)));
     phase_end(kPhMixedPanel, s, 0.0, 0.0);

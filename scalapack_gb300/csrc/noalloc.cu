@@ -9,8 +9,8 @@
 // allocates nothing.
 //
 // The factorization's only scratch -- the device status word, the
-// first-zero-pivot column and the panel kernel's exchange area -- lives in the
-// file-scope array below, a fixed 1 MiB that every GPU
+// first-zero-pivot column, the panel kernel's exchange area and the plan of a
+// panel's row interchanges -- lives in the file-scope array below, a fixed 1 MiB that every GPU
 // which loads this library holds until the process exits. The caller passes
 // the matrix and the pivot array as usual.
 //
@@ -33,12 +33,13 @@
 namespace {
 
 // Stated maximum of the static scratch: 1 MiB. It holds 4 ints at offset 0
-// (two spare words, status word, first zero-pivot column) and from offset 256
-// the panel kernel's exchange area.
+// (two spare words, status word, first zero-pivot column), from offset 256 the
+// panel kernel's exchange area, then the plan of a panel's row interchanges.
 constexpr size_t kScratchBytes = (size_t)1 << 20;
 constexpr size_t kCandOffset = 256;
-static_assert(kCandOffset + sl::kPanelCandDoubles * sizeof(double) <= kScratchBytes,
-              "the panel exchange area must fit the static scratch");
+constexpr size_t kPlanOffset = (kCandOffset + sl::kPanelCandDoubles * sizeof(double) + 255) / 256 * 256;
+static_assert(kPlanOffset + sl::kSwapPlanInts * sizeof(int) <= kScratchBytes,
+              "the panel exchange area and the interchange plan must fit the static scratch");
 
 static __device__ __align__(256) unsigned char g_dgetrf_scratch[kScratchBytes];
 
@@ -89,6 +90,7 @@ extern "C" int sl1x1_dgetrf_noalloc(int m, int n, double* dA, long long ldda, in
   w.status = static_cast<int*>(base) + 2;
   w.info_col = static_cast<int*>(base) + 3;
   w.cand = reinterpret_cast<double*>(static_cast<unsigned char*>(base) + kCandOffset);
+  w.swap_plan = reinterpret_cast<int*>(static_cast<unsigned char*>(base) + kPlanOffset);
   w.perm = nullptr;
   w.bswap = nullptr;
   w.perm_len = 0;

@@ -61,6 +61,7 @@ struct LuWork {
   int* status;       // 1 int: device status word (DevStatus)
   int* info_col;     // 1 int: first zero-pivot column (0-based), INT_MAX if none
   double* cand;      // exchange area of the panel kernel (kPanelCandDoubles words)
+  int* swap_plan = nullptr;  // kSwapPlanInts: composite form of a panel's interchanges
   int* perm;         // n ints: composed row permutation (solve)
   double* bswap;     // n * nrhs doubles: gathered right-hand sides (solve)
   size_t perm_len;
@@ -77,6 +78,8 @@ size_t panel_cand_doubles();
 // words, 2 x 224 x 4 key words, 224 CTAs x 2 parities x 64 row words);
 // panel_cand_doubles() returns it.
 constexpr size_t kPanelCandDoubles = (size_t)4 * 32 + (size_t)8 * 224 + (size_t)224 * 2 * 2 * 32;
+// Ints of a panel's interchange plan (count + 2 x 512 (row, src) pairs).
+constexpr size_t kSwapPlanInts = 1 + 4 * 256 + 15;
 // Largest M the FP64 panel supports on this device (rows held in shared memory).
 int panel_max_rows();
 // Smallest row slice per CTA of the cooperative panel (tunable; 0, the
