@@ -54,6 +54,8 @@ def parse():
     p.add_argument("--mixed-n", type=int, default=32768,
                    help="size of the mixed-precision LU-IR comparison (0 disables it)")
     p.add_argument("--mixed-fmts", default="bf16x3,fp16,bf16")
+    p.add_argument("--cond-n", type=int, default=8192,
+                   help="size of the conditioned-matrix sweep of the mixed solver (0 disables it)")
     p.add_argument("--batch", type=int, default=4096,
                    help="systems in the batched-solver comparison (0 disables it)")
     return p.parse_args()
@@ -216,6 +218,60 @@ def mixed_section(sl, torch, dev, args, stream):
         r["time_ratio_vs_fp64"] = r["time_to_solution_ms"] / ms64
         r["meets_target"] = bool(r["sresid"] < 16.0 and r["time_ratio_vs_fp64"] <= 1.0 / 3.0)
     del Ac, Bc, At, Bt
+    torch.cuda.empty_cache()
+    return out
+
+
+def conditioned_section(sl, torch, dev, args, stream):
+    """Config: N=cond_n, A = (H_1 ... H_64) diag(s) (G_1 ... G_64)^T with Householder
+    reflectors from seeded U[-0.5,0.5] vectors and s geometric from 1 to 1/kappa
+    (the pattern of TOOLS/LAPACK/dlagge.f), kappa in {1e2, 1e4, 1e6, 1e8}, NRHS=4,
+    B iid U[-1,1]: mixed LU-IR (BF16x3) against the plain FP64 GPU solve."""
+    n, nrhs = args.cond_n, 4
+    g = torch.Generator(device=dev).manual_seed(args.seed + 31)
+    out = {"workload": f"conditioned N={n} NRHS={nrhs}, 64+64 Householder reflectors around "
+                       "diag(s), s geometric 1..1/kappa (torch Philox seed), tol: scaled "
+                       "residual <= 1", "n": n, "nrhs": nrhs, "runs": {}}
+    piv = torch.zeros(n, dtype=torch.int32, device=dev)
+    for kappa in (1e2, 1e4, 1e6, 1e8):
+        s = torch.logspace(0.0, -float(np.log10(kappa)), n, dtype=torch.float64, device=dev)
+        A = torch.diag(s)
+        for side in (0, 1):
+            for _ in range(64):
+                v = torch.rand(n, dtype=torch.float64, device=dev, generator=g) - 0.5
+                tau = 2.0 / float(v @ v)
+                if side == 0:
+                    A -= tau * torch.outer(v, v @ A)
+                else:
+                    A -= tau * torch.outer(A @ v, v)
+        At = A.T.contiguous()  # column-major storage of A
+        Bt = (torch.rand((nrhs, n), dtype=torch.float64, device=dev, generator=g) * 2.0 - 1.0)
+        Xt = torch.zeros_like(Bt)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        info, it, st = sl.dgesv_ir_dev(n, nrhs, At.data_ptr(), n, piv.data_ptr(), Bt.data_ptr(), n,
+                                       Xt.data_ptr(), n, fmt="bf16x3", nb=256, tol=1.0,
+                                       keep_a=True, stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        Ac, Bc = At.clone(), Bt.clone()
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        info64 = sl.dgesv_dev(n, nrhs, Ac.data_ptr(), n, piv.data_ptr(), Bc.data_ptr(), n, 256,
+                              stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms64 = e0.elapsed_time(e1)
+        out["runs"][f"{kappa:.0e}"] = {
+            "info": info, "iter": it, "time_to_solution_ms": ms, "fp64_ms": ms64,
+            "time_ratio_vs_fp64": ms / ms64, "classical_steps": int(st["classical"]),
+            "gmres_outer": int(st["gmres_outer"]), "gmres_inner": int(st["gmres_inner"]),
+            "fell_back_to_fp64": bool(st["fell_back"]),
+            "sresid": torch_sresid(torch, A, Bt.T, Xt.T),
+            "sresid_fp64": torch_sresid(torch, A, Bt.T, Bc.T), "info_fp64": info64}
+        del A, At, Ac, Bc, Bt, Xt
     torch.cuda.empty_cache()
     return out
 
@@ -464,6 +520,9 @@ def run_gpu(args):
     mixed = None
     if args.mixed_n > 0:
         mixed = mixed_section(sl, torch, dev, args, stream)
+    conditioned = None
+    if args.cond_n > 0:
+        conditioned = conditioned_section(sl, torch, dev, args, stream)
     batched = None
     if args.batch > 0:
         batched = batched_section(sl, torch, dev, args, stream)
@@ -499,6 +558,7 @@ def run_gpu(args):
             "accuracy": {"sresid": sresid, "threshold": 16.0},
             "phases": phase_summary,
             "mixed_ir": mixed,
+            "conditioned": conditioned,
             "batched": batched,
             "yardstick_cublas_dgemm_tflops": yard,
         }

@@ -167,7 +167,7 @@ void release_all() {
   cudaFree(g_dev.dF); cudaFree(g_dev.dpermx); cudaFree(g_dev.dR); cudaFree(g_dev.dD);
   cudaFree(g_dev.dXf); cudaFree(g_dev.dXt); cudaFree(g_dev.dcm); cudaFree(g_dev.dV);
   cudaFree(g_dev.dw); cudaFree(g_dev.dAx); cudaFree(g_dev.dh); cudaFree(g_dev.dAcopy);
-  cudaFree(g_dev.dchain); cudaFree(g_dev.dsplitk); cudaFree(g_dev.daux);
+  cudaFree(g_dev.dchain); cudaFree(g_dev.dsplitk); cudaFree(g_dev.daux); cudaFree(g_dev.ddinv);
   cudaFree(g_dev.dA2); cudaFree(g_dev.dX); cudaFree(g_dev.drw); cudaFree(g_dev.drc);
   cudaFree(g_dev.dipiv2);
   sl::splitk_scratch() = sl::SplitKScratch();
@@ -639,6 +639,7 @@ int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, 
   GROW(dbswap, capBs, (size_t)n * nrhs);
   if (keep_a) GROW(dAcopy, capAcopy, (size_t)ldf * n);
   GROW(dsplitk, capSplitk, (size_t)32 * 4 * n);  // split-K partials of the FP64 products
+  GROW(ddinv, capDinv, (size_t)2 * ((n + 63) / 64) * 64 * 64);  // diagonal-block inverses
   if (e == cudaSuccess) {
     sl::splitk_scratch().ptr = g_dev.dsplitk;
     sl::splitk_scratch().bytes = g_dev.capSplitk * sizeof(double);
@@ -662,6 +663,7 @@ int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, 
   mw.V = g_dev.dV; mw.w = g_dev.dw; mw.Ax = g_dev.dAx; mw.h = g_dev.dh;
   mw.Acopy = keep_a ? g_dev.dAcopy : nullptr; mw.ldacopy = ldf;
   mw.chain = g_dev.dchain; mw.epoch = &g_dev.chain_epoch; mw.status = g_dev.dsmall + 4;
+  mw.dinv = g_dev.ddinv;
   if (e == cudaSuccess) e = cudaMemsetAsync(mw.status, 0, sizeof(int), s);
   if (e != cudaSuccess) return cuda_info(e);
   sl::LuWork w = make_work();

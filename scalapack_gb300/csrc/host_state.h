@@ -49,6 +49,7 @@ struct DevState {
   double* dh = nullptr; size_t capH = 0;
   double* dAcopy = nullptr; size_t capAcopy = 0;
   int* dchain = nullptr; size_t capChain = 0;
+  float* ddinv = nullptr; size_t capDinv = 0;
   double* dsplitk = nullptr; size_t capSplitk = 0;
   double* daux = nullptr; size_t capAux = 0;
   int chain_epoch = 0;

@@ -643,21 +643,22 @@ trsv_warp_kernel(int w, int ncols, const T* __restrict__ Tm, long long ldt, T* B
 // started: the waits below always end (no residency assumption). Solved
 // blocks are published as tagged words {x bits, epoch} in xt, so a consumer
 // polls the values themselves (one round trip, no flag and no fence). A CTA
-// stages its diagonal block and the off-diagonal block of its immediate
-// predecessor in shared memory, consumes the earlier solved blocks in chunks
-// of up to 8 (2 for more than 4 right-hand sides) as they appear (4 thread groups of 64 rows x 16 columns apply
-// the 64x64 blocks of the factor), and when the predecessor's x arrives only
-// a 64x64 product from shared memory and the diagonal solve (one warp per
-// right-hand side, shuffles) remain on the chain. Waits are bounded
+// stages the inverse of its diagonal block (precomputed once per factorization,
+// diag_inv) and the off-diagonal block of its immediate predecessor in shared
+// memory, consumes the earlier solved blocks in chunks as they appear (4
+// thread groups of 64 rows x 16 columns apply the 64x64 blocks of the factor),
+// and when the predecessor's x arrives only two 64x64 products from shared
+// memory remain on the chain (no serial substitution). Waits are bounded
 // (kSpinLimit); on timeout the CTA records kFlagTimeout in *status and stops.
 template <typename T, bool FORWARD, int NRM>
 __global__ void __launch_bounds__(256)
 trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long ldx, int nrhs,
-                  int* ticket, unsigned long long* xt, int epoch, int* status) {
+                  const T* __restrict__ Dinv, int* ticket, unsigned long long* xt, int epoch,
+                  int* status) {
   static_assert(sizeof(T) == 4, "tagged words carry 32-bit values");
   constexpr int KB = 64;
-  constexpr int kChunk = NRM > 4 ? 2 : 8;  // keeps static shared memory under 48 KB
-  __shared__ T Ds[KB][KB + 1];          // diagonal block, Ds[r][i] = A(r0+r, r0+i)
+  constexpr int kChunk = NRM > 4 ? 1 : (NRM > 1 ? 4 : 8);  // static shared memory under 48 KB
+  __shared__ T Ds[KB][KB + 1];          // inverse of the diagonal block, Ds[r][i]
   __shared__ T Ls[KB][KB + 1];          // predecessor block, Ls[r][i] = A(r0+r, kp*KB+i)
   __shared__ T xs[kChunk * KB][NRM];    // x of the blocks being applied
   __shared__ T part[4][KB][NRM];        // partial sums of the 4 column groups
@@ -673,10 +674,11 @@ trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long
   const int r0 = b * KB, rb = min(KB, n - r0);
   const int kp = FORWARD ? b - 1 : b + 1;  // predecessor in solve order
   const int wp = (sidx > 0) ? min(KB, n - kp * KB) : 0;
+  const T* Db = Dinv + (size_t)b * KB * KB;  // row-major [KB][KB]
   for (int idx = tid; idx < KB * KB; idx += 256) {
     int r = idx % KB, i = idx / KB;
-    Ds[r][i] = (r < rb && i < rb) ? A[(r0 + r) + (long long)(r0 + i) * lda] : (T)0;
     Ls[r][i] = (r < rb && i < wp) ? A[(r0 + r) + (long long)(kp * KB + i) * lda] : (T)0;
+    Ds[idx / KB][idx % KB] = Db[idx];
   }
   const int r = tid & (KB - 1), q = tid >> 6;
   const int warp = tid >> 5, lane = tid & 31;
@@ -787,29 +789,24 @@ trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long
 #pragma unroll
   for (int c = 0; c < NRM; ++c) part[q][r][c] = acc[c];
   __syncthreads();
-  // v = b - sum of the partials, diagonal solve: warp c owns column c, lanes own rows lane, lane+32
+  // v = b - sum of the partials, then x = inv(T_bb) v from shared memory:
+  // warp c owns column c, lanes own rows lane and lane+32
+  __shared__ T vs[8][KB];
   if (warp < nrhs) {
     const int c = warp;
-    T x0 = (T)0, x1 = (T)0;
-    if (lane < rb) x0 = bx0 - (part[0][lane][c] + part[1][lane][c] + part[2][lane][c] + part[3][lane][c]);
+    T v0 = (T)0, v1 = (T)0;
+    if (lane < rb) v0 = bx0 - (part[0][lane][c] + part[1][lane][c] + part[2][lane][c] + part[3][lane][c]);
     if (lane + 32 < rb)
-      x1 = bx1 - (part[0][lane + 32][c] + part[1][lane + 32][c] + part[2][lane + 32][c] + part[3][lane + 32][c]);
-    for (int s = 0; s < rb; ++s) {
-      const int i = FORWARD ? s : rb - 1 - s;
-      const int li = i & 31;
-      const bool hi = i >= 32;
-      if (!FORWARD && lane == li) {
-        if (hi) x1 = x1 / Ds[i][i];
-        else x0 = x0 / Ds[i][i];
-      }
-      const T xi = __shfl_sync(0xffffffffu, hi ? x1 : x0, li);
-      if (FORWARD) {
-        if (lane > i) x0 = fma(-Ds[lane][i], xi, x0);
-        if (lane + 32 > i) x1 = fma(-Ds[lane + 32][i], xi, x1);
-      } else {
-        if (lane < i) x0 = fma(-Ds[lane][i], xi, x0);
-        if (lane + 32 < i) x1 = fma(-Ds[lane + 32][i], xi, x1);
-      }
+      v1 = bx1 - (part[0][lane + 32][c] + part[1][lane + 32][c] + part[2][lane + 32][c] + part[3][lane + 32][c]);
+    vs[c][lane] = v0;
+    vs[c][lane + 32] = v1;
+    __syncwarp();
+    T x0 = (T)0, x1 = (T)0;
+#pragma unroll 16
+    for (int i = 0; i < KB; ++i) {
+      const T vi = vs[c][i];
+      x0 = fma(Ds[lane][i], vi, x0);
+      x1 = fma(Ds[lane + 32][i], vi, x1);
     }
     // publish: tagged words for the consumers, plain values for the result
     const unsigned long long t0 = ((unsigned long long)tag << 32) | __float_as_uint(x0);
@@ -830,17 +827,17 @@ trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long
 // from every earlier one).
 template <typename T, bool FORWARD>
 inline cudaError_t trsv_chain(const T* A, long long lda, int n, T* X, long long ldx, int nrhs,
-                              int* sync, int epoch, int* status, cudaStream_t s) {
+                              const T* Dinv, int* sync, int epoch, int* status, cudaStream_t s) {
   if (n <= 0 || nrhs <= 0) return cudaSuccess;
   const int nblk = (n + 63) / 64;
   SL_TRY(cudaMemsetAsync(sync, 0, sizeof(int), s));
   unsigned long long* xt = reinterpret_cast<unsigned long long*>(sync + 16);
   if (nrhs <= 1)
-    trsv_chain_kernel<T, FORWARD, 1><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, sync, xt, epoch, status);
+    trsv_chain_kernel<T, FORWARD, 1><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, sync, xt, epoch, status);
   else if (nrhs <= 4)
-    trsv_chain_kernel<T, FORWARD, 4><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, sync, xt, epoch, status);
+    trsv_chain_kernel<T, FORWARD, 4><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, sync, xt, epoch, status);
   else
-    trsv_chain_kernel<T, FORWARD, 8><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, sync, xt, epoch, status);
+    trsv_chain_kernel<T, FORWARD, 8><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, sync, xt, epoch, status);
   count_launches(1);
   return cudaGetLastError();
 }

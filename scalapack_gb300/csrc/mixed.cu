@@ -313,16 +313,63 @@ cudaError_t sgetrf_mixed_device(int n, float* F, long long ldf, int* dipiv, int 
   return cudaGetLastError();
 }
 
+// Inverses of the 64x64 diagonal blocks of the FP32 factors for the chained
+// solves: block b of L (unit lower, LOWER) or U (non-unit upper) is inverted
+// column by column (thread t solves T x = e_t by substitution, accumulating in
+// FP64) and stored row-major at Dinv[b*64*64 + r*64 + i]; a partial last block
+// is padded with the identity.
+template <bool LOWER>
+__global__ void __launch_bounds__(64)
+diag_inv_kernel(int n, const float* __restrict__ F, long long ldf, float* Dinv) {
+  constexpr int KB = 64;
+  __shared__ float T[KB][KB];   // read as broadcasts: no padding needed
+  __shared__ double X[KB][KB];  // X[i][t]: column t of the inverse (thread t's own column)
+  const int b = blockIdx.x, t = threadIdx.x;
+  const int r0 = b * KB, rb = min(KB, n - r0);
+  for (int r = 0; r < KB; ++r) {
+    const int i = t;
+    const bool in = r < rb && i < rb && (LOWER ? i < r : i >= r);
+    T[r][i] = in ? F[(r0 + r) + (long long)(r0 + i) * ldf] : (r == i ? 1.0f : 0.0f);
+  }
+  __syncthreads();
+  if (LOWER) {
+    for (int i = 0; i < KB; ++i) {
+      double acc = (i == t) ? 1.0 : 0.0;
+      for (int j = t; j < i; ++j) acc -= (double)T[i][j] * X[j][t];
+      X[i][t] = (i < t) ? 0.0 : acc;
+    }
+  } else {
+    for (int i = KB - 1; i >= 0; --i) {
+      double acc = (i == t) ? 1.0 : 0.0;
+      for (int j = i + 1; j <= t; ++j) acc -= (double)T[i][j] * X[j][t];
+      X[i][t] = (i > t) ? 0.0 : acc / (double)T[i][i];
+    }
+  }
+  __syncthreads();
+  float* D = Dinv + (size_t)b * KB * KB;
+  for (int r = 0; r < KB; ++r) D[r * KB + t] = (float)X[r][t];
+}
+
+cudaError_t diag_inverses(int n, const float* F, long long ldf, float* dinv, cudaStream_t s) {
+  const int nblk = (n + 63) / 64;
+  diag_inv_kernel<true><<<nblk, 64, 0, s>>>(n, F, ldf, dinv);
+  diag_inv_kernel<false><<<nblk, 64, 0, s>>>(n, F, ldf, dinv + (size_t)nblk * 64 * 64);
+  count_launches(2);
+  return cudaGetLastError();
+}
+
 // Solve with the FP32 factors: Xf (n x nrhs, ld n) overwritten in place.
 // Up to 8 right-hand sides use the single-launch chained solves.
 static cudaError_t sgetrs_inplace(int n, int nrhs, const float* F, long long ldf, const int* perm,
                                   float* Xf, float* tmp, const MixedWork& mw, cudaStream_t s) {
   SL_TRY((permute_rows<float, float>(Xf, n, tmp, n, perm, n, nrhs, 0, s)));
-  if (nrhs <= 8 && mw.chain && mw.epoch) {
+  if (nrhs <= 8 && mw.chain && mw.epoch && mw.dinv) {
+    const size_t half = (size_t)((n + 63) / 64) * 64 * 64;
     *mw.epoch += 1;
-    SL_TRY((trsv_chain<float, true>(F, ldf, n, tmp, n, nrhs, mw.chain, *mw.epoch, mw.status, s)));
+    SL_TRY((trsv_chain<float, true>(F, ldf, n, tmp, n, nrhs, mw.dinv, mw.chain, *mw.epoch, mw.status, s)));
     *mw.epoch += 1;
-    SL_TRY((trsv_chain<float, false>(F, ldf, n, tmp, n, nrhs, mw.chain, *mw.epoch, mw.status, s)));
+    SL_TRY((trsv_chain<float, false>(F, ldf, n, tmp, n, nrhs, mw.dinv + half, mw.chain, *mw.epoch,
+                                     mw.status, s)));
   } else {
     SL_TRY(tri_solve<float>(true, false, true, n, nrhs, F, ldf, tmp, n, s));
     SL_TRY(tri_solve<float>(false, false, false, n, nrhs, F, ldf, tmp, n, s));
@@ -487,6 +534,7 @@ cudaError_t dgesv_ir_device(int n, int nrhs, double* dA, long long lda, const do
   count_launches(1);
   SL_TRY(sgetrf_mixed_device(n, mw.F, mw.ldf, dipiv, opt.nb, opt.fmt, ws, mw, s));
   SL_TRY(perm_compose(dipiv, n, mw.perm, s));
+  if (mw.dinv) SL_TRY(diag_inverses(n, mw.F, mw.ldf, mw.dinv, s));
   int hstat[2] = {0, 0};
   SL_TRY(cudaMemcpyAsync(hstat, ws.status, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
   SL_TRY(cudaStreamSynchronize(s));
