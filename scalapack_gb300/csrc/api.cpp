@@ -645,8 +645,9 @@ int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, 
     sl::splitk_scratch().bytes = g_dev.capSplitk * sizeof(double);
   }
   {
-    // ticket (64 bytes) + n x 8 tagged 8-byte words of the chained solves
-    const size_t need = 16 + (size_t)n * 8 * 2;
+    // ticket (64 bytes) + n x 8 values of the chained solves, each up to two
+    // tagged 8-byte words (FP64 vectors)
+    const size_t need = 16 + (size_t)n * 8 * 2 * 2;
     if (need > g_dev.capChain || !g_dev.dchain) {
       GROW(dchain, capChain, need);
       if (e == cudaSuccess) e = cudaMemsetAsync(g_dev.dchain, 0, sizeof(int) * g_dev.capChain, s);

@@ -650,20 +650,52 @@ trsv_warp_kernel(int w, int ncols, const T* __restrict__ Tm, long long ldt, T* B
 // and when the predecessor's x arrives only two 64x64 products from shared
 // memory remain on the chain (no serial substitution). Waits are bounded
 // (kSpinLimit); on timeout the CTA records kFlagTimeout in *status and stops.
-template <typename T, bool FORWARD, int NRM>
+// TM: storage of the factor and of the diagonal-block inverses (FP32). TV:
+// the arithmetic and the vectors: FP32, or FP64 for a preconditioner applied
+// in the working precision (the FP32 factors and inverses then define the
+// operator exactly and only FP64 rounding enters). An FP64 value travels as
+// two tagged words (low and high halves).
+template <typename TM, typename TV, bool FORWARD, int NRM>
 __global__ void __launch_bounds__(256)
-trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long ldx, int nrhs,
-                  const T* __restrict__ Dinv, int* ticket, unsigned long long* xt, int epoch,
+trsv_chain_kernel(const TM* __restrict__ A, long long lda, int n, TV* X, long long ldx, int nrhs,
+                  const TM* __restrict__ Dinv, int* ticket, unsigned long long* xt, int epoch,
                   int* status) {
-  static_assert(sizeof(T) == 4, "tagged words carry 32-bit values");
+  static_assert(sizeof(TM) == 4, "FP32 factors");
+  constexpr int VW = sizeof(TV) / 4;  // tagged words per value
   constexpr int KB = 64;
   constexpr int kChunk = NRM > 4 ? 1 : (NRM > 1 ? 4 : 8);  // static shared memory under 48 KB
-  __shared__ T Ds[KB][KB + 1];          // inverse of the diagonal block, Ds[r][i]
-  __shared__ T Ls[KB][KB + 1];          // predecessor block, Ls[r][i] = A(r0+r, kp*KB+i)
-  __shared__ T xs[kChunk * KB][NRM];    // x of the blocks being applied
-  __shared__ T part[4][KB][NRM];        // partial sums of the 4 column groups
+  __shared__ TM Ds[KB][KB + 1];         // inverse of the diagonal block, Ds[r][i]
+  __shared__ TM Ls[KB][KB + 1];         // predecessor block, Ls[r][i] = A(r0+r, kp*KB+i)
+  __shared__ TV xs[kChunk * KB][NRM];   // x of the blocks being applied
+  __shared__ TV part[4][KB][NRM];       // partial sums of the 4 column groups
   __shared__ int s_b, s_fail, s_bad[kChunk];
   const uint32_t tag = (uint32_t)epoch;
+  auto word = [&](int c, long long row) { return xt + ((size_t)c * n + row) * VW; };
+  // reads one published value; false while its tag(s) are not the current one
+  auto read_val = [&](const unsigned long long* p, TV& v) -> bool {
+    if constexpr (VW == 1) {
+      unsigned long long wd;
+      asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(wd) : "l"(p) : "memory");
+      v = __uint_as_float((uint32_t)wd);
+      return (uint32_t)(wd >> 32) == tag;
+    } else {
+      unsigned long long lo, hi;
+      asm volatile("ld.relaxed.gpu.global.v2.b64 {%0, %1}, [%2];" : "=l"(lo), "=l"(hi) : "l"(p) : "memory");
+      v = __longlong_as_double((long long)(((unsigned long long)(uint32_t)hi << 32) | (uint32_t)lo));
+      return (uint32_t)(lo >> 32) == tag && (uint32_t)(hi >> 32) == tag;
+    }
+  };
+  auto publish = [&](unsigned long long* p, TV v) {
+    if constexpr (VW == 1) {
+      const unsigned long long wd = ((unsigned long long)tag << 32) | __float_as_uint(v);
+      asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(wd) : "memory");
+    } else {
+      const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+      const unsigned long long lo = ((unsigned long long)tag << 32) | (uint32_t)bits;
+      const unsigned long long hi = ((unsigned long long)tag << 32) | (uint32_t)(bits >> 32);
+      asm volatile("st.relaxed.gpu.global.v2.b64 [%0], {%1, %2};" ::"l"(p), "l"(lo), "l"(hi) : "memory");
+    }
+  };
   const int tid = threadIdx.x;
   const int nblk = (n + KB - 1) / KB;
   if (tid == 0) { s_b = atomicAdd(ticket, 1); s_fail = 0; }
@@ -674,24 +706,24 @@ trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long
   const int r0 = b * KB, rb = min(KB, n - r0);
   const int kp = FORWARD ? b - 1 : b + 1;  // predecessor in solve order
   const int wp = (sidx > 0) ? min(KB, n - kp * KB) : 0;
-  const T* Db = Dinv + (size_t)b * KB * KB;  // row-major [KB][KB]
+  const TM* Db = Dinv + (size_t)b * KB * KB;  // row-major [KB][KB]
   for (int idx = tid; idx < KB * KB; idx += 256) {
     int r = idx % KB, i = idx / KB;
-    Ls[r][i] = (r < rb && i < wp) ? A[(r0 + r) + (long long)(kp * KB + i) * lda] : (T)0;
+    Ls[r][i] = (r < rb && i < wp) ? A[(r0 + r) + (long long)(kp * KB + i) * lda] : (TM)0;
     Ds[idx / KB][idx % KB] = Db[idx];
   }
   const int r = tid & (KB - 1), q = tid >> 6;
   const int warp = tid >> 5, lane = tid & 31;
   // the block's right-hand side, read now rather than on the chain (warp c
   // owns column c; only this CTA writes these rows)
-  T bx0 = (T)0, bx1 = (T)0;
+  TV bx0 = (TV)0, bx1 = (TV)0;
   if (warp < nrhs) {
     if (lane < rb) bx0 = X[(r0 + lane) + (long long)warp * ldx];
     if (lane + 32 < rb) bx1 = X[(r0 + lane + 32) + (long long)warp * ldx];
   }
-  T acc[NRM];
+  TV acc[NRM];
 #pragma unroll
-  for (int c = 0; c < NRM; ++c) acc[c] = (T)0;
+  for (int c = 0; c < NRM; ++c) acc[c] = (TV)0;
   // Blocks 0 .. sidx-2 in solve order: chunks of the consecutive solved blocks
   // that are already published (at least the first one, waited for).
   int t = 0;
@@ -702,14 +734,13 @@ trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long
     const int k0 = kfirst * KB;
     const int kn = min(want * KB, n - k0);
     if (tid == 0) {
-      // one thread watches the chunk's first block (its last word) before the
+      // one thread watches the chunk's first block (its last value) before the
       // whole chunk is read, so waiting CTAs do not stream through L2
       const int kb0 = FORWARD ? t : nblk - 1 - t;
-      const unsigned long long* p = xt + kb0 * KB + min(KB, n - kb0 * KB) - 1;
+      const unsigned long long* p = word(0, kb0 * KB + min(KB, n - kb0 * KB) - 1);
       for (long long sp = 0;; ++sp) {
-        unsigned long long wd;
-        asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(wd) : "l"(p) : "memory");
-        if ((uint32_t)(wd >> 32) == tag) break;
+        TV v;
+        if (read_val(p, v)) break;
         if (sp > kSpinLimit) { s_fail = 1; break; }
       }
     }
@@ -721,18 +752,17 @@ trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long
     }
     for (int idx = tid; idx < kn * nrhs; idx += 256) {
       const int i = idx % kn, c = idx / kn;
-      unsigned long long wd;
-      asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(wd) : "l"(xt + (size_t)c * n + k0 + i) : "memory");
-      xs[i][c] = __uint_as_float((uint32_t)wd);
-      if ((uint32_t)(wd >> 32) != tag) {
+      TV v;
+      if (!read_val(word(c, k0 + i), v)) {
         const int blk = i / KB;                                  // chunk block, matrix order
         s_bad[FORWARD ? blk : want - 1 - blk] = 1;               // solve order
       }
+      xs[i][c] = v;
     }
     __syncthreads();
     int av = 0;
     while (av < want && s_bad[av] == 0) ++av;
-    if (av == 0) {  // the watched word arrived before the rest of its block
+    if (av == 0) {  // the watched value arrived before the rest of its block
       if (++spins > kSpinLimit) {
         if (tid == 0) atomicExch(status, (int)kFlagTimeout);
         return;
@@ -747,7 +777,7 @@ trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long
       for (int g0 = c0 + q * 16; g0 < c1; g0 += 64) {
         const int g1 = min(g0 + 16, c1);
         for (int kk = g0; kk < g1; ++kk) {
-          const T a = A[(r0 + r) + (long long)(k0 + kk) * lda];
+          const TV a = (TV)A[(r0 + r) + (long long)(k0 + kk) * lda];
 #pragma unroll
           for (int c = 0; c < NRM; ++c)
             if (c < nrhs) acc[c] = fma(a, xs[kk][c], acc[c]);
@@ -761,14 +791,13 @@ trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long
   if (sidx > 0) {
     for (int idx = tid; idx < wp * nrhs; idx += 256) {
       const int i = idx % wp, c = idx / wp;
-      const unsigned long long* p = xt + (size_t)c * n + kp * KB + i;
-      unsigned long long wd;
+      const unsigned long long* p = word(c, kp * KB + i);
+      TV v = (TV)0;
       for (long long sp = 0;; ++sp) {
-        asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(wd) : "l"(p) : "memory");
-        if ((uint32_t)(wd >> 32) == tag) break;
+        if (read_val(p, v)) break;
         if (sp > kSpinLimit) { s_fail = 1; break; }
       }
-      xs[i][c] = __uint_as_float((uint32_t)wd);
+      xs[i][c] = v;
     }
     __syncthreads();
     if (s_fail) {
@@ -781,7 +810,7 @@ trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long
         if (kk < wp) {
 #pragma unroll
           for (int c = 0; c < NRM; ++c)
-            if (c < nrhs) acc[c] = fma(Ls[r][kk], xs[kk][c], acc[c]);
+            if (c < nrhs) acc[c] = fma((TV)Ls[r][kk], xs[kk][c], acc[c]);
         }
       }
     }
@@ -791,53 +820,53 @@ trsv_chain_kernel(const T* __restrict__ A, long long lda, int n, T* X, long long
   __syncthreads();
   // v = b - sum of the partials, then x = inv(T_bb) v from shared memory:
   // warp c owns column c, lanes own rows lane and lane+32
-  __shared__ T vs[8][KB];
+  __shared__ TV vs[NRM][KB];
   if (warp < nrhs) {
     const int c = warp;
-    T v0 = (T)0, v1 = (T)0;
+    TV v0 = (TV)0, v1 = (TV)0;
     if (lane < rb) v0 = bx0 - (part[0][lane][c] + part[1][lane][c] + part[2][lane][c] + part[3][lane][c]);
     if (lane + 32 < rb)
       v1 = bx1 - (part[0][lane + 32][c] + part[1][lane + 32][c] + part[2][lane + 32][c] + part[3][lane + 32][c]);
     vs[c][lane] = v0;
     vs[c][lane + 32] = v1;
     __syncwarp();
-    T x0 = (T)0, x1 = (T)0;
+    TV x0 = (TV)0, x1 = (TV)0;
 #pragma unroll 16
     for (int i = 0; i < KB; ++i) {
-      const T vi = vs[c][i];
-      x0 = fma(Ds[lane][i], vi, x0);
-      x1 = fma(Ds[lane + 32][i], vi, x1);
+      const TV vi = vs[c][i];
+      x0 = fma((TV)Ds[lane][i], vi, x0);
+      x1 = fma((TV)Ds[lane + 32][i], vi, x1);
     }
     // publish: tagged words for the consumers, plain values for the result
-    const unsigned long long t0 = ((unsigned long long)tag << 32) | __float_as_uint(x0);
-    const unsigned long long t1 = ((unsigned long long)tag << 32) | __float_as_uint(x1);
     if (lane < rb) {
-      asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(xt + (size_t)c * n + r0 + lane), "l"(t0) : "memory");
+      publish(word(c, r0 + lane), x0);
       X[(r0 + lane) + (long long)c * ldx] = x0;
     }
     if (lane + 32 < rb) {
-      asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(xt + (size_t)c * n + r0 + lane + 32), "l"(t1) : "memory");
+      publish(word(c, r0 + lane + 32), x1);
       X[(r0 + lane + 32) + (long long)c * ldx] = x1;
     }
   }
 }
 
 // Launch the chained solve; `sync` holds 1 ticket int (64 bytes reserved)
-// followed by n x nrhs tagged 8-byte words (zeroed once; epoch must differ
-// from every earlier one).
-template <typename T, bool FORWARD>
-inline cudaError_t trsv_chain(const T* A, long long lda, int n, T* X, long long ldx, int nrhs,
-                              const T* Dinv, int* sync, int epoch, int* status, cudaStream_t s) {
+// followed by the tagged words: n x nrhs values of 1 (FP32) or 2 (FP64) words
+// (zeroed once; epoch must differ from every earlier one).
+template <typename TM, typename TV, bool FORWARD>
+inline cudaError_t trsv_chain(const TM* A, long long lda, int n, TV* X, long long ldx, int nrhs,
+                              const TM* Dinv, int* sync, int epoch, int* status, cudaStream_t s) {
   if (n <= 0 || nrhs <= 0) return cudaSuccess;
   const int nblk = (n + 63) / 64;
   SL_TRY(cudaMemsetAsync(sync, 0, sizeof(int), s));
   unsigned long long* xt = reinterpret_cast<unsigned long long*>(sync + 16);
   if (nrhs <= 1)
-    trsv_chain_kernel<T, FORWARD, 1><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, sync, xt, epoch, status);
+    trsv_chain_kernel<TM, TV, FORWARD, 1><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, sync, xt, epoch, status);
+  else if constexpr (sizeof(TV) == 8)
+    return cudaErrorInvalidValue;  // FP64 vectors: one right-hand side (GMRES)
   else if (nrhs <= 4)
-    trsv_chain_kernel<T, FORWARD, 4><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, sync, xt, epoch, status);
+    trsv_chain_kernel<TM, TV, FORWARD, 4><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, sync, xt, epoch, status);
   else
-    trsv_chain_kernel<T, FORWARD, 8><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, sync, xt, epoch, status);
+    trsv_chain_kernel<TM, TV, FORWARD, 8><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, sync, xt, epoch, status);
   count_launches(1);
   return cudaGetLastError();
 }

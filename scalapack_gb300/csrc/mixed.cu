@@ -366,10 +366,10 @@ static cudaError_t sgetrs_inplace(int n, int nrhs, const float* F, long long ldf
   if (nrhs <= 8 && mw.chain && mw.epoch && mw.dinv) {
     const size_t half = (size_t)((n + 63) / 64) * 64 * 64;
     *mw.epoch += 1;
-    SL_TRY((trsv_chain<float, true>(F, ldf, n, tmp, n, nrhs, mw.dinv, mw.chain, *mw.epoch, mw.status, s)));
+    SL_TRY((trsv_chain<float, float, true>(F, ldf, n, tmp, n, nrhs, mw.dinv, mw.chain, *mw.epoch, mw.status, s)));
     *mw.epoch += 1;
-    SL_TRY((trsv_chain<float, false>(F, ldf, n, tmp, n, nrhs, mw.dinv + half, mw.chain, *mw.epoch,
-                                     mw.status, s)));
+    SL_TRY((trsv_chain<float, float, false>(F, ldf, n, tmp, n, nrhs, mw.dinv + half, mw.chain,
+                                            *mw.epoch, mw.status, s)));
   } else {
     SL_TRY(tri_solve<float>(true, false, true, n, nrhs, F, ldf, tmp, n, s));
     SL_TRY(tri_solve<float>(false, false, false, n, nrhs, F, ldf, tmp, n, s));
@@ -393,6 +393,26 @@ static cudaError_t precond_apply(int n, int ncols, const double* r, long long ld
   count_launches(1);
   phase_end(kPhPrecond, s, 2.0 * (double)n * n * ncols, 4.0 * (double)n * n);
   return cudaGetLastError();
+}
+
+// out = (LU)^-1 r for one column with FP64 arithmetic on the FP32 factors
+// (and their FP32 diagonal-block inverses): the preconditioner GMRES applies
+// must be a fixed operator known to working precision, which an FP32 solve of
+// a rounded right-hand side is not once kappa approaches 1/eps(FP32).
+static cudaError_t precond_apply64(int n, const double* r, double* out, const float* F,
+                                   long long ldf, const MixedWork& mw, cudaStream_t s) {
+  if (!(mw.chain && mw.epoch && mw.dinv)) return precond_apply(n, 1, r, n, 0.0, out, n, F, ldf, mw, s);
+  phase_begin(kPhPrecond, s);
+  SL_TRY((permute_rows<double, double>(r, n, out, n, mw.perm, n, 1, 0, s)));
+  const size_t half = (size_t)((n + 63) / 64) * 64 * 64;
+  *mw.epoch += 1;
+  SL_TRY((trsv_chain<float, double, true>(F, ldf, n, out, n, 1, mw.dinv, mw.chain, *mw.epoch,
+                                          mw.status, s)));
+  *mw.epoch += 1;
+  SL_TRY((trsv_chain<float, double, false>(F, ldf, n, out, n, 1, mw.dinv + half, mw.chain,
+                                           *mw.epoch, mw.status, s)));
+  phase_end(kPhPrecond, s, 2.0 * (double)n * n, 4.0 * (double)n * n);
+  return cudaSuccess;
 }
 
 // R = B - A X (FP64) for ncols columns.
@@ -435,7 +455,7 @@ static cudaError_t gmres_column(int n, const double* A, long long lda, const dou
   std::vector<double> hcol(mmax + 2);
   *its = 0;
   // v0 = M^-1 r / beta
-  SL_TRY(precond_apply(n, 1, r, n, 0.0, w, n, F, ldf, mw, s));
+  SL_TRY(precond_apply64(n, r, w, F, ldf, mw, s));
   dots_kernel<<<1, 1024, 0, s>>>(w, n, n, 1, w, mw.h);
   count_launches(1);
   double beta2 = 0.0;
@@ -455,7 +475,7 @@ static cudaError_t gmres_column(int n, const double* A, long long lda, const dou
     SL_TRY(cudaMemsetAsync(mw.Ax, 0, sizeof(double) * n, s));
     SL_TRY(gemm_update<double>(false, n, 1, n, 1.0, A, lda, V + (long long)k * ldv, ldv, mw.Ax, n, s));
     phase_end(kPhResidual, s, 2.0 * (double)n * n, 8.0 * (double)n * n);
-    SL_TRY(precond_apply(n, 1, mw.Ax, n, 0.0, w, n, F, ldf, mw, s));
+    SL_TRY(precond_apply64(n, mw.Ax, w, F, ldf, mw, s));
     // classical Gram-Schmidt, twice
     std::fill(hcol.begin(), hcol.end(), 0.0);
     for (int pass = 0; pass < 2; ++pass) {

@@ -142,7 +142,7 @@ struct MixedWork {
   double* h = nullptr;         // gmres_m + 8
   double* Acopy = nullptr;     // optional FP64 copy of A for the fallback (keeps A)
   long long ldacopy = 0;
-  int* chain = nullptr;        // chained solves: ticket (16 ints) + n x 8 tagged words
+  int* chain = nullptr;        // chained solves: ticket (16 ints) + n x 8 x 2 tagged words
   float* dinv = nullptr;       // inverses of the 64x64 diagonal blocks of L then U (2 x ceil(n/64) x 4096)
   int* epoch = nullptr;        // host-side counter of chained-solve epochs
   int* status = nullptr;       // device status word
