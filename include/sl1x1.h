@@ -275,6 +275,23 @@ void sl1x1_set_panel_rows(int rows);
  * (two CTAs per SM, one's epilogue overlapping the other's main loop). Changes
  * only the speed, not the results. */
 void sl1x1_set_lowp_stages(int stages);
+/* Arithmetic of the FP64 factorization's trailing update (PDGEMM step of
+ * SRC/pdgetrf.f:288-290): 1 (default) = the product formed exactly on the
+ * BF16 tensor cores (tcgen05) from 7-bit integer slices of the operands (8
+ * slices, row and column power-of-two scales, diagonals d <= 6 of the slice
+ * products summed exactly as integers), accurate to a few units of 2^-53 of
+ * max|L21(i,:)| max|U12(:,j)| and independent of the summation order; 0 =
+ * FP64 DMMA (mma.sync m16n8k4). The sliced form needs device scratch of about
+ * 4 KB per row plus 4 KB per column of the matrix; where it cannot be had
+ * (sl1x1_dgetrf_noalloc) the DMMA form runs. */
+void sl1x1_set_f64_update(int mode);
+int sl1x1_get_f64_update(void);
+/* dC (m x n) += alpha * dA (m x k) * dB (k x n), FP64, column-major device
+ * arrays, through the sliced tensor-core product above (any k: passes of 256).
+ * Returns 0, -i for an illegal i-th argument, <= -10000 for a CUDA error,
+ * <= -20000 for a device timeout. */
+int sl1x1_ozgemm_dev(int m, int n, int k, double alpha, const double* dA, long long ldda,
+                     const double* dB, long long lddb, double* dC, long long lddc, void* stream);
 /* 1 if the library found a usable sm_103 device, else 0. */
 int sl1x1_device_ok(void);
 /* Version string. */

@@ -130,6 +130,11 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_set_default_nb.argtypes = [C.c_int]
     L.sl1x1_set_panel_rows.argtypes = [C.c_int]
     L.sl1x1_set_lowp_stages.argtypes = [C.c_int]
+    L.sl1x1_set_f64_update.argtypes = [C.c_int]
+    L.sl1x1_get_f64_update.restype = C.c_int
+    L.sl1x1_ozgemm_dev.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, vp, C.c_longlong, vp,
+                                   C.c_longlong, vp, C.c_longlong, vp]
+    L.sl1x1_ozgemm_dev.restype = C.c_int
     L.sl1x1_set_lookahead.argtypes = [C.c_int]
     L.sl1x1_device_ok.restype = C.c_int
     L.sl1x1_version.restype = C.c_char_p
@@ -376,6 +381,22 @@ def dgetrf_dev(m, n, a_ptr, ldda, ipiv_ptr, nb=0, stream=None) -> int:
     """sl1x1_dgetrf_dev on device pointers (e.g. torch ``.data_ptr()``)."""
     return lib().sl1x1_dgetrf_dev(m, n, C.c_void_p(a_ptr), ldda, C.c_void_p(ipiv_ptr), nb,
                                   _stream_ptr(stream))
+
+
+def set_f64_update(mode: int):
+    """Trailing-update arithmetic of the FP64 factorization: 1 = sliced BF16
+    tensor-core product (default), 0 = FP64 DMMA."""
+    lib().sl1x1_set_f64_update(int(mode))
+
+
+def get_f64_update() -> int:
+    return int(lib().sl1x1_get_f64_update())
+
+
+def ozgemm_dev(m, n, k, alpha, a_ptr, ldda, b_ptr, lddb, c_ptr, lddc, stream=None) -> int:
+    """C += alpha * A * B (FP64 device arrays) through the sliced tensor-core product."""
+    return lib().sl1x1_ozgemm_dev(m, n, k, float(alpha), C.c_void_p(a_ptr), ldda, C.c_void_p(b_ptr),
+                                  lddb, C.c_void_p(c_ptr), lddc, _stream_ptr(stream))
 
 
 def dgetrf_noalloc(m, n, a_ptr, ldda, ipiv_ptr, nb=0, stream=None) -> int:

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIBNAME = "libsl1x1gpu.so"
-SOURCES = ["api.cpp", "expert_api.cpp", "redist.cpp", "prof.cpp", "dgemm_f64.cu", "lu_f64.cu", "noalloc.cu", "mixed_gemm.cu", "mixed.cu", "batched.cu", "aux.cu", "refine.cu"]
+SOURCES = ["api.cpp", "expert_api.cpp", "redist.cpp", "prof.cpp", "dgemm_f64.cu", "lu_f64.cu", "noalloc.cu", "mixed_gemm.cu", "ozgemm_f64.cu", "mixed.cu", "batched.cu", "aux.cu", "refine.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -169,13 +169,27 @@ void release_all() {
   cudaFree(g_dev.dw); cudaFree(g_dev.dAx); cudaFree(g_dev.dh); cudaFree(g_dev.dAcopy);
   cudaFree(g_dev.dchain); cudaFree(g_dev.dsplitk); cudaFree(g_dev.daux); cudaFree(g_dev.ddinv);
   cudaFree(g_dev.dA2); cudaFree(g_dev.dX); cudaFree(g_dev.drw); cudaFree(g_dev.drc);
-  cudaFree(g_dev.dipiv2);
+  cudaFree(g_dev.dipiv2); cudaFree(g_dev.doz);
   sl::splitk_scratch() = sl::SplitKScratch();
+  sl::oz_scratch() = sl::OzScratch();
   if (g_dev.stream) cudaStreamDestroy(g_dev.stream);
   if (g_dev.aux) cudaStreamDestroy(g_dev.aux);
   if (g_dev.ev_next) cudaEventDestroy(g_dev.ev_next);
   if (g_dev.ev_panel) cudaEventDestroy(g_dev.ev_panel);
   g_dev = DevState();
+}
+
+void ensure_oz(int m, int n, int nb) {
+  if (sl::f64_update_get() != 1 || m <= 0 || n <= 0) return;
+  const size_t need = sl::oz_scratch_bytes(m, n, nb > 0 ? nb : g_default_nb);
+  if (need <= g_dev.capOz && g_dev.doz) return;
+  if (grow(&g_dev.doz, &g_dev.capOz, need) == cudaSuccess) {
+    sl::oz_scratch().ptr = g_dev.doz;
+    sl::oz_scratch().bytes = g_dev.capOz;
+  } else {
+    cudaGetLastError();
+    sl::oz_scratch() = sl::OzScratch();
+  }
 }
 
 sl::LuWork make_work() {
@@ -232,6 +246,7 @@ int factor_host(int m, int n, double* A, int ia, int ja, const int* desca, int* 
   e = cudaMemcpy2DAsync(g_dev.dA, ldda * sizeof(double), src, lld * sizeof(double),
                         (size_t)m * sizeof(double), n, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_info(e);
+  ensure_oz(m, n, desca[NB_]);
   sl::LuWork w = make_work();
   e = sl::dgetrf_device(m, n, g_dev.dA, ldda, g_dev.dipiv, desca[NB_], w, s);
   if (e == cudaErrorInvalidValue) return -30000;
@@ -522,6 +537,7 @@ int sl1x1_dgetrf_dev(int m, int n, double* dA, long long ldda, int* dipiv, int n
   if (!ensure_device()) return cuda_info(cudaErrorNoDevice);
   cudaStream_t s = (cudaStream_t)stream;
   if (nb <= 0) nb = g_default_nb;
+  ensure_oz(m, n, nb);
   sl::LuWork w = make_work();
   cudaError_t e = sl::dgetrf_device(m, n, dA, ldda, dipiv, nb, w, s);
   if (e == cudaErrorInvalidValue) return -30000;
@@ -616,6 +632,7 @@ int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, 
   opt.nb = nb > 0 ? nb : 256;
   opt.nb_fp64 = g_default_nb;
   if (tol > 0) opt.tol = tol;
+  ensure_oz(n, n, opt.nb_fp64);  // the FP64 fallback factorization
   const long long ldf = round_ld(n);
   const int kpad = sl::lowp_kpad(opt.nb) * sl::lowp_kmult(fmt);
   const size_t m1 = (size_t)opt.gmres_m + 1;
@@ -639,7 +656,7 @@ int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, 
   GROW(dbswap, capBs, (size_t)n * nrhs);
   if (keep_a) GROW(dAcopy, capAcopy, (size_t)ldf * n);
   GROW(dsplitk, capSplitk, (size_t)32 * 4 * n);  // split-K partials of the FP64 products
-  GROW(ddinv, capDinv, (size_t)2 * ((n + 63) / 64) * 64 * 64);  // diagonal-block inverses
+  GROW(ddinv, capDinv, (size_t)4 * ((n + 63) / 64) * 64 * 64);  // diagonal-block inverses and M_b
   if (e == cudaSuccess) {
     sl::splitk_scratch().ptr = g_dev.dsplitk;
     sl::splitk_scratch().bytes = g_dev.capSplitk * sizeof(double);
@@ -958,6 +975,45 @@ void sl1x1_set_panel_rows(int rows) {
 void sl1x1_set_lowp_stages(int stages) {
   std::lock_guard<std::mutex> lk(g_mu);
   sl::lowp_set_stages(stages);
+}
+
+void sl1x1_set_f64_update(int mode) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  sl::f64_update_set(mode);
+}
+
+int sl1x1_get_f64_update(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return sl::f64_update_get();
+}
+
+int sl1x1_ozgemm_dev(int m, int n, int k, double alpha, const double* dA, long long ldda,
+                     const double* dB, long long lddb, double* dC, long long lddc, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (k < 0) return -3;
+  if (ldda < (m > 1 ? m : 1)) return -6;
+  if (lddb < (k > 1 ? k : 1)) return -8;
+  if (lddc < (m > 1 ? m : 1)) return -10;
+  if (m == 0 || n == 0 || k == 0) return 0;
+  if (!ensure_device()) return cuda_info(cudaErrorNoDevice);
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t need = sl::oz_scratch_bytes(m, n, k);
+  if (need > g_dev.capOz || !g_dev.doz) {
+    cudaError_t e = grow(&g_dev.doz, &g_dev.capOz, need);
+    if (e != cudaSuccess) return cuda_info(e);
+    sl::oz_scratch().ptr = g_dev.doz;
+    sl::oz_scratch().bytes = g_dev.capOz;
+  }
+  cudaError_t e = cudaMemsetAsync(g_dev.dsmall + 2, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = sl::oz_dgemm(m, n, k, alpha, dA, ldda, dB, lddb, dC, lddc, g_dev.dsmall + 2, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_info(e);
+  int st = 0;
+  e = cudaMemcpy(&st, g_dev.dsmall + 2, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_info(e);
+  return st ? -20000 - st : 0;
 }
 
 void sl1x1_set_default_nb(int nb) {

@@ -459,6 +459,7 @@ void pdgesvx_(const char* FACT, const char* TRANS, const int* N, const int* NRHS
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
       if (e != cudaSuccess) return fail(e);
     } else {
+      ensure_oz(n, n, DESCAF[NB_]);
       e = sl::dgetrf_device(n, n, g_dev.dA, st.ldd, g_dev.dipiv, DESCAF[NB_], w, s);
       if (e == cudaErrorInvalidValue) { *INFO = -30000; return; }
       if (e != cudaSuccess) return fail(e);

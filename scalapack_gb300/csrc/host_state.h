@@ -52,6 +52,7 @@ struct DevState {
   float* ddinv = nullptr; size_t capDinv = 0;
   double* dsplitk = nullptr; size_t capSplitk = 0;
   double* daux = nullptr; size_t capAux = 0;
+  unsigned char* doz = nullptr; size_t capOz = 0;  // sliced FP64 update scratch (bytes)
   int chain_epoch = 0;
   unsigned short* dA16 = nullptr; size_t capA16 = 0;
   unsigned short* dB16 = nullptr; size_t capB16 = 0;
@@ -67,6 +68,10 @@ struct DevState {
 extern DevState g_dev;
 extern int g_default_nb;
 extern bool g_lookahead;
+
+// Grows the sliced-update scratch for an m x n factorization with block nb
+// (failure leaves the DMMA update in use).
+void ensure_oz(int m, int n, int nb);
 
 // Grid query (1x1 only; any other grid reads as NPROW = -1).
 void gridinfo(int ictxt, int* nprow, int* npcol, int* myrow, int* mycol);

@@ -127,6 +127,21 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
   return cudaSuccess;
 }
 
+static int g_f64_update = 1;
+
+void f64_update_set(int mode) { g_f64_update = (mode == 0) ? 0 : 1; }
+int f64_update_get() { return g_f64_update; }
+
+// A22 -= L21 * U12 (m x n, k = the panel width): the sliced tensor-core
+// product when selected and its scratch fits, else FP64 DMMA.
+static cudaError_t trailing_update(int m, int n, int k, const double* L21, long long ldl,
+                            const double* U12, long long ldu, double* C, long long ldc,
+                            const LuWork& ws, cudaStream_t s) {
+  if (g_f64_update == 1 && oz_fits(m, n, k))
+    return oz_dgemm(m, n, k, -1.0, L21, ldl, U12, ldu, C, ldc, ws.status, s);
+  return dgemm(false, m, n, k, -1.0, L21, ldl, U12, ldu, 1.0, C, ldc, s);
+}
+
 // Right-looking blocked LU. With look-ahead resources in `ws`, the panel of
 // step j+1 is factored on ws.aux while the trailing update of step j runs on
 // s: the columns of the next panel are updated first (event ev_next), the
@@ -165,8 +180,8 @@ cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, 
         if (lookahead && jb2 > 0) {
           // next panel's columns first, then the panel on the look-ahead stream
           phase_begin(kPhGemm, s);
-          SL_TRY(dgemm(false, m - jn, jb2, jb, -1.0, Ap(jn, j), ldda, Ap(j, jn), ldda, 1.0,
-                       Ap(jn, jn), ldda, s));
+          SL_TRY(trailing_update(m - jn, jb2, jb, Ap(jn, j), ldda, Ap(j, jn), ldda, Ap(jn, jn),
+                                 ldda, ws, s));
           phase_end(kPhGemm, s, 2.0 * mr * jb2 * jb, 8.0 * (mr * jb + (double)jb * jb2 + 2.0 * mr * jb2));
           SL_TRY(cudaEventRecord(ws.ev_next, s));
           SL_TRY(cudaStreamWaitEvent(ws.aux, ws.ev_next, 0));
@@ -176,14 +191,14 @@ cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, 
           const int rest = n - jn - jb2;
           if (rest > 0) {
             phase_begin(kPhGemm, s);
-            SL_TRY(dgemm(false, m - jn, rest, jb, -1.0, Ap(jn, j), ldda, Ap(j, jn + jb2), ldda, 1.0,
-                         Ap(jn, jn + jb2), ldda, s));
+            SL_TRY(trailing_update(m - jn, rest, jb, Ap(jn, j), ldda, Ap(j, jn + jb2), ldda,
+                                   Ap(jn, jn + jb2), ldda, ws, s));
             phase_end(kPhGemm, s, 2.0 * mr * rest * jb, 8.0 * (mr * jb + (double)jb * rest + 2.0 * mr * rest));
           }
         } else {
           phase_begin(kPhGemm, s);
-          SL_TRY(dgemm(false, m - jn, n - jn, jb, -1.0, Ap(jn, j), ldda, Ap(j, jn), ldda, 1.0,
-                       Ap(jn, jn), ldda, s));
+          SL_TRY(trailing_update(m - jn, n - jn, jb, Ap(jn, j), ldda, Ap(j, jn), ldda, Ap(jn, jn),
+                                 ldda, ws, s));
           phase_end(kPhGemm, s, 2.0 * mr * nr * jb, 8.0 * (mr * jb + jb * nr + 2.0 * mr * nr));
         }
       }

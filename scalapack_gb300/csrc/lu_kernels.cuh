@@ -644,11 +644,12 @@ trsv_warp_kernel(int w, int ncols, const T* __restrict__ Tm, long long ldt, T* B
 // blocks are published as tagged words {x bits, epoch} in xt, so a consumer
 // polls the values themselves (one round trip, no flag and no fence). A CTA
 // stages the inverse of its diagonal block (precomputed once per factorization,
-// diag_inv) and the off-diagonal block of its immediate predecessor in shared
-// memory, consumes the earlier solved blocks in chunks as they appear (4
-// thread groups of 64 rows x 16 columns apply the 64x64 blocks of the factor),
-// and when the predecessor's x arrives only two 64x64 products from shared
-// memory remain on the chain (no serial substitution). Waits are bounded
+// diag_inv) and M_b = inv(T_bb) T_bp for its immediate predecessor p in
+// shared memory, consumes the earlier solved blocks in chunks as they appear
+// (4 thread groups of 64 rows x 16 columns apply the 64x64 blocks of the
+// factor), forms y_b = inv(T_bb) v_b before the predecessor is solved, and
+// when x_p arrives one 64x64 product from shared memory remains on the chain,
+// x_b = y_b - M_b x_p (no serial substitution). Waits are bounded
 // (kSpinLimit); on timeout the CTA records kFlagTimeout in *status and stops.
 // TM: storage of the factor and of the diagonal-block inverses (FP32). TV:
 // the arithmetic and the vectors: FP32, or FP64 for a preconditioner applied
@@ -658,14 +659,14 @@ trsv_warp_kernel(int w, int ncols, const T* __restrict__ Tm, long long ldt, T* B
 template <typename TM, typename TV, bool FORWARD, int NRM>
 __global__ void __launch_bounds__(256)
 trsv_chain_kernel(const TM* __restrict__ A, long long lda, int n, TV* X, long long ldx, int nrhs,
-                  const TM* __restrict__ Dinv, int* ticket, unsigned long long* xt, int epoch,
-                  int* status) {
+                  const TM* __restrict__ Dinv, const TM* __restrict__ Mp, int* ticket,
+                  unsigned long long* xt, int epoch, int* status) {
   static_assert(sizeof(TM) == 4, "FP32 factors");
   constexpr int VW = sizeof(TV) / 4;  // tagged words per value
   constexpr int KB = 64;
   constexpr int kChunk = NRM > 4 ? 1 : (NRM > 1 ? 4 : 8);  // static shared memory under 48 KB
   __shared__ TM Ds[KB][KB + 1];         // inverse of the diagonal block, Ds[r][i]
-  __shared__ TM Ls[KB][KB + 1];         // predecessor block, Ls[r][i] = A(r0+r, kp*KB+i)
+  __shared__ TM Ms[KB][KB + 1];         // M_b = inv(T_bb) T_bp, Ms[r][i]
   __shared__ TV xs[kChunk * KB][NRM];   // x of the blocks being applied
   __shared__ TV part[4][KB][NRM];       // partial sums of the 4 column groups
   __shared__ int s_b, s_fail, s_bad[kChunk];
@@ -707,10 +708,10 @@ trsv_chain_kernel(const TM* __restrict__ A, long long lda, int n, TV* X, long lo
   const int kp = FORWARD ? b - 1 : b + 1;  // predecessor in solve order
   const int wp = (sidx > 0) ? min(KB, n - kp * KB) : 0;
   const TM* Db = Dinv + (size_t)b * KB * KB;  // row-major [KB][KB]
+  const TM* Mb = Mp + (size_t)b * KB * KB;
   for (int idx = tid; idx < KB * KB; idx += 256) {
-    int r = idx % KB, i = idx / KB;
-    Ls[r][i] = (r < rb && i < wp) ? A[(r0 + r) + (long long)(kp * KB + i) * lda] : (TM)0;
     Ds[idx / KB][idx % KB] = Db[idx];
+    Ms[idx / KB][idx % KB] = (sidx > 0) ? Mb[idx] : (TM)0;
   }
   const int r = tid & (KB - 1), q = tid >> 6;
   const int warp = tid >> 5, lane = tid & 31;
@@ -787,7 +788,43 @@ trsv_chain_kernel(const TM* __restrict__ A, long long lda, int n, TV* X, long lo
     __syncthreads();
     t += av;
   }
-  // The predecessor: poll its x (the chain's one round trip), apply Ls.
+#pragma unroll
+  for (int c = 0; c < NRM; ++c) part[q][r][c] = acc[c];
+  __syncthreads();
+  // v = b - sum of the partials (warp c owns column c, lanes rows lane and
+  // lane+32), then y = inv(T_bb) v by all four thread groups
+  __shared__ TV vs[NRM][KB];
+  if (warp < nrhs) {
+    const int c = warp;
+    TV v0 = (TV)0, v1 = (TV)0;
+    if (lane < rb) v0 = bx0 - (part[0][lane][c] + part[1][lane][c] + part[2][lane][c] + part[3][lane][c]);
+    if (lane + 32 < rb)
+      v1 = bx1 - (part[0][lane + 32][c] + part[1][lane + 32][c] + part[2][lane + 32][c] + part[3][lane + 32][c]);
+    vs[c][lane] = v0;
+    vs[c][lane + 32] = v1;
+  }
+  __syncthreads();
+  {
+#pragma unroll
+    for (int c = 0; c < NRM; ++c) acc[c] = (TV)0;
+#pragma unroll
+    for (int i = q * 16; i < q * 16 + 16; ++i) {
+      const TV d = (TV)Ds[r][i];
+#pragma unroll
+      for (int c = 0; c < NRM; ++c)
+        if (c < nrhs) acc[c] = fma(d, vs[c][i], acc[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < NRM; ++c) part[q][r][c] = acc[c];
+  }
+  __syncthreads();
+  TV x0 = (TV)0, x1 = (TV)0;
+  if (warp < nrhs) {
+    const int c = warp;
+    x0 = part[0][lane][c] + part[1][lane][c] + part[2][lane][c] + part[3][lane][c];
+    x1 = part[0][lane + 32][c] + part[1][lane + 32][c] + part[2][lane + 32][c] + part[3][lane + 32][c];
+  }
+  // The predecessor: poll its x (the chain's one round trip), x -= M_b x_p.
   if (sidx > 0) {
     for (int idx = tid; idx < wp * nrhs; idx += 256) {
       const int i = idx % wp, c = idx / wp;
@@ -799,45 +836,34 @@ trsv_chain_kernel(const TM* __restrict__ A, long long lda, int n, TV* X, long lo
       }
       xs[i][c] = v;
     }
-    __syncthreads();
+    __syncthreads();  // also orders the reads of part above before the writes below
     if (s_fail) {
       if (tid == 0) atomicExch(status, (int)kFlagTimeout);
       return;
     }
-    if (r < rb) {
-#pragma unroll 4
-      for (int kk = q * 16; kk < q * 16 + 16; ++kk) {
-        if (kk < wp) {
 #pragma unroll
-          for (int c = 0; c < NRM; ++c)
-            if (c < nrhs) acc[c] = fma((TV)Ls[r][kk], xs[kk][c], acc[c]);
-        }
+    for (int c = 0; c < NRM; ++c) acc[c] = (TV)0;
+#pragma unroll 4
+    for (int kk = q * 16; kk < q * 16 + 16; ++kk) {
+      if (kk < wp) {
+        const TV m = (TV)Ms[r][kk];
+#pragma unroll
+        for (int c = 0; c < NRM; ++c)
+          if (c < nrhs) acc[c] = fma(m, xs[kk][c], acc[c]);
       }
     }
-  }
 #pragma unroll
-  for (int c = 0; c < NRM; ++c) part[q][r][c] = acc[c];
-  __syncthreads();
-  // v = b - sum of the partials, then x = inv(T_bb) v from shared memory:
-  // warp c owns column c, lanes own rows lane and lane+32
-  __shared__ TV vs[NRM][KB];
+    for (int c = 0; c < NRM; ++c) part[q][r][c] = acc[c];
+    __syncthreads();
+    if (warp < nrhs) {
+      const int c = warp;
+      x0 -= part[0][lane][c] + part[1][lane][c] + part[2][lane][c] + part[3][lane][c];
+      x1 -= part[0][lane + 32][c] + part[1][lane + 32][c] + part[2][lane + 32][c] + part[3][lane + 32][c];
+    }
+  }
+  // publish: tagged words for the consumers, plain values for the result
   if (warp < nrhs) {
     const int c = warp;
-    TV v0 = (TV)0, v1 = (TV)0;
-    if (lane < rb) v0 = bx0 - (part[0][lane][c] + part[1][lane][c] + part[2][lane][c] + part[3][lane][c]);
-    if (lane + 32 < rb)
-      v1 = bx1 - (part[0][lane + 32][c] + part[1][lane + 32][c] + part[2][lane + 32][c] + part[3][lane + 32][c]);
-    vs[c][lane] = v0;
-    vs[c][lane + 32] = v1;
-    __syncwarp();
-    TV x0 = (TV)0, x1 = (TV)0;
-#pragma unroll 16
-    for (int i = 0; i < KB; ++i) {
-      const TV vi = vs[c][i];
-      x0 = fma((TV)Ds[lane][i], vi, x0);
-      x1 = fma((TV)Ds[lane + 32][i], vi, x1);
-    }
-    // publish: tagged words for the consumers, plain values for the result
     if (lane < rb) {
       publish(word(c, r0 + lane), x0);
       X[(r0 + lane) + (long long)c * ldx] = x0;
@@ -854,19 +880,20 @@ trsv_chain_kernel(const TM* __restrict__ A, long long lda, int n, TV* X, long lo
 // (zeroed once; epoch must differ from every earlier one).
 template <typename TM, typename TV, bool FORWARD>
 inline cudaError_t trsv_chain(const TM* A, long long lda, int n, TV* X, long long ldx, int nrhs,
-                              const TM* Dinv, int* sync, int epoch, int* status, cudaStream_t s) {
+                              const TM* Dinv, const TM* Mp, int* sync, int epoch, int* status,
+                              cudaStream_t s) {
   if (n <= 0 || nrhs <= 0) return cudaSuccess;
   const int nblk = (n + 63) / 64;
   SL_TRY(cudaMemsetAsync(sync, 0, sizeof(int), s));
   unsigned long long* xt = reinterpret_cast<unsigned long long*>(sync + 16);
   if (nrhs <= 1)
-    trsv_chain_kernel<TM, TV, FORWARD, 1><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, sync, xt, epoch, status);
+    trsv_chain_kernel<TM, TV, FORWARD, 1><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, Mp, sync, xt, epoch, status);
   else if constexpr (sizeof(TV) == 8)
     return cudaErrorInvalidValue;  // FP64 vectors: one right-hand side (GMRES)
   else if (nrhs <= 4)
-    trsv_chain_kernel<TM, TV, FORWARD, 4><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, sync, xt, epoch, status);
+    trsv_chain_kernel<TM, TV, FORWARD, 4><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, Mp, sync, xt, epoch, status);
   else
-    trsv_chain_kernel<TM, TV, FORWARD, 8><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, sync, xt, epoch, status);
+    trsv_chain_kernel<TM, TV, FORWARD, 8><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, Dinv, Mp, sync, xt, epoch, status);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -317,10 +317,13 @@ cudaError_t sgetrf_mixed_device(int n, float* F, long long ldf, int* dipiv, int 
 // solves: block b of L (unit lower, LOWER) or U (non-unit upper) is inverted
 // column by column (thread t solves T x = e_t by substitution, accumulating in
 // FP64) and stored row-major at Dinv[b*64*64 + r*64 + i]; a partial last block
-// is padded with the identity.
+// is padded with the identity. Also M_b = inv(T_bb) T_bp, with p the block
+// solved just before b (b-1 for L, b+1 for U; zero for the first one), stored
+// the same way at Mp: the chained solve then finishes block b with one 64x64
+// product once x_p arrives, x_b = inv(T_bb) v_b - M_b x_p.
 template <bool LOWER>
 __global__ void __launch_bounds__(64)
-diag_inv_kernel(int n, const float* __restrict__ F, long long ldf, float* Dinv) {
+diag_inv_kernel(int n, const float* __restrict__ F, long long ldf, float* Dinv, float* Mp) {
   constexpr int KB = 64;
   __shared__ float T[KB][KB];   // read as broadcasts: no padding needed
   __shared__ double X[KB][KB];  // X[i][t]: column t of the inverse (thread t's own column)
@@ -348,12 +351,28 @@ diag_inv_kernel(int n, const float* __restrict__ F, long long ldf, float* Dinv) 
   __syncthreads();
   float* D = Dinv + (size_t)b * KB * KB;
   for (int r = 0; r < KB; ++r) D[r * KB + t] = (float)X[r][t];
+  // the predecessor block into T (its triangle is no longer needed)
+  const int nblk = (n + KB - 1) / KB;
+  const int p = LOWER ? b - 1 : b + 1;
+  const bool has_p = p >= 0 && p < nblk;
+  const int wp = has_p ? min(KB, n - p * KB) : 0;
+  for (int r = 0; r < KB; ++r)
+    T[r][t] = (r < rb && t < wp) ? F[(r0 + r) + (long long)(p * KB + t) * ldf] : 0.0f;
+  __syncthreads();
+  float* M = Mp + (size_t)b * KB * KB;
+  for (int r = 0; r < KB; ++r) {
+    double acc = 0.0;
+    for (int i = 0; i < KB; ++i) acc = fma(X[r][i], (double)T[i][t], acc);
+    M[r * KB + t] = (float)acc;
+  }
 }
 
+// dinv: [inv L blocks | inv U blocks | M of L | M of U], each ceil(n/64) x 4096.
 cudaError_t diag_inverses(int n, const float* F, long long ldf, float* dinv, cudaStream_t s) {
   const int nblk = (n + 63) / 64;
-  diag_inv_kernel<true><<<nblk, 64, 0, s>>>(n, F, ldf, dinv);
-  diag_inv_kernel<false><<<nblk, 64, 0, s>>>(n, F, ldf, dinv + (size_t)nblk * 64 * 64);
+  const size_t half = (size_t)nblk * 64 * 64;
+  diag_inv_kernel<true><<<nblk, 64, 0, s>>>(n, F, ldf, dinv, dinv + 2 * half);
+  diag_inv_kernel<false><<<nblk, 64, 0, s>>>(n, F, ldf, dinv + half, dinv + 3 * half);
   count_launches(2);
   return cudaGetLastError();
 }
@@ -366,10 +385,11 @@ static cudaError_t sgetrs_inplace(int n, int nrhs, const float* F, long long ldf
   if (nrhs <= 8 && mw.chain && mw.epoch && mw.dinv) {
     const size_t half = (size_t)((n + 63) / 64) * 64 * 64;
     *mw.epoch += 1;
-    SL_TRY((trsv_chain<float, float, true>(F, ldf, n, tmp, n, nrhs, mw.dinv, mw.chain, *mw.epoch, mw.status, s)));
+    SL_TRY((trsv_chain<float, float, true>(F, ldf, n, tmp, n, nrhs, mw.dinv, mw.dinv + 2 * half,
+                                           mw.chain, *mw.epoch, mw.status, s)));
     *mw.epoch += 1;
-    SL_TRY((trsv_chain<float, float, false>(F, ldf, n, tmp, n, nrhs, mw.dinv + half, mw.chain,
-                                            *mw.epoch, mw.status, s)));
+    SL_TRY((trsv_chain<float, float, false>(F, ldf, n, tmp, n, nrhs, mw.dinv + half,
+                                            mw.dinv + 3 * half, mw.chain, *mw.epoch, mw.status, s)));
   } else {
     SL_TRY(tri_solve<float>(true, false, true, n, nrhs, F, ldf, tmp, n, s));
     SL_TRY(tri_solve<float>(false, false, false, n, nrhs, F, ldf, tmp, n, s));
@@ -406,11 +426,11 @@ static cudaError_t precond_apply64(int n, const double* r, double* out, const fl
   SL_TRY((permute_rows<double, double>(r, n, out, n, mw.perm, n, 1, 0, s)));
   const size_t half = (size_t)((n + 63) / 64) * 64 * 64;
   *mw.epoch += 1;
-  SL_TRY((trsv_chain<float, double, true>(F, ldf, n, out, n, 1, mw.dinv, mw.chain, *mw.epoch,
-                                          mw.status, s)));
+  SL_TRY((trsv_chain<float, double, true>(F, ldf, n, out, n, 1, mw.dinv, mw.dinv + 2 * half,
+                                          mw.chain, *mw.epoch, mw.status, s)));
   *mw.epoch += 1;
-  SL_TRY((trsv_chain<float, double, false>(F, ldf, n, out, n, 1, mw.dinv + half, mw.chain,
-                                           *mw.epoch, mw.status, s)));
+  SL_TRY((trsv_chain<float, double, false>(F, ldf, n, out, n, 1, mw.dinv + half,
+                                           mw.dinv + 3 * half, mw.chain, *mw.epoch, mw.status, s)));
   phase_end(kPhPrecond, s, 2.0 * (double)n * n, 4.0 * (double)n * n);
   return cudaSuccess;
 }

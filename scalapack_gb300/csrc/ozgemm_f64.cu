@@ -1,0 +1,482 @@
+// FP64 trailing update of the plain LU on the BF16 tensor cores (the PDGEMM
+// step of SRC/pdgetrf.f:288-290, C <- C + alpha * A * B with FP64 A, B, C):
+// sm_103a's tcgen05.mma has no FP64 kind, so the product is formed exactly
+// from integer slices (the error-free splitting of Ozaki, Ogita and Oishi,
+// "Error-free transformations of matrix multiplication by using fast routines
+// of matrix multiplication and its applications", Numer. Algorithms 59, 2012).
+//
+// Splitting. Row i of A is scaled by 2^-e_i (e_i the exponent of its largest
+// magnitude, so |A(i,k)| 2^-e_i < 1) and cut into S = 8 slices of 7 bits:
+//   A(i,k) 2^-e_i = sum_{s=1..8} a_s(i,k) 2^-7s,  a_s integer, |a_s| <= 127,
+// by exact FP64 truncation; column j of B likewise with 2^-f_j and b_t. The
+// slices are stored in BF16 as a_s 2^-7(s-1) (8 significant bits hold any
+// |a_s| <= 127 and the power of two is exact), K-major, so that the product of
+// slices s and t carries its weight 2^-7(s+t-2) by itself.
+//
+// Exact products. For K <= 256, sum_k a_s b_t is an integer of magnitude at
+// most 256 * 127^2 < 2^22: up to four such products sum exactly in FP32, in
+// any order and with any alignment the tensor core uses, because every partial
+// sum is an integer multiple of the diagonal's unit below 2^24. With
+// d = s + t, the update is
+//   (A B)(i,j) = 2^(e_i + f_j) sum_d 2^-7d P_d,   P_d = sum_{s+t=d} sum_k a_s b_t.
+// Diagonals d = 2..6 each get their own TMEM accumulator (exact: d <= 5 holds
+// at most 4 products; d = 6 holds 5, exact unless their sum passes 2^24, which
+// takes nearly all 1280 terms at full magnitude with one sign); d = 7..9 share
+// a sixth accumulator in plain FP32 (its rounding, 2^-24 relative to a term
+// already 2^-49 below the row and column scales, is far below FP64 rounding);
+// d >= 10 is dropped (below 2^-56 of the scales per term). 36 slice products.
+//
+// Epilogue. P_2..P_6 are read back as exact integers, combined with the tail
+// into one 64-bit integer I = sum_d P_d 2^(52-7d) (|I| < 2^61), converted to
+// FP64 once, and C(i,j) = fma(alpha 2^(e_i+f_j-52), I, C(i,j)). The result is
+// within a few units of 2^-53 of |A(i,:)|_max |B(:,j)|_max of the exact
+// product, and independent of the accumulation order (run to run identical).
+// Rows or columns holding Inf or NaN give NaN in their row or column of C.
+//
+// Structure (one 128 x 64 tile of C per CTA, 4 warps, one CTA per SM):
+//   * warp 0 allocates all 512 TMEM columns (6 accumulators x 64 columns);
+//   * one thread issues TMA loads: for each 64-wide k block, the eight 64x64
+//     B slices into one half of a double buffer, then the eight 128x64 A
+//     slices one at a time through a 4-deep ring (128-byte swizzle);
+//   * one thread issues tcgen05.mma.kind::f16 (M=128, N=64, K=16): A slice s
+//     against B slices t <= 9 - s into accumulator min(s+t-2, 5);
+//   * all 4 warps read the accumulators with tcgen05.ld (warp w owns lanes
+//     32w..32w+31 = tile rows) and update C in place (coalesced per column).
+// Every mbarrier wait is bounded; on timeout the CTA records kFlagTimeout,
+// drains what it issued, frees its TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <climits>
+
+#include "common.cuh"
+#include "sl_internal.h"
+#include "tc_common.cuh"
+
+namespace sl {
+namespace {
+using namespace tc;
+
+constexpr int OZ_S = 8;          // slices per operand
+constexpr int OZ_BITS = 7;       // bits per slice
+constexpr int OZ_NACC = 6;       // accumulators: d = 2..6 exact, 7..9 tail
+constexpr int OZ_KMAX = 256;     // exactness bound on K per pass
+constexpr int OBM = 128, OBN = 64, OBK = 64;
+constexpr int A_SLICE_BYTES = OBM * OBK * 2;          // 16 KB
+constexpr int B_SLICE_BYTES = OBN * OBK * 2;          // 8 KB
+constexpr int B_CHUNK_BYTES = OZ_S * B_SLICE_BYTES;   // 64 KB per k block
+constexpr int A_RING = 4;
+constexpr int OZ_TMEM_COLS = 512;
+constexpr int GROUP_M = 8;       // tile raster: 8 row tiles sweep the columns together
+
+struct __align__(8) OzBars {
+  uint64_t afull[A_RING], aempty[A_RING];
+  uint64_t bfull[2], bempty[2];
+  uint64_t done;
+  uint32_t tmem_base;
+};
+
+size_t oz_smem_bytes() {
+  return 1024 + (size_t)A_RING * A_SLICE_BYTES + 2 * (size_t)B_CHUNK_BYTES + sizeof(OzBars) + 64;
+}
+
+__host__ __device__ constexpr uint32_t oz_idesc() {
+  return (1u << 4)                       // D format: F32
+         | (1u << 7) | (1u << 10)        // A, B: BF16
+         | ((uint32_t)(OBN >> 3) << 17)  // N / 8
+         | ((uint32_t)(OBM >> 4) << 24); // M / 16
+}
+
+__device__ __forceinline__ void touch16(uint32_t* r) {
+  asm volatile(""
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                 "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]));
+}
+
+__global__ void __launch_bounds__(128, 1)
+ozgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+              int m, int n, int kpad, int m_pad, int n_pad, const double* __restrict__ rs,
+              const double* __restrict__ cs, double alpha, double* C, long long ldc,
+              int* status) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* sA = base;                                   // A_RING x 16 KB
+  unsigned char* sB = base + A_RING * A_SLICE_BYTES;          // 2 x 64 KB
+  OzBars* bars = (OzBars*)(sB + 2 * B_CHUNK_BYTES);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // grouped raster over (row tile, column tile)
+  const int tiles_m = m_pad / OBM, tiles_n = n_pad / OBN;
+  const int per_group = GROUP_M * tiles_n;
+  const int gid = blockIdx.x / per_group, first_m = gid * GROUP_M;
+  const int gsize = min(tiles_m - first_m, GROUP_M);
+  const int in_group = blockIdx.x % per_group;
+  const int m0 = (first_m + in_group % gsize) * OBM;
+  const int n0 = (in_group / gsize) * OBN;
+  const int nkc = kpad / OBK;
+  __shared__ int s_fail, s_issued, s_consumed, s_bissued, s_bconsumed;
+  // a CTA that timed out already marked the launch failed: skip the work
+  if (*(volatile int*)status != 0) return;
+
+  if (threadIdx.x == 0) {
+    s_fail = 0;
+    s_issued = 0;
+    s_consumed = 0;
+    s_bissued = 0;
+    s_bconsumed = 0;
+    for (int i = 0; i < A_RING; ++i) {
+      mbar_init(&bars->afull[i], 1);
+      mbar_init(&bars->aempty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&bars->bfull[i], 1);
+      mbar_init(&bars->bempty[i], 1);
+    }
+    mbar_init(&bars->done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&bars->tmem_base)),
+                 "r"(OZ_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = bars->tmem_base;
+
+  if (warp == 0 && lane == 0) {
+    // TMA producer. s_issued / s_bissued count A-slice and B-chunk loads (the
+    // drain below waits for the ones never consumed).
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
+    for (int kc = 0; kc < nkc && !s_fail; ++kc) {
+      const int hb = kc & 1;
+      if (kc >= 2 && !mbar_wait(&bars->bempty[hb], ((kc >> 1) - 1) & 1)) {
+        atomicExch(status, (int)kFlagTimeout);
+        s_fail = 1;
+        break;
+      }
+      mbar_expect_tx(&bars->bfull[hb], B_CHUNK_BYTES);
+      for (int t = 0; t < OZ_S; ++t)
+        tma_load_2d(sB + hb * B_CHUNK_BYTES + t * B_SLICE_BYTES, &tmB, &bars->bfull[hb], kc * OBK,
+                    t * n_pad + n0);
+      s_bissued = kc + 1;
+      for (int sl = 0; sl < OZ_S; ++sl) {
+        const int g = kc * OZ_S + sl, st = g % A_RING;
+        if (g >= A_RING && !mbar_wait(&bars->aempty[st], ((g / A_RING) - 1) & 1)) {
+          atomicExch(status, (int)kFlagTimeout);
+          s_fail = 1;
+          break;
+        }
+        mbar_expect_tx(&bars->afull[st], A_SLICE_BYTES);
+        tma_load_2d(sA + st * A_SLICE_BYTES, &tmA, &bars->afull[st], kc * OBK, sl * m_pad + m0);
+        s_issued = g + 1;
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    const uint32_t idesc = oz_idesc();
+    uint32_t written = 0;
+    for (int kc = 0; kc < nkc && !s_fail; ++kc) {
+      const int hb = kc & 1;
+      if (!mbar_wait(&bars->bfull[hb], (kc >> 1) & 1)) {
+        atomicExch(status, (int)kFlagTimeout);
+        s_fail = 1;
+        break;
+      }
+      s_bconsumed = kc + 1;
+      const unsigned char* bchunk = sB + hb * B_CHUNK_BYTES;
+      for (int sl = 0; sl < OZ_S; ++sl) {
+        const int g = kc * OZ_S + sl, st = g % A_RING;
+        if (!mbar_wait(&bars->afull[st], (g / A_RING) & 1)) {
+          atomicExch(status, (int)kFlagTimeout);
+          s_fail = 1;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const unsigned char* aslice = sA + st * A_SLICE_BYTES;
+        for (int t = 0; t + sl < OZ_S; ++t) {  // s + t <= 9 (1-based)
+          const int acc = min(sl + t, OZ_NACC - 1);
+          const uint32_t dst = tmem + (uint32_t)(acc * OBN);
+#pragma unroll
+          for (int kk = 0; kk < OBK / 16; ++kk) {
+            const uint64_t ad = smem_desc_sw128(aslice + kk * 32);
+            const uint64_t bd = smem_desc_sw128(bchunk + t * B_SLICE_BYTES + kk * 32);
+            umma_f16(dst, ad, bd, idesc, (written >> acc) & 1u);
+            written |= 1u << acc;
+          }
+        }
+        umma_commit(&bars->aempty[st]);
+        s_consumed = g + 1;
+      }
+      if (s_fail) break;
+      umma_commit(&bars->bempty[hb]);
+    }
+    umma_commit(&bars->done);  // arrives when every issued MMA has completed
+  }
+  __syncwarp();
+  const bool ok = mbar_wait(&bars->done, 0);
+  if (!ok) atomicExch(status, (int)kFlagTimeout);
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  __syncthreads();
+  if (ok && !s_fail) {
+    const int row = m0 + warp * 32 + lane;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    const double rsc = (row < m) ? alpha * rs[row] : 0.0;
+#pragma unroll 1
+    for (int c0 = 0; c0 < OBN; c0 += 16) {
+      if (n0 + c0 >= n) break;  // warp-uniform
+      uint32_t r[OZ_NACC][16];
+#pragma unroll
+      for (int a = 0; a < OZ_NACC; ++a) tmem_ld16_nowait(trow + (uint32_t)(a * OBN + c0), r[a]);
+      tmem_ld_wait();
+#pragma unroll
+      for (int a = 0; a < OZ_NACC; ++a) touch16(r[a]);
+      const int ncol = min(16, n - (n0 + c0));
+      if (row < m) {
+        double* cbase = C + (long long)row + (long long)(n0 + c0) * ldc;
+        double cv[16], sc[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          cv[j] = (j < ncol) ? cbase[(long long)j * ldc] : 0.0;
+          sc[j] = (j < ncol) ? __ldg(cs + n0 + c0 + j) : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          // P_d = acc_d * 2^(7(d-2)) exactly; the tail keeps 3 fraction bits
+          const long long p2 = __float2int_rn(__uint_as_float(r[0][j]));
+          const long long p3 = __float2int_rn(__uint_as_float(r[1][j]) * 128.0f);
+          const long long p4 = __float2int_rn(__uint_as_float(r[2][j]) * 16384.0f);
+          const long long p5 = __float2int_rn(__uint_as_float(r[3][j]) * 2097152.0f);
+          const long long p6 = __float2int_rn(__uint_as_float(r[4][j]) * 268435456.0f);
+          const long long t8 = __float2ll_rn(__uint_as_float(r[5][j]) * 274877906944.0f);  // 2^38
+          const long long I = (p2 << 38) + (p3 << 31) + (p4 << 24) + (p5 << 17) + (p6 << 10) + t8;
+          if (j < ncol) cbase[(long long)j * ldc] = fma(rsc * sc[j], __ll2double_rn(I), cv[j]);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (s_fail && threadIdx.x == 0) {
+    // Drain A-slice copies that were issued but never consumed, then any B
+    // chunk still in flight (bounded waits).
+    for (int g = s_consumed; g < s_issued; ++g)
+      mbar_wait(&bars->afull[g % A_RING], (g / A_RING) & 1);
+    for (int kc = s_bconsumed; kc < s_bissued; ++kc)
+      mbar_wait(&bars->bfull[kc & 1], (kc >> 1) & 1);
+  }
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(OZ_TMEM_COLS));
+  }
+}
+
+// Slices of the rows of A (m x k, column-major): scale rs[i] = 2^(e_i - 26)
+// (NaN for a row holding Inf or NaN, whose slices are zero), slices
+// S[s][i][kk] (s-major, rows padded to m_pad, k to kpad, zero-filled).
+// One CTA per 32 rows, 256 threads.
+__global__ void __launch_bounds__(256)
+oz_split_rows_kernel(const double* __restrict__ A, long long lda, int m, int k, int kpad,
+                     int m_pad, __nv_bfloat16* Sl, double* rs) {
+  __shared__ double tile[64][33];
+  __shared__ double red[8][33];
+  __shared__ int s_e[32];
+  const int i0 = blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int i = i0 + tx;
+  // row maxima (a non-finite entry poisons the row)
+  double mx = 0.0;
+  bool bad = false;
+  if (i < m)
+    for (int kk = ty; kk < k; kk += 8) {
+      const double v = fabs(A[i + (long long)kk * lda]);
+      if (!(v <= 1.79769313486231570e308)) bad = true;
+      else mx = fmax(mx, v);
+    }
+  red[ty][tx] = bad ? -1.0 : mx;
+  __syncthreads();
+  if (ty == 0) {
+    double r = 0.0;
+    bool b = false;
+    for (int q = 0; q < 8; ++q) {
+      const double v = red[q][tx];
+      if (v < 0.0) b = true;
+      else r = fmax(r, v);
+    }
+    int e = 0;
+    if (!b && r > 0.0) frexp(r, &e);
+    s_e[tx] = b ? INT_MIN : e;
+    if (i < m_pad) rs[i] = (i < m) ? (b ? __longlong_as_double(0x7ff8000000000000LL) : ldexp(1.0, e - 26)) : 0.0;
+  }
+  __syncthreads();
+  // slices, 64 k at a time: read coalesced along rows, write 64 k per row
+  for (int k0 = 0; k0 < kpad; k0 += 64) {
+    for (int q = ty; q < 64; q += 8) {
+      const int kk = k0 + q;
+      tile[q][tx] = (i < m && kk < k) ? A[i + (long long)kk * lda] : 0.0;
+    }
+    __syncthreads();
+    const int r = threadIdx.x >> 3, g = threadIdx.x & 7;  // row r, k group g (8 values)
+    const int e = s_e[r];
+    const bool zero = (e == INT_MIN);
+    float vals[OZ_S][8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      double y = zero ? 0.0 : ldexp(tile[g * 8 + q][r], OZ_BITS - e);
+#pragma unroll
+      for (int s = 0; s < OZ_S; ++s) {
+        const double a = trunc(y);
+        vals[s][q] = (float)a;
+        y = (y - a) * (double)(1 << OZ_BITS);
+      }
+    }
+    const int row = i0 + r;
+    if (row < m_pad) {
+#pragma unroll
+      for (int s = 0; s < OZ_S; ++s) {
+        const float w = ldexpf(1.0f, -OZ_BITS * s);
+        __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) h[q] = __float2bfloat16_rn(vals[s][q] * w);
+        *reinterpret_cast<uint4*>(Sl + ((size_t)s * m_pad + row) * kpad + k0 + g * 8) =
+            *reinterpret_cast<const uint4*>(h);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Slices of the columns of B (k x n, column-major, columns contiguous in k):
+// scale cs[j] = 2^(f_j - 26) (NaN for a non-finite column), slices
+// S[t][j][kk]. One warp per column, lane l holds k = 8l .. 8l+7.
+__global__ void __launch_bounds__(256)
+oz_split_cols_kernel(const double* __restrict__ B, long long ldb, int k, int n, int kpad,
+                     int n_pad, __nv_bfloat16* Sl, double* cs) {
+  const int j = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (j >= n_pad) return;
+  double x[8];
+  double mx = 0.0;
+  bool bad = false;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int kk = lane * 8 + q;
+    x[q] = (j < n && kk < k) ? B[kk + (long long)j * ldb] : 0.0;
+    const double v = fabs(x[q]);
+    if (!(v <= 1.79769313486231570e308)) bad = true;
+    else mx = fmax(mx, v);
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    bad = __any_sync(0xffffffffu, bad);
+  }
+  int e = 0;
+  if (!bad && mx > 0.0) frexp(mx, &e);
+  if (lane == 0)
+    cs[j] = (j < n) ? (bad ? __longlong_as_double(0x7ff8000000000000LL) : ldexp(1.0, e - 26)) : 0.0;
+  if (lane * 8 >= kpad) return;
+  float vals[OZ_S][8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    double y = bad ? 0.0 : ldexp(x[q], OZ_BITS - e);
+#pragma unroll
+    for (int s = 0; s < OZ_S; ++s) {
+      const double a = trunc(y);
+      vals[s][q] = (float)a;
+      y = (y - a) * (double)(1 << OZ_BITS);
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < OZ_S; ++s) {
+    const float w = ldexpf(1.0f, -OZ_BITS * s);
+    __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) h[q] = __float2bfloat16_rn(vals[s][q] * w);
+    *reinterpret_cast<uint4*>(Sl + ((size_t)s * n_pad + j) * kpad + lane * 8) =
+        *reinterpret_cast<const uint4*>(h);
+  }
+}
+
+// 2D map over the slices: rows = S * rows_pad (slice-major), kpad columns of
+// BF16, box {64, box_rows}, 128-byte swizzle.
+bool make_slice_map(CUtensorMap* map, const void* ptr, int rows_total, int kpad, int box_rows) {
+  auto enc = get_encode();
+  if (!enc) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)kpad, (cuuint64_t)rows_total};
+  cuuint64_t strides[1] = {(cuuint64_t)kpad * 2};
+  cuuint32_t box[2] = {(cuuint32_t)OBK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims,
+                   strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+cudaError_t oz_smem_once() {
+  static const cudaError_t e = cudaFuncSetAttribute(
+      ozgemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_smem_bytes());
+  return e;
+}
+
+inline int round_up(int x, int q) { return (x + q - 1) / q * q; }
+
+}  // namespace
+
+OzScratch& oz_scratch() {
+  static OzScratch s;
+  return s;
+}
+
+size_t oz_scratch_bytes(int m, int n, int k) {
+  const size_t kp = (size_t)round_up(k < OZ_KMAX ? k : OZ_KMAX, OBK);
+  const size_t mp = (size_t)round_up(m, OBM), np = (size_t)round_up(n, OBN);
+  return OZ_S * (mp + np) * kp * 2 + (mp + np) * sizeof(double) + 1024;
+}
+
+bool oz_fits(int m, int n, int k) {
+  const OzScratch& s = oz_scratch();
+  return s.ptr && oz_scratch_bytes(m, n, k) <= s.bytes;
+}
+
+// C (m x n) += alpha * A (m x k) * B (k x n), all FP64 column-major, through
+// the sliced BF16 product; K is taken in passes of at most 256.
+cudaError_t oz_dgemm(int m, int n, int k, double alpha, const double* A, long long lda,
+                     const double* B, long long ldb, double* C, long long ldc, int* status,
+                     cudaStream_t s) {
+  if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
+  if (!oz_fits(m, n, k)) return cudaErrorMemoryAllocation;
+  SL_TRY(oz_smem_once());
+  const int m_pad = round_up(m, OBM), n_pad = round_up(n, OBN);
+  OzScratch& sc = oz_scratch();
+  for (int k0 = 0; k0 < k; k0 += OZ_KMAX) {
+    const int kb = (k - k0) < OZ_KMAX ? (k - k0) : OZ_KMAX;
+    const int kpad = round_up(kb, OBK);
+    unsigned char* p = reinterpret_cast<unsigned char*>(sc.ptr);
+    __nv_bfloat16* sa = reinterpret_cast<__nv_bfloat16*>(p);
+    __nv_bfloat16* sb = sa + (size_t)OZ_S * m_pad * kpad;
+    double* rs = reinterpret_cast<double*>(sb + (size_t)OZ_S * n_pad * kpad);
+    double* cs = rs + m_pad;
+    oz_split_rows_kernel<<<m_pad / 32, 256, 0, s>>>(A + (long long)k0 * lda, lda, m, kb, kpad, m_pad,
+                                                    sa, rs);
+    oz_split_cols_kernel<<<n_pad / 8, 256, 0, s>>>(B + k0, ldb, kb, n, kpad, n_pad, sb, cs);
+    CUtensorMap ta, tb;
+    if (!make_slice_map(&ta, sa, OZ_S * m_pad, kpad, OBM) ||
+        !make_slice_map(&tb, sb, OZ_S * n_pad, kpad, OBN))
+      return cudaErrorInvalidResourceHandle;
+    const int tiles = (m_pad / OBM) * (n_pad / OBN);
+    ozgemm_kernel<<<tiles, 128, oz_smem_bytes(), s>>>(ta, tb, m, n, kpad, m_pad, n_pad, rs, cs,
+                                                      alpha, C, ldc, status);
+    count_launches(3);
+    SL_TRY(cudaGetLastError());
+  }
+  return cudaSuccess;
+}
+
+}  // namespace sl

@@ -47,6 +47,26 @@ struct SplitKScratch {
 };
 SplitKScratch& splitk_scratch();
 
+// Scratch of the sliced FP64 trailing update (ozgemm_f64.cu): BF16 slices of
+// both operands and their row / column scales. Grown by the library before a
+// factorization; when it is absent or too small the DMMA product is used.
+struct OzScratch {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+OzScratch& oz_scratch();
+size_t oz_scratch_bytes(int m, int n, int k);
+bool oz_fits(int m, int n, int k);
+// C (m x n) += alpha * A (m x k) * B (k x n), FP64, column-major, on the BF16
+// tensor cores through exact 7-bit slices (needs oz_fits(m, n, k)).
+cudaError_t oz_dgemm(int m, int n, int k, double alpha, const double* A, long long lda,
+                     const double* B, long long ldb, double* C, long long ldc, int* status,
+                     cudaStream_t s);
+// Trailing-update arithmetic of the FP64 factorization: 0 = FP64 DMMA,
+// 1 = sliced BF16 tensor-core product (when its scratch is present).
+void f64_update_set(int mode);
+int f64_update_get();
+
 // Register-only DMMA throughput loop (FP64 tensor peak calibration), TFLOP/s.
 double dmma_peak_tflops(cudaStream_t s);
 
@@ -143,7 +163,7 @@ struct MixedWork {
   double* Acopy = nullptr;     // optional FP64 copy of A for the fallback (keeps A)
   long long ldacopy = 0;
   int* chain = nullptr;        // chained solves: ticket (16 ints) + n x 8 x 2 tagged words
-  float* dinv = nullptr;       // inverses of the 64x64 diagonal blocks of L then U (2 x ceil(n/64) x 4096)
+  float* dinv = nullptr;       // inverses of the 64x64 diagonal blocks of L, of U, then M_b of L, of U (4 x ceil(n/64) x 4096)
   int* epoch = nullptr;        // host-side counter of chained-solve epochs
   int* status = nullptr;       // device status word
 };
