@@ -228,11 +228,15 @@ int sl1x1_batch_plan_results(sl1x1_batch_plan plan, int* info, int* iters, doubl
 int sl1x1_batch_plan_shape(sl1x1_batch_plan plan, int* threads, int* chunk, int* ctas_per_sm);
 void sl1x1_batch_plan_destroy(sl1x1_batch_plan plan);
 
-/* Allocation-free FP64 LU (no counterpart in the reference): the same
- * factorization, pivots and INFO as sl1x1_dgetrf_dev, for callers that may not
- * allocate GPU memory (memory pools or arenas that own the device heap,
- * loops that must not allocate after start-up). Its scratch is a static
- * 1 MiB device array held by every GPU that loads this library until exit.
+/* Allocation-free FP64 LU (no counterpart in the reference): the
+ * factorization of sl1x1_dgetrf_dev for callers that may not allocate GPU
+ * memory (memory pools or arenas that own the device heap, loops that must not
+ * allocate after start-up). Its scratch is a static 1 MiB device array held by
+ * every GPU that loads this library until exit; the sliced tensor-core update,
+ * whose scratch grows with the matrix, does not fit there, so this entry point
+ * always runs the FP64 DMMA update: its factors, pivots and INFO are those of
+ * sl1x1_dgetrf_dev with sl1x1_set_f64_update(0), and agree with the default
+ * (sliced) factorization to rounding, with the same pivots.
  * The first call on a device looks up that array's address (make it before
  * any stream capture); calls whose GPU work overlaps race on the shared array.
  * M above 152 SMs x 768 rows is rejected with -30000 before any launch. */

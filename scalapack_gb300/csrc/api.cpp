@@ -169,9 +169,8 @@ void release_all() {
   cudaFree(g_dev.dw); cudaFree(g_dev.dAx); cudaFree(g_dev.dh); cudaFree(g_dev.dAcopy);
   cudaFree(g_dev.dchain); cudaFree(g_dev.dsplitk); cudaFree(g_dev.daux); cudaFree(g_dev.ddinv);
   cudaFree(g_dev.dA2); cudaFree(g_dev.dX); cudaFree(g_dev.drw); cudaFree(g_dev.drc);
-  cudaFree(g_dev.dipiv2); cudaFree(g_dev.doz);
+  cudaFree(g_dev.dipiv2); cudaFree(g_dev.doz); cudaFree(g_dev.doz2); cudaFree(g_dev.ddinv64);
   sl::splitk_scratch() = sl::SplitKScratch();
-  sl::oz_scratch() = sl::OzScratch();
   if (g_dev.stream) cudaStreamDestroy(g_dev.stream);
   if (g_dev.aux) cudaStreamDestroy(g_dev.aux);
   if (g_dev.ev_next) cudaEventDestroy(g_dev.ev_next);
@@ -181,15 +180,15 @@ void release_all() {
 
 void ensure_oz(int m, int n, int nb) {
   if (sl::f64_update_get() != 1 || m <= 0 || n <= 0) return;
-  const size_t need = sl::oz_scratch_bytes(m, n, nb > 0 ? nb : g_default_nb);
-  if (need <= g_dev.capOz && g_dev.doz) return;
-  if (grow(&g_dev.doz, &g_dev.capOz, need) == cudaSuccess) {
-    sl::oz_scratch().ptr = g_dev.doz;
-    sl::oz_scratch().bytes = g_dev.capOz;
-  } else {
-    cudaGetLastError();
-    sl::oz_scratch() = sl::OzScratch();
-  }
+  if (nb <= 0) nb = g_default_nb;
+  const size_t need = sl::oz_scratch_bytes(m, n, nb);
+  const size_t need2 = sl::oz_scratch_bytes(m, nb, 32);  // the panel's 32-column updates
+  cudaError_t e = cudaSuccess;
+  if (need > g_dev.capOz || !g_dev.doz) e = grow(&g_dev.doz, &g_dev.capOz, need);
+  if (e == cudaSuccess && (need2 > g_dev.capOz2 || !g_dev.doz2))
+    e = grow(&g_dev.doz2, &g_dev.capOz2, need2);
+  if (e == cudaSuccess && !g_dev.ddinv64) e = cudaMalloc(&g_dev.ddinv64, sl::kDinv64Doubles * sizeof(double));
+  if (e != cudaSuccess) cudaGetLastError();  // the DMMA update covers what is missing
 }
 
 sl::LuWork make_work() {
@@ -202,6 +201,11 @@ sl::LuWork make_work() {
   w.bswap = g_dev.dbswap;
   w.perm_len = g_dev.capPerm;
   w.bswap_len = g_dev.capBs;
+  w.oz.ptr = g_dev.doz;
+  w.oz.bytes = g_dev.doz ? g_dev.capOz : 0;
+  w.oz_aux.ptr = g_dev.doz2;
+  w.oz_aux.bytes = g_dev.doz2 ? g_dev.capOz2 : 0;
+  w.dinv64 = g_dev.ddinv64;
   if (g_lookahead) {
     w.aux = g_dev.aux;
     w.ev_next = g_dev.ev_next;
@@ -1003,11 +1007,12 @@ int sl1x1_ozgemm_dev(int m, int n, int k, double alpha, const double* dA, long l
   if (need > g_dev.capOz || !g_dev.doz) {
     cudaError_t e = grow(&g_dev.doz, &g_dev.capOz, need);
     if (e != cudaSuccess) return cuda_info(e);
-    sl::oz_scratch().ptr = g_dev.doz;
-    sl::oz_scratch().bytes = g_dev.capOz;
   }
+  sl::OzScratch sc;
+  sc.ptr = g_dev.doz;
+  sc.bytes = g_dev.capOz;
   cudaError_t e = cudaMemsetAsync(g_dev.dsmall + 2, 0, sizeof(int), s);
-  if (e == cudaSuccess) e = sl::oz_dgemm(m, n, k, alpha, dA, ldda, dB, lddb, dC, lddc, g_dev.dsmall + 2, s);
+  if (e == cudaSuccess) e = sl::oz_dgemm(sc, m, n, k, alpha, dA, ldda, dB, lddb, dC, lddc, g_dev.dsmall + 2, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_info(e);
   int st = 0;

@@ -52,7 +52,9 @@ struct DevState {
   float* ddinv = nullptr; size_t capDinv = 0;
   double* dsplitk = nullptr; size_t capSplitk = 0;
   double* daux = nullptr; size_t capAux = 0;
-  unsigned char* doz = nullptr; size_t capOz = 0;  // sliced FP64 update scratch (bytes)
+  unsigned char* doz = nullptr; size_t capOz = 0;    // sliced-product scratch, caller's stream (bytes)
+  unsigned char* doz2 = nullptr; size_t capOz2 = 0;  // sliced-product scratch, panel stream (bytes)
+  double* ddinv64 = nullptr;                          // U12 solve: inverses of L11's 64x64 blocks
   int chain_epoch = 0;
   unsigned short* dA16 = nullptr; size_t capA16 = 0;
   unsigned short* dB16 = nullptr; size_t capB16 = 0;

@@ -93,12 +93,76 @@ cudaError_t perm_compose(const int* dipiv, int n, int* perm, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+static int g_f64_update = 1;
+
+void f64_update_set(int mode) { g_f64_update = (mode == 0) ? 0 : 1; }
+int f64_update_get() { return g_f64_update; }
+
+// C (m x n) -= A (m x k) * B (k x n) inside the factorization: the sliced
+// tensor-core product when selected and its scratch fits, else FP64 DMMA.
+static cudaError_t lu_update(const OzScratch& sc, int m, int n, int k, double alpha,
+                             const double* A, long long lda, const double* B, long long ldb,
+                             double* C, long long ldc, const LuWork& ws, cudaStream_t s) {
+  if (g_f64_update == 1 && oz_fits(sc, m, n, k))
+    return oz_dgemm(sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, ws.status, s);
+  return dgemm(false, m, n, k, alpha, A, lda, B, ldb, 1.0, C, ldc, s);
+}
+
+// N_b = inv(L_bb) - I for the 64x64 diagonal blocks of the unit-lower L11
+// (jb x jb, leading dimension ldl): block b at Ninv + b*4096, column-major
+// with leading dimension 64; a partial last block is padded with the
+// identity. Thread t forms column t of the inverse by substitution in FP64.
+__global__ void __launch_bounds__(64)
+unit_lower_inv64_kernel(int jb, const double* __restrict__ L, long long ldl, double* Ninv) {
+  extern __shared__ double inv_smem[];  // Ls[64][65] then X[64][65]
+  double(*Ls)[65] = reinterpret_cast<double(*)[65]>(inv_smem);
+  double(*X)[65] = reinterpret_cast<double(*)[65]>(inv_smem + 64 * 65);
+  const int b = blockIdx.x, t = threadIdx.x;
+  const int r0 = b * 64, rb = min(64, jb - r0);
+  for (int c = 0; c < 64; ++c)
+    Ls[t][c] = (t < rb && c < t) ? L[(r0 + t) + (long long)(r0 + c) * ldl] : 0.0;
+  for (int i = 0; i < 64; ++i) X[i][t] = (i == t) ? 1.0 : 0.0;
+  __syncthreads();
+  for (int i = t + 1; i < 64; ++i) {
+    double acc = 0.0;
+    for (int q = t; q < i; ++q) acc = fma(Ls[i][q], X[q][t], acc);
+    X[i][t] = -acc;
+  }
+  __syncthreads();
+  double* Nb = Ninv + (size_t)b * 4096;
+  for (int q = 0; q < 64; ++q) {
+    const int i = t, c = q;  // coalesced along rows i
+    Nb[i + 64 * c] = (i > c) ? X[i][c] : 0.0;
+  }
+}
+
+// U12 = L11^-1 A12 (jb x nr, in place). With the sliced product and the
+// diagonal-block inverses of L11 at hand (formed at the end of its panel):
+// per 64-row block b, X_b = A12_b + (inv(L_bb) - I) A12_b, then the rows below
+// lose L(below, b) X_b -- every product on the tensor cores. Otherwise the
+// FP64 strip solve.
+static cudaError_t solve_u12(int jb, int nr, const double* L11, long long ldl, double* A12,
+                             long long lda, const LuWork& ws, cudaStream_t s) {
+  if (!(g_f64_update == 1 && ws.dinv64 && jb <= 1024 && oz_fits(ws.oz, jb, nr, 64)))
+    return trsm_strip<double, false, false, true>(jb, nr, L11, ldl, A12, lda, s);
+  for (int r0 = 0; r0 < jb; r0 += 64) {
+    const int w = (jb - r0) < 64 ? (jb - r0) : 64;
+    SL_TRY(oz_dgemm(ws.oz, w, nr, w, 1.0, ws.dinv64 + (size_t)(r0 / 64) * 4096, 64, A12 + r0, lda,
+                    A12 + r0, lda, ws.status, s));
+    if (r0 + w < jb)
+      SL_TRY(oz_dgemm(ws.oz, jb - r0 - w, nr, w, -1.0, L11 + (r0 + w) + (long long)r0 * ldl, ldl,
+                      A12 + r0, lda, A12 + r0 + w, lda, ws.status, s));
+  }
+  return cudaSuccess;
+}
+
 // PDGETF2 on columns [j, j+jb), rows [j, m): 32-wide cooperative sub-panels,
 // each followed by its row interchanges on the rest of the panel, the U solve
 // and the GEMM update of the panel's remaining columns.
 static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, int j, int jb,
                                 const LuWork& ws, cudaStream_t s) {
   auto Ap = [&](long long i, long long c) { return dA + i + c * ldda; };
+  const OzScratch& sc = (ws.aux && s == ws.aux) ? ws.oz_aux : ws.oz;
   phase_begin(kPhPanel, s);
   double pflops = 0.0;
   for (int c = 0; c < jb; c += PW) {
@@ -113,8 +177,8 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
                                                       Ap(r0, r0 + w), ldda, s)));
       pflops += (double)kw * kw * (jb - c - w);
       if (r0 + kw < m) {
-        SL_TRY(dgemm(false, m - r0 - kw, jb - c - w, kw, -1.0, Ap(r0 + kw, r0), ldda,
-                     Ap(r0, r0 + w), ldda, 1.0, Ap(r0 + kw, r0 + w), ldda, s));
+        SL_TRY(lu_update(sc, m - r0 - kw, jb - c - w, kw, -1.0, Ap(r0 + kw, r0), ldda,
+                         Ap(r0, r0 + w), ldda, Ap(r0 + kw, r0 + w), ldda, ws, s));
         pflops += 2.0 * (double)(m - r0 - kw) * (jb - c - w) * kw;
       }
     }
@@ -123,23 +187,17 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
   // the other columns (computed here, on the panel's stream)
   const int npiv = (m - j) < jb ? (m - j) : jb;
   if (ws.swap_plan && npiv <= LSW_MAXP) SL_TRY(laswp_plan(j, j + npiv, dipiv, ws.swap_plan, s));
+  // inverses of L11's diagonal blocks for the U12 solve of this step
+  if (g_f64_update == 1 && ws.dinv64 && npiv == jb && jb <= 1024) {
+    constexpr int kInvSmem = 2 * 64 * 65 * (int)sizeof(double);
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        unit_lower_inv64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvSmem);
+    SL_TRY(attr);
+    unit_lower_inv64_kernel<<<(jb + 63) / 64, 64, kInvSmem, s>>>(jb, Ap(j, j), ldda, ws.dinv64);
+    count_launches(1);
+  }
   phase_end(kPhPanel, s, pflops, 16.0 * (double)(m - j) * jb);
   return cudaSuccess;
-}
-
-static int g_f64_update = 1;
-
-void f64_update_set(int mode) { g_f64_update = (mode == 0) ? 0 : 1; }
-int f64_update_get() { return g_f64_update; }
-
-// A22 -= L21 * U12 (m x n, k = the panel width): the sliced tensor-core
-// product when selected and its scratch fits, else FP64 DMMA.
-static cudaError_t trailing_update(int m, int n, int k, const double* L21, long long ldl,
-                            const double* U12, long long ldu, double* C, long long ldc,
-                            const LuWork& ws, cudaStream_t s) {
-  if (g_f64_update == 1 && oz_fits(m, n, k))
-    return oz_dgemm(m, n, k, -1.0, L21, ldl, U12, ldu, C, ldc, ws.status, s);
-  return dgemm(false, m, n, k, -1.0, L21, ldl, U12, ldu, 1.0, C, ldc, s);
 }
 
 // Right-looking blocked LU. With look-ahead resources in `ws`, the panel of
@@ -172,7 +230,7 @@ cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, 
       // ---- PDTRSM: U12 = L11^{-1} A12 ----
       const double nr = (double)(n - jn);
       phase_begin(kPhTrsm, s);
-      SL_TRY((trsm_strip<double, false, false, true>(jb, n - jn, Ap(j, j), ldda, Ap(j, jn), ldda, s)));
+      SL_TRY(solve_u12(jb, n - jn, Ap(j, j), ldda, Ap(j, jn), ldda, ws, s));
       phase_end(kPhTrsm, s, (double)jb * jb * nr, 8.0 * (0.5 * jb * jb + 2.0 * jb * nr));
       // ---- PDGEMM: A22 -= L21 * U12 ----
       if (jn < m) {
@@ -180,8 +238,8 @@ cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, 
         if (lookahead && jb2 > 0) {
           // next panel's columns first, then the panel on the look-ahead stream
           phase_begin(kPhGemm, s);
-          SL_TRY(trailing_update(m - jn, jb2, jb, Ap(jn, j), ldda, Ap(j, jn), ldda, Ap(jn, jn),
-                                 ldda, ws, s));
+          SL_TRY(lu_update(ws.oz, m - jn, jb2, jb, -1.0, Ap(jn, j), ldda, Ap(j, jn), ldda,
+                           Ap(jn, jn), ldda, ws, s));
           phase_end(kPhGemm, s, 2.0 * mr * jb2 * jb, 8.0 * (mr * jb + (double)jb * jb2 + 2.0 * mr * jb2));
           SL_TRY(cudaEventRecord(ws.ev_next, s));
           SL_TRY(cudaStreamWaitEvent(ws.aux, ws.ev_next, 0));
@@ -191,14 +249,14 @@ cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, 
           const int rest = n - jn - jb2;
           if (rest > 0) {
             phase_begin(kPhGemm, s);
-            SL_TRY(trailing_update(m - jn, rest, jb, Ap(jn, j), ldda, Ap(j, jn + jb2), ldda,
-                                   Ap(jn, jn + jb2), ldda, ws, s));
+            SL_TRY(lu_update(ws.oz, m - jn, rest, jb, -1.0, Ap(jn, j), ldda, Ap(j, jn + jb2), ldda,
+                             Ap(jn, jn + jb2), ldda, ws, s));
             phase_end(kPhGemm, s, 2.0 * mr * rest * jb, 8.0 * (mr * jb + (double)jb * rest + 2.0 * mr * rest));
           }
         } else {
           phase_begin(kPhGemm, s);
-          SL_TRY(trailing_update(m - jn, n - jn, jb, Ap(jn, j), ldda, Ap(j, jn), ldda, Ap(jn, jn),
-                                 ldda, ws, s));
+          SL_TRY(lu_update(ws.oz, m - jn, n - jn, jb, -1.0, Ap(jn, j), ldda, Ap(j, jn), ldda,
+                           Ap(jn, jn), ldda, ws, s));
           phase_end(kPhGemm, s, 2.0 * mr * nr * jb, 8.0 * (mr * jb + jb * nr + 2.0 * mr * nr));
         }
       }

@@ -12,7 +12,10 @@
 // first-zero-pivot column, the panel kernel's exchange area and the plan of a
 // panel's row interchanges -- lives in the file-scope array below, a fixed 1 MiB that every GPU
 // which loads this library holds until the process exits. The caller passes
-// the matrix and the pivot array as usual.
+// the matrix and the pivot array as usual. The LuWork below carries no
+// sliced-product scratch (its size grows with the matrix), so the trailing
+// update and the U12 solve run in FP64 (DMMA and the strip solve): the
+// results are those of sl1x1_dgetrf_dev with sl1x1_set_f64_update(0).
 //
 // Set-up: the first call on each device looks up the device address of that
 // array (cudaGetSymbolAddress, with that device current) and caches it; make

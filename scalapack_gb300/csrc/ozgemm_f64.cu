@@ -278,129 +278,152 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
   }
 }
 
-// Slices of the rows of A (m x k, column-major): scale rs[i] = 2^(e_i - 26)
-// (NaN for a row holding Inf or NaN, whose slices are zero), slices
-// S[s][i][kk] (s-major, rows padded to m_pad, k to kpad, zero-filled).
-// One CTA per 32 rows, 256 threads.
-__global__ void __launch_bounds__(256)
-oz_split_rows_kernel(const double* __restrict__ A, long long lda, int m, int k, int kpad,
-                     int m_pad, __nv_bfloat16* Sl, double* rs) {
-  __shared__ double tile[64][33];
-  __shared__ double red[8][33];
-  __shared__ int s_e[32];
-  const int i0 = blockIdx.x * 32;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int i = i0 + tx;
-  // row maxima (a non-finite entry poisons the row)
-  double mx = 0.0;
-  bool bad = false;
-  if (i < m)
-    for (int kk = ty; kk < k; kk += 8) {
-      const double v = fabs(A[i + (long long)kk * lda]);
-      if (!(v <= 1.79769313486231570e308)) bad = true;
-      else mx = fmax(mx, v);
-    }
-  red[ty][tx] = bad ? -1.0 : mx;
-  __syncthreads();
-  if (ty == 0) {
-    double r = 0.0;
-    bool b = false;
-    for (int q = 0; q < 8; ++q) {
-      const double v = red[q][tx];
-      if (v < 0.0) b = true;
-      else r = fmax(r, v);
-    }
-    int e = 0;
-    if (!b && r > 0.0) frexp(r, &e);
-    s_e[tx] = b ? INT_MIN : e;
-    if (i < m_pad) rs[i] = (i < m) ? (b ? __longlong_as_double(0x7ff8000000000000LL) : ldexp(1.0, e - 26)) : 0.0;
+// ---- slicing (integer arithmetic on the FP64 bit patterns) ----------------
+//
+// With x = +-m 2^q (m the significand as an integer, 53 bits for normal x)
+// and a scale exponent e with |x| < 2^e, U = floor(|x| 2^(56-e)) is m shifted
+// left by at most 3 bits, or right (dropping the bits below 2^-56 of the
+// scale). Slice s (1-based) is bits [56-7s, 63-7s) of U with the sign of x:
+// exactly the integer parts of the FP64 truncation x 2^-e = sum a_s 2^-7s.
+constexpr unsigned long long kMagMask = 0x7fffffffffffffffULL;
+constexpr unsigned long long kInfBits = 0x7ff0000000000000ULL;
+
+__device__ __forceinline__ unsigned long long oz_fixed(unsigned long long bits, int e) {
+  const int bexp = (int)((bits >> 52) & 0x7ff);
+  unsigned long long m = bits & 0xfffffffffffffULL;
+  int q = -1074;
+  if (bexp != 0) {
+    m |= 1ULL << 52;
+    q = bexp - 1075;
   }
-  __syncthreads();
-  // slices, 64 k at a time: read coalesced along rows, write 64 k per row
-  for (int k0 = 0; k0 < kpad; k0 += 64) {
-    for (int q = ty; q < 64; q += 8) {
-      const int kk = k0 + q;
-      tile[q][tx] = (i < m && kk < k) ? A[i + (long long)kk * lda] : 0.0;
+  const int sh = q - e + 56;
+  if (sh >= 0) return m << sh;
+  if (sh <= -64) return 0ULL;
+  return m >> (-sh);
+}
+
+// frexp exponent of the largest magnitude (its bit pattern, finite, nonzero)
+__device__ __forceinline__ int oz_scale_exp(unsigned long long kmax) {
+  const int bexp = (int)(kmax >> 52);
+  if (bexp != 0) return bexp - 1022;
+  return (63 - __clzll((long long)kmax)) - 1073;  // subnormal
+}
+
+// 2^(e - 26) as a double (the epilogue's scale factor half), NaN for a
+// non-finite row or column, 0 for a zero one
+__device__ __forceinline__ double oz_scale_value(unsigned long long kmax, bool bad) {
+  if (bad) return __longlong_as_double(0x7ff8000000000000LL);
+  if (kmax == 0ULL) return 0.0;
+  const int be = oz_scale_exp(kmax) - 26 + 1023;
+  if (be >= 1 && be <= 2046) return __longlong_as_double((long long)((unsigned long long)be << 52));
+  return ldexp(1.0, oz_scale_exp(kmax) - 26);
+}
+
+__device__ __forceinline__ __nv_bfloat16 oz_slice_bf16(unsigned long long U, int s, bool neg) {
+  // s is 0-based here: bits [49-7s, 56-7s), weight 2^-7s in the stored slice
+  const float a = (float)(unsigned)((U >> (49 - OZ_BITS * s)) & 127ULL);
+  return __float2bfloat16_rn((neg ? -a : a) * __int_as_float((127 - OZ_BITS * s) << 23));
+}
+
+// Both operands in one launch. Blocks [0, m_pad/32): 32 rows of A (m x kb,
+// column-major) each, staged through shared memory 64 k at a time so that
+// the reads run along the columns; slices Sa[s][i][kk]. Blocks after that: 8
+// columns of B (kb x n, column-major, a column contiguous in k) each, one
+// warp per column; slices Sb[t][j][kk]. Padding rows, columns and k are zero.
+__global__ void __launch_bounds__(256)
+oz_split_kernel(const double* __restrict__ A, long long lda, int m, const double* __restrict__ B,
+                long long ldb, int n, int kb, int kpad, int m_pad, int n_pad,
+                __nv_bfloat16* Sa, __nv_bfloat16* Sb, double* rs, double* cs) {
+  const int nrb = m_pad / 32;
+  if ((int)blockIdx.x < nrb) {
+    __shared__ unsigned long long tile[64][33];
+    __shared__ unsigned long long red[8][33];
+    __shared__ int s_e[32];
+    __shared__ int s_bad[32];
+    const int i0 = blockIdx.x * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i = i0 + tx;
+    unsigned long long km = 0ULL;
+    if (i < m)
+      for (int kk = ty; kk < kb; kk += 8) {
+        const unsigned long long key =
+            (unsigned long long)__double_as_longlong(A[i + (long long)kk * lda]) & kMagMask;
+        km = key > km ? key : km;
+      }
+    red[ty][tx] = km;
+    __syncthreads();
+    if (ty == 0) {
+      unsigned long long r = 0ULL;
+      for (int q = 0; q < 8; ++q) r = red[q][tx] > r ? red[q][tx] : r;
+      const bool bad = r >= kInfBits;
+      s_bad[tx] = bad ? 1 : 0;
+      s_e[tx] = (bad || r == 0ULL) ? 0 : oz_scale_exp(r);
+      if (i < m_pad) rs[i] = (i < m) ? oz_scale_value(r, bad) : 0.0;
     }
     __syncthreads();
     const int r = threadIdx.x >> 3, g = threadIdx.x & 7;  // row r, k group g (8 values)
-    const int e = s_e[r];
-    const bool zero = (e == INT_MIN);
-    float vals[OZ_S][8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      double y = zero ? 0.0 : ldexp(tile[g * 8 + q][r], OZ_BITS - e);
-#pragma unroll
-      for (int s = 0; s < OZ_S; ++s) {
-        const double a = trunc(y);
-        vals[s][q] = (float)a;
-        y = (y - a) * (double)(1 << OZ_BITS);
-      }
-    }
     const int row = i0 + r;
-    if (row < m_pad) {
-#pragma unroll
-      for (int s = 0; s < OZ_S; ++s) {
-        const float w = ldexpf(1.0f, -OZ_BITS * s);
-        __align__(16) __nv_bfloat16 h[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) h[q] = __float2bfloat16_rn(vals[s][q] * w);
-        *reinterpret_cast<uint4*>(Sl + ((size_t)s * m_pad + row) * kpad + k0 + g * 8) =
-            *reinterpret_cast<const uint4*>(h);
+    const int e = s_e[r];
+    const bool zero = s_bad[r] != 0;
+    for (int k0 = 0; k0 < kpad; k0 += 64) {
+      for (int q = ty; q < 64; q += 8) {
+        const int kk = k0 + q;
+        tile[q][tx] = (i < m && kk < kb)
+                          ? (unsigned long long)__double_as_longlong(A[i + (long long)kk * lda])
+                          : 0ULL;
       }
+      __syncthreads();
+      unsigned long long U[8];
+      bool neg[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const unsigned long long bits = tile[g * 8 + q][r];
+        neg[q] = (bits >> 63) != 0ULL;
+        U[q] = zero ? 0ULL : oz_fixed(bits & kMagMask, e);
+      }
+      if (row < m_pad) {
+#pragma unroll
+        for (int sl = 0; sl < OZ_S; ++sl) {
+          __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) h[q] = oz_slice_bf16(U[q], sl, neg[q]);
+          *reinterpret_cast<uint4*>(Sa + ((size_t)sl * m_pad + row) * kpad + k0 + g * 8) =
+              *reinterpret_cast<const uint4*>(h);
+        }
+      }
+      __syncthreads();
     }
-    __syncthreads();
+    return;
   }
-}
-
-// Slices of the columns of B (k x n, column-major, columns contiguous in k):
-// scale cs[j] = 2^(f_j - 26) (NaN for a non-finite column), slices
-// S[t][j][kk]. One warp per column, lane l holds k = 8l .. 8l+7.
-__global__ void __launch_bounds__(256)
-oz_split_cols_kernel(const double* __restrict__ B, long long ldb, int k, int n, int kpad,
-                     int n_pad, __nv_bfloat16* Sl, double* cs) {
-  const int j = blockIdx.x * 8 + (threadIdx.x >> 5);
+  // columns of B: one warp per column, lane l holds k = l, l+32, ...
+  const int j = ((int)blockIdx.x - nrb) * 8 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (j >= n_pad) return;
-  double x[8];
-  double mx = 0.0;
-  bool bad = false;
+  unsigned long long bits[OZ_KMAX / 32];
+  unsigned long long km = 0ULL;
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const int kk = lane * 8 + q;
-    x[q] = (j < n && kk < k) ? B[kk + (long long)j * ldb] : 0.0;
-    const double v = fabs(x[q]);
-    if (!(v <= 1.79769313486231570e308)) bad = true;
-    else mx = fmax(mx, v);
+  for (int q = 0; q < OZ_KMAX / 32; ++q) {
+    const int kk = lane + 32 * q;
+    bits[q] = (j < n && kk < kb) ? (unsigned long long)__double_as_longlong(B[kk + (long long)j * ldb]) : 0ULL;
+    const unsigned long long key = bits[q] & kMagMask;
+    km = key > km ? key : km;
   }
+#pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
-    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-    bad = __any_sync(0xffffffffu, bad);
+    const unsigned long long o = __shfl_xor_sync(0xffffffffu, km, off);
+    km = o > km ? o : km;
   }
-  int e = 0;
-  if (!bad && mx > 0.0) frexp(mx, &e);
-  if (lane == 0)
-    cs[j] = (j < n) ? (bad ? __longlong_as_double(0x7ff8000000000000LL) : ldexp(1.0, e - 26)) : 0.0;
-  if (lane * 8 >= kpad) return;
-  float vals[OZ_S][8];
+  const bool bad = km >= kInfBits;
+  const int e = (bad || km == 0ULL) ? 0 : oz_scale_exp(km);
+  if (lane == 0) cs[j] = (j < n) ? oz_scale_value(km, bad) : 0.0;
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    double y = bad ? 0.0 : ldexp(x[q], OZ_BITS - e);
+  for (int q = 0; q < OZ_KMAX / 32; ++q) {
+    const int kk = lane + 32 * q;
+    if (kk >= kpad) break;
+    const bool neg = (bits[q] >> 63) != 0ULL;
+    const unsigned long long U = bad ? 0ULL : oz_fixed(bits[q] & kMagMask, e);
 #pragma unroll
-    for (int s = 0; s < OZ_S; ++s) {
-      const double a = trunc(y);
-      vals[s][q] = (float)a;
-      y = (y - a) * (double)(1 << OZ_BITS);
-    }
-  }
-#pragma unroll
-  for (int s = 0; s < OZ_S; ++s) {
-    const float w = ldexpf(1.0f, -OZ_BITS * s);
-    __align__(16) __nv_bfloat16 h[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) h[q] = __float2bfloat16_rn(vals[s][q] * w);
-    *reinterpret_cast<uint4*>(Sl + ((size_t)s * n_pad + j) * kpad + lane * 8) =
-        *reinterpret_cast<const uint4*>(h);
+    for (int sl = 0; sl < OZ_S; ++sl) Sb[((size_t)sl * n_pad + j) * kpad + kk] = oz_slice_bf16(U, sl, neg);
   }
 }
 
@@ -429,32 +452,25 @@ inline int round_up(int x, int q) { return (x + q - 1) / q * q; }
 
 }  // namespace
 
-OzScratch& oz_scratch() {
-  static OzScratch s;
-  return s;
-}
-
 size_t oz_scratch_bytes(int m, int n, int k) {
   const size_t kp = (size_t)round_up(k < OZ_KMAX ? k : OZ_KMAX, OBK);
   const size_t mp = (size_t)round_up(m, OBM), np = (size_t)round_up(n, OBN);
   return OZ_S * (mp + np) * kp * 2 + (mp + np) * sizeof(double) + 1024;
 }
 
-bool oz_fits(int m, int n, int k) {
-  const OzScratch& s = oz_scratch();
-  return s.ptr && oz_scratch_bytes(m, n, k) <= s.bytes;
+bool oz_fits(const OzScratch& sc, int m, int n, int k) {
+  return sc.ptr && oz_scratch_bytes(m, n, k) <= sc.bytes;
 }
 
 // C (m x n) += alpha * A (m x k) * B (k x n), all FP64 column-major, through
 // the sliced BF16 product; K is taken in passes of at most 256.
-cudaError_t oz_dgemm(int m, int n, int k, double alpha, const double* A, long long lda,
-                     const double* B, long long ldb, double* C, long long ldc, int* status,
-                     cudaStream_t s) {
+cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, const double* A,
+                     long long lda, const double* B, long long ldb, double* C, long long ldc,
+                     int* status, cudaStream_t s) {
   if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
-  if (!oz_fits(m, n, k)) return cudaErrorMemoryAllocation;
+  if (!oz_fits(sc, m, n, k)) return cudaErrorMemoryAllocation;
   SL_TRY(oz_smem_once());
   const int m_pad = round_up(m, OBM), n_pad = round_up(n, OBN);
-  OzScratch& sc = oz_scratch();
   for (int k0 = 0; k0 < k; k0 += OZ_KMAX) {
     const int kb = (k - k0) < OZ_KMAX ? (k - k0) : OZ_KMAX;
     const int kpad = round_up(kb, OBK);
@@ -463,9 +479,9 @@ cudaError_t oz_dgemm(int m, int n, int k, double alpha, const double* A, long lo
     __nv_bfloat16* sb = sa + (size_t)OZ_S * m_pad * kpad;
     double* rs = reinterpret_cast<double*>(sb + (size_t)OZ_S * n_pad * kpad);
     double* cs = rs + m_pad;
-    oz_split_rows_kernel<<<m_pad / 32, 256, 0, s>>>(A + (long long)k0 * lda, lda, m, kb, kpad, m_pad,
-                                                    sa, rs);
-    oz_split_cols_kernel<<<n_pad / 8, 256, 0, s>>>(B + k0, ldb, kb, n, kpad, n_pad, sb, cs);
+    oz_split_kernel<<<m_pad / 32 + n_pad / 8, 256, 0, s>>>(A + (long long)k0 * lda, lda, m, B + k0,
+                                                          ldb, n, kb, kpad, m_pad, n_pad, sa, sb,
+                                                          rs, cs);
     CUtensorMap ta, tb;
     if (!make_slice_map(&ta, sa, OZ_S * m_pad, kpad, OBM) ||
         !make_slice_map(&tb, sb, OZ_S * n_pad, kpad, OBN))
@@ -473,7 +489,7 @@ cudaError_t oz_dgemm(int m, int n, int k, double alpha, const double* A, long lo
     const int tiles = (m_pad / OBM) * (n_pad / OBN);
     ozgemm_kernel<<<tiles, 128, oz_smem_bytes(), s>>>(ta, tb, m, n, kpad, m_pad, n_pad, rs, cs,
                                                       alpha, C, ldc, status);
-    count_launches(3);
+    count_launches(2);
     SL_TRY(cudaGetLastError());
   }
   return cudaSuccess;

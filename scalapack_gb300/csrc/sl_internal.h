@@ -47,21 +47,21 @@ struct SplitKScratch {
 };
 SplitKScratch& splitk_scratch();
 
-// Scratch of the sliced FP64 trailing update (ozgemm_f64.cu): BF16 slices of
-// both operands and their row / column scales. Grown by the library before a
-// factorization; when it is absent or too small the DMMA product is used.
+// Scratch of the sliced FP64 product (ozgemm_f64.cu): BF16 slices of both
+// operands and their row / column scales. One per stream that runs products
+// concurrently; when it is absent or too small the DMMA product is used.
 struct OzScratch {
   void* ptr = nullptr;
   size_t bytes = 0;
 };
-OzScratch& oz_scratch();
 size_t oz_scratch_bytes(int m, int n, int k);
-bool oz_fits(int m, int n, int k);
+bool oz_fits(const OzScratch& sc, int m, int n, int k);
 // C (m x n) += alpha * A (m x k) * B (k x n), FP64, column-major, on the BF16
-// tensor cores through exact 7-bit slices (needs oz_fits(m, n, k)).
-cudaError_t oz_dgemm(int m, int n, int k, double alpha, const double* A, long long lda,
-                     const double* B, long long ldb, double* C, long long ldc, int* status,
-                     cudaStream_t s);
+// tensor cores through exact 7-bit slices (needs oz_fits). B is read in full
+// (sliced) before C is written, so B may alias C.
+cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, const double* A,
+                     long long lda, const double* B, long long ldb, double* C, long long ldc,
+                     int* status, cudaStream_t s);
 // Trailing-update arithmetic of the FP64 factorization: 0 = FP64 DMMA,
 // 1 = sliced BF16 tensor-core product (when its scratch is present).
 void f64_update_set(int mode);
@@ -91,7 +91,13 @@ struct LuWork {
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_next = nullptr;
   cudaEvent_t ev_panel = nullptr;
+  // Sliced-product scratch for the caller's stream and for the panel's
+  // stream, and 64x64 FP64 blocks for the U12 solve (kDinv64Doubles).
+  OzScratch oz, oz_aux;
+  double* dinv64 = nullptr;
 };
+// Doubles of the U12 solve's diagonal-block inverses: NB <= 1024 in 64-row blocks.
+constexpr size_t kDinv64Doubles = (size_t)16 * 64 * 64;
 
 size_t panel_cand_doubles();
 // 8-byte words of the panel kernel's exchange area (2 diagonal rows of 2 x 32
