@@ -70,6 +70,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--f64-update", default="sliced", choices=["sliced", "dmma"],
                    help="trailing-update arithmetic of the FP64 factorization")
+    p.add_argument("--ozgemm", default="",
+                   help="M,N,K: time only the sliced FP64 product C += -A*B at that size "
+                        "(the kernel the profiles capture) and exit")
     p.add_argument("--mixed-n", type=int, default=32768,
                    help="size of the mixed-precision LU-IR comparison (0 disables it)")
     p.add_argument("--mixed-fmts", default="bf16x3,fp16,bf16")
@@ -608,10 +611,44 @@ def run_gpu(args):
     return 0
 
 
+def run_ozgemm(args):
+    """The sliced FP64 product alone at one size: 3 untimed and `steps` timed
+    calls of sl1x1_ozgemm_dev on device-resident U[-0.5,0.5] operands."""
+    import torch
+
+    import scalapack_gb300 as sl
+
+    m, n, k = (int(v) for v in args.ozgemm.split(","))
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev).manual_seed(args.seed)
+    A = torch.rand((k, m), dtype=torch.float64, device=dev, generator=g) - 0.5
+    B = torch.rand((n, k), dtype=torch.float64, device=dev, generator=g) - 0.5
+    C = torch.rand((n, m), dtype=torch.float64, device=dev, generator=g) - 0.5
+    call = lambda: sl.ozgemm_dev(m, n, k, -1.0, A.data_ptr(), m, B.data_ptr(), k, C.data_ptr(), m)
+    for _ in range(3):
+        assert call() == 0
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(max(1, args.steps)):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        assert call() == 0
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    ms = float(np.median(ts))
+    print(json.dumps({"ozgemm": [m, n, k], "ms": ms, "fp64_equivalent_tflops": 2 * m * n * k / ms / 1e9,
+                      "bf16_slice_tflops": 36 * 2 * m * n * k / ms / 1e9}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.ozgemm:
+        return run_ozgemm(args)
     return run_gpu(args)
 
 

@@ -290,6 +290,11 @@ void sl1x1_set_lowp_stages(int stages);
  * (sl1x1_dgetrf_noalloc) the DMMA form runs. */
 void sl1x1_set_f64_update(int mode);
 int sl1x1_get_f64_update(void);
+/* Output tiles (128 x 64) each CTA of the sliced product takes in turn
+ * (default 4; 1..4096): more overlap one tile's epilogue with the next
+ * tile's products, fewer free SMs more often for the look-ahead panel's
+ * kernels. Changes only the speed, not the results. */
+void sl1x1_set_ozgemm_tiles(int tiles_per_cta);
 /* dC (m x n) += alpha * dA (m x k) * dB (k x n), FP64, column-major device
  * arrays, through the sliced tensor-core product above (any k: passes of 256).
  * Returns 0, -i for an illegal i-th argument, <= -10000 for a CUDA error,

@@ -132,6 +132,7 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_set_lowp_stages.argtypes = [C.c_int]
     L.sl1x1_set_f64_update.argtypes = [C.c_int]
     L.sl1x1_get_f64_update.restype = C.c_int
+    L.sl1x1_set_ozgemm_tiles.argtypes = [C.c_int]
     L.sl1x1_ozgemm_dev.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, vp, C.c_longlong, vp,
                                    C.c_longlong, vp, C.c_longlong, vp]
     L.sl1x1_ozgemm_dev.restype = C.c_int

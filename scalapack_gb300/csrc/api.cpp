@@ -986,6 +986,11 @@ void sl1x1_set_f64_update(int mode) {
   sl::f64_update_set(mode);
 }
 
+void sl1x1_set_ozgemm_tiles(int tiles_per_cta) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  sl::oz_set_tiles_per_cta(tiles_per_cta);
+}
+
 int sl1x1_get_f64_update(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   return sl::f64_update_get();

@@ -33,15 +33,19 @@
 // product, and independent of the accumulation order (run to run identical).
 // Rows or columns holding Inf or NaN give NaN in their row or column of C.
 //
-// Structure (one 128 x 64 tile of C per CTA, 4 warps, one CTA per SM):
+// Structure (one CTA per SM, a few 128 x 64 tiles of C per CTA, 10 warps):
 //   * warp 0 allocates all 512 TMEM columns (6 accumulators x 64 columns);
-//   * one thread issues TMA loads: for each 64-wide k block, the eight 64x64
-//     B slices into one half of a double buffer, then the eight 128x64 A
-//     slices one at a time through a 4-deep ring (128-byte swizzle);
+//   * one thread issues TMA loads: for each 64-wide k block, the eight 128x64
+//     A slices one at a time through a 4-deep ring and the eight 64x64 B
+//     slices into one half of a double buffer, half a block ahead (128-byte
+//     swizzle);
 //   * one thread issues tcgen05.mma.kind::f16 (M=128, N=64, K=16): A slice s
 //     against B slices t <= 9 - s into accumulator min(s+t-2, 5);
-//   * all 4 warps read the accumulators with tcgen05.ld (warp w owns lanes
-//     32w..32w+31 = tile rows) and update C in place (coalesced per column).
+//   * 8 epilogue warps read the accumulators with tcgen05.ld (warp w owns
+//     lanes 32(w%4).. = tile rows, and half of the columns), combine them
+//     into integers, hand the TMEM
+//     back to the MMA thread, and update C in place (coalesced per column)
+//     while the next tile's products run.
 // Every mbarrier wait is bounded; on timeout the CTA records kFlagTimeout,
 // drains what it issued, frees its TMEM and returns.
 #include <cuda.h>
@@ -49,6 +53,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <climits>
 
 #include "common.cuh"
@@ -74,9 +79,12 @@ constexpr int GROUP_M = 8;       // tile raster: 8 row tiles sweep the columns t
 struct __align__(8) OzBars {
   uint64_t afull[A_RING], aempty[A_RING];
   uint64_t bfull[2], bempty[2];
-  uint64_t done;
+  uint64_t tfull, tempty;  // accumulators complete / drained
   uint32_t tmem_base;
 };
+
+constexpr int OZ_THREADS = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
+constexpr int OZ_EPI_WARPS = 8;  // two per TMEM lane quadrant, 32 columns each
 
 size_t oz_smem_bytes() {
   return 1024 + (size_t)A_RING * A_SLICE_BYTES + 2 * (size_t)B_CHUNK_BYTES + sizeof(OzBars) + 64;
@@ -96,10 +104,52 @@ __device__ __forceinline__ void touch16(uint32_t* r) {
                  "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]));
 }
 
-__global__ void __launch_bounds__(128, 1)
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Tile t of the grouped raster: (m0, n0).
+__device__ __forceinline__ void oz_tile(int t, int tiles_m, int tiles_n, int& m0, int& n0) {
+  const int per_group = GROUP_M * tiles_n;
+  const int gid = t / per_group, first_m = gid * GROUP_M;
+  const int gsize = min(tiles_m - first_m, GROUP_M);
+  const int in_group = t % per_group;
+  m0 = (first_m + in_group % gsize) * OBM;
+  n0 = (in_group / gsize) * OBN;
+}
+
+// The eight B slices of chunk c (tile first + c / nkc, k block c % nkc) into
+// half c & 1 of the B double buffer, once chunk c-2 has released it.
+__device__ __forceinline__ bool oz_issue_b(int c, int first, int nkc, int tiles_m, int tiles_n,
+                                           int n_pad, unsigned char* sB, const CUtensorMap* tmB,
+                                           OzBars* bars, int* issued) {
+  const int hb = c & 1;
+  if (c >= 2 && !mbar_wait(&bars->bempty[hb], ((c >> 1) - 1) & 1)) return false;
+  int m0, n0;
+  oz_tile(first + c / nkc, tiles_m, tiles_n, m0, n0);
+  const int kc = c % nkc;
+  mbar_expect_tx(&bars->bfull[hb], B_CHUNK_BYTES);
+  for (int t = 0; t < OZ_S; ++t)
+    tma_load_2d(sB + hb * B_CHUNK_BYTES + t * B_SLICE_BYTES, tmB, &bars->bfull[hb], kc * OBK,
+                t * n_pad + n0);
+  *issued = c + 1;
+  return true;
+}
+
+// CTA b takes tiles b tpc .. b tpc + tpc - 1 of the raster (a few, so that
+// SMs turn over and the panel's kernels on the high-priority stream find
+// room between them). The TMA thread runs
+// ahead through a flat sequence of k blocks ("chunks", nkc per tile): for
+// chunk c it loads the eight A slices through the ring, and after the fourth
+// of them the eight B slices of chunk c+1 into the other half of the B double
+// buffer. The MMA thread starts a tile once the epilogue has drained the
+// previous tile's accumulators (tempty); the epilogue warps drain them into
+// 32 combined integers per thread (tmem -> registers), release the TMEM, and
+// update C from registers while the next tile's products run.
+__global__ void __launch_bounds__(OZ_THREADS, 1)
 ozgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               int m, int n, int kpad, int m_pad, int n_pad, const double* __restrict__ rs,
-              const double* __restrict__ cs, double alpha, double* C, long long ldc,
+              const double* __restrict__ cs, double alpha, double* C, long long ldc, int tpc,
               int* status) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -108,25 +158,19 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
   OzBars* bars = (OzBars*)(sB + 2 * B_CHUNK_BYTES);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // grouped raster over (row tile, column tile)
   const int tiles_m = m_pad / OBM, tiles_n = n_pad / OBN;
-  const int per_group = GROUP_M * tiles_n;
-  const int gid = blockIdx.x / per_group, first_m = gid * GROUP_M;
-  const int gsize = min(tiles_m - first_m, GROUP_M);
-  const int in_group = blockIdx.x % per_group;
-  const int m0 = (first_m + in_group % gsize) * OBM;
-  const int n0 = (in_group / gsize) * OBN;
+  const int tiles = tiles_m * tiles_n;
+  const int first_tile = (int)blockIdx.x * tpc;
+  const int my_tiles = max(0, min(tpc, tiles - first_tile));
   const int nkc = kpad / OBK;
-  __shared__ int s_fail, s_issued, s_consumed, s_bissued, s_bconsumed;
+  const int total = my_tiles * nkc;  // chunks of this CTA
+  __shared__ int s_fail, s_aiss, s_acons, s_biss, s_bcons;
   // a CTA that timed out already marked the launch failed: skip the work
   if (*(volatile int*)status != 0) return;
 
   if (threadIdx.x == 0) {
     s_fail = 0;
-    s_issued = 0;
-    s_consumed = 0;
-    s_bissued = 0;
-    s_bconsumed = 0;
+    s_aiss = s_acons = s_biss = s_bcons = 0;
     for (int i = 0; i < A_RING; ++i) {
       mbar_init(&bars->afull[i], 1);
       mbar_init(&bars->aempty[i], 1);
@@ -135,7 +179,8 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
       mbar_init(&bars->bfull[i], 1);
       mbar_init(&bars->bempty[i], 1);
     }
-    mbar_init(&bars->done, 1);
+    mbar_init(&bars->tfull, 1);
+    mbar_init(&bars->tempty, OZ_EPI_WARPS);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -149,127 +194,162 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = bars->tmem_base;
 
-  if (warp == 0 && lane == 0) {
-    // TMA producer. s_issued / s_bissued count A-slice and B-chunk loads (the
-    // drain below waits for the ones never consumed).
-    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
-    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
-    for (int kc = 0; kc < nkc && !s_fail; ++kc) {
-      const int hb = kc & 1;
-      if (kc >= 2 && !mbar_wait(&bars->bempty[hb], ((kc >> 1) - 1) & 1)) {
-        atomicExch(status, (int)kFlagTimeout);
-        s_fail = 1;
-        break;
-      }
-      mbar_expect_tx(&bars->bfull[hb], B_CHUNK_BYTES);
-      for (int t = 0; t < OZ_S; ++t)
-        tma_load_2d(sB + hb * B_CHUNK_BYTES + t * B_SLICE_BYTES, &tmB, &bars->bfull[hb], kc * OBK,
-                    t * n_pad + n0);
-      s_bissued = kc + 1;
-      for (int sl = 0; sl < OZ_S; ++sl) {
-        const int g = kc * OZ_S + sl, st = g % A_RING;
-        if (g >= A_RING && !mbar_wait(&bars->aempty[st], ((g / A_RING) - 1) & 1)) {
-          atomicExch(status, (int)kFlagTimeout);
-          s_fail = 1;
-          break;
-        }
-        mbar_expect_tx(&bars->afull[st], A_SLICE_BYTES);
-        tma_load_2d(sA + st * A_SLICE_BYTES, &tmA, &bars->afull[st], kc * OBK, sl * m_pad + m0);
-        s_issued = g + 1;
-      }
-    }
-  } else if (warp == 1 && lane == 0) {
-    // MMA issuer
-    const uint32_t idesc = oz_idesc();
-    uint32_t written = 0;
-    for (int kc = 0; kc < nkc && !s_fail; ++kc) {
-      const int hb = kc & 1;
-      if (!mbar_wait(&bars->bfull[hb], (kc >> 1) & 1)) {
-        atomicExch(status, (int)kFlagTimeout);
-        s_fail = 1;
-        break;
-      }
-      s_bconsumed = kc + 1;
-      const unsigned char* bchunk = sB + hb * B_CHUNK_BYTES;
-      for (int sl = 0; sl < OZ_S; ++sl) {
-        const int g = kc * OZ_S + sl, st = g % A_RING;
-        if (!mbar_wait(&bars->afull[st], (g / A_RING) & 1)) {
-          atomicExch(status, (int)kFlagTimeout);
-          s_fail = 1;
-          break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        const unsigned char* aslice = sA + st * A_SLICE_BYTES;
-        for (int t = 0; t + sl < OZ_S; ++t) {  // s + t <= 9 (1-based)
-          const int acc = min(sl + t, OZ_NACC - 1);
-          const uint32_t dst = tmem + (uint32_t)(acc * OBN);
-#pragma unroll
-          for (int kk = 0; kk < OBK / 16; ++kk) {
-            const uint64_t ad = smem_desc_sw128(aslice + kk * 32);
-            const uint64_t bd = smem_desc_sw128(bchunk + t * B_SLICE_BYTES + kk * 32);
-            umma_f16(dst, ad, bd, idesc, (written >> acc) & 1u);
-            written |= 1u << acc;
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer ----
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
+      bool ok = total == 0 ||
+                oz_issue_b(0, first_tile, nkc, tiles_m, tiles_n, n_pad, sB, &tmB, bars, &s_biss);
+      for (int c = 0; ok && c < total; ++c) {
+        int m0, n0;
+        oz_tile(first_tile + c / nkc, tiles_m, tiles_n, m0, n0);
+        const int kc = c % nkc;
+        for (int sl = 0; ok && sl < OZ_S; ++sl) {
+          const int g = c * OZ_S + sl, st = g % A_RING;
+          if (g >= A_RING && !mbar_wait(&bars->aempty[st], ((g / A_RING) - 1) & 1)) {
+            ok = false;
+            break;
           }
+          mbar_expect_tx(&bars->afull[st], A_SLICE_BYTES);
+          tma_load_2d(sA + st * A_SLICE_BYTES, &tmA, &bars->afull[st], kc * OBK, sl * m_pad + m0);
+          s_aiss = g + 1;
+          if (sl == 3 && c + 1 < total &&
+              !oz_issue_b(c + 1, first_tile, nkc, tiles_m, tiles_n, n_pad, sB, &tmB, bars, &s_biss))
+            ok = false;
         }
-        umma_commit(&bars->aempty[st]);
-        s_consumed = g + 1;
+        if (s_fail) ok = false;
       }
-      if (s_fail) break;
-      umma_commit(&bars->bempty[hb]);
+      if (!ok) {
+        atomicExch(status, (int)kFlagTimeout);
+        s_fail = 1;
+      }
     }
-    umma_commit(&bars->done);  // arrives when every issued MMA has completed
-  }
-  __syncwarp();
-  const bool ok = mbar_wait(&bars->done, 0);
-  if (!ok) atomicExch(status, (int)kFlagTimeout);
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  __syncthreads();
-  if (ok && !s_fail) {
-    const int row = m0 + warp * 32 + lane;
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-    const double rsc = (row < m) ? alpha * rs[row] : 0.0;
-#pragma unroll 1
-    for (int c0 = 0; c0 < OBN; c0 += 16) {
-      if (n0 + c0 >= n) break;  // warp-uniform
-      uint32_t r[OZ_NACC][16];
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer ----
+      const uint32_t idesc = oz_idesc();
+      bool ok = true;
+      for (int it = 0; ok && it < my_tiles; ++it) {
+        if (it >= 1 && !mbar_wait(&bars->tempty, (it - 1) & 1)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        uint32_t written = 0;
+        for (int kc = 0; ok && kc < nkc; ++kc) {
+          const int c = it * nkc + kc, hb = c & 1;
+          if (!mbar_wait(&bars->bfull[hb], (c >> 1) & 1)) { ok = false; break; }
+          s_bcons = c + 1;
+          const unsigned char* bchunk = sB + hb * B_CHUNK_BYTES;
+          for (int sl = 0; sl < OZ_S; ++sl) {
+            const int g = c * OZ_S + sl, st = g % A_RING;
+            if (!mbar_wait(&bars->afull[st], (g / A_RING) & 1)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const unsigned char* aslice = sA + st * A_SLICE_BYTES;
+            for (int t = 0; t + sl < OZ_S; ++t) {  // s + t <= 9 (1-based)
+              const int acc = min(sl + t, OZ_NACC - 1);
+              const uint32_t dst = tmem + (uint32_t)(acc * OBN);
 #pragma unroll
-      for (int a = 0; a < OZ_NACC; ++a) tmem_ld16_nowait(trow + (uint32_t)(a * OBN + c0), r[a]);
-      tmem_ld_wait();
-#pragma unroll
-      for (int a = 0; a < OZ_NACC; ++a) touch16(r[a]);
-      const int ncol = min(16, n - (n0 + c0));
-      if (row < m) {
-        double* cbase = C + (long long)row + (long long)(n0 + c0) * ldc;
-        double cv[16], sc[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          cv[j] = (j < ncol) ? cbase[(long long)j * ldc] : 0.0;
-          sc[j] = (j < ncol) ? __ldg(cs + n0 + c0 + j) : 0.0;
+              for (int kk = 0; kk < OBK / 16; ++kk) {
+                const uint64_t ad = smem_desc_sw128(aslice + kk * 32);
+                const uint64_t bd = smem_desc_sw128(bchunk + t * B_SLICE_BYTES + kk * 32);
+                umma_f16(dst, ad, bd, idesc, (written >> acc) & 1u);
+                written |= 1u << acc;
+              }
+            }
+            umma_commit(&bars->aempty[st]);
+            s_acons = g + 1;
+          }
+          if (!ok) break;
+          umma_commit(&bars->bempty[hb]);
         }
+        if (ok) umma_commit(&bars->tfull);  // arrives when the tile's products are complete
+        if (s_fail) ok = false;
+      }
+      if (!ok) {
+        atomicExch(status, (int)kFlagTimeout);
+        s_fail = 1;
+      }
+    }
+  } else {
+    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 = tile rows,
+    // columns 32 h .. 32 h + 31 with h = (w - 2) / 4 ----
+    constexpr int EC = OBN / 2;
+    const int quad = warp & 3, half = (warp - 2) >> 2;
+    const uint32_t trow = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(half * EC);
+    for (int it = 0; it < my_tiles; ++it) {
+      if (!mbar_wait(&bars->tfull, it & 1)) {
+        if (lane == 0) {
+          atomicExch(status, (int)kFlagTimeout);
+          s_fail = 1;
+        }
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      int m0, n0;
+      oz_tile(first_tile + it, tiles_m, tiles_n, m0, n0);
+      long long I[EC];
+#pragma unroll
+      for (int c0 = 0; c0 < EC; c0 += 16) {
+        // P_d = acc_d * 2^(7(d-2)) exactly; the tail keeps 3 fraction bits.
+        // Three accumulators at a time keep the register count down.
+        uint32_t r[3][16];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) tmem_ld16_nowait(trow + (uint32_t)(a * OBN + c0), r[a]);
+        tmem_ld_wait();
+#pragma unroll
+        for (int a = 0; a < 3; ++a) touch16(r[a]);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          // P_d = acc_d * 2^(7(d-2)) exactly; the tail keeps 3 fraction bits
           const long long p2 = __float2int_rn(__uint_as_float(r[0][j]));
           const long long p3 = __float2int_rn(__uint_as_float(r[1][j]) * 128.0f);
           const long long p4 = __float2int_rn(__uint_as_float(r[2][j]) * 16384.0f);
-          const long long p5 = __float2int_rn(__uint_as_float(r[3][j]) * 2097152.0f);
-          const long long p6 = __float2int_rn(__uint_as_float(r[4][j]) * 268435456.0f);
-          const long long t8 = __float2ll_rn(__uint_as_float(r[5][j]) * 274877906944.0f);  // 2^38
-          const long long I = (p2 << 38) + (p3 << 31) + (p4 << 24) + (p5 << 17) + (p6 << 10) + t8;
-          if (j < ncol) cbase[(long long)j * ldc] = fma(rsc * sc[j], __ll2double_rn(I), cv[j]);
+          I[c0 + j] = (p2 << 38) + (p3 << 31) + (p4 << 24);
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) tmem_ld16_nowait(trow + (uint32_t)((a + 3) * OBN + c0), r[a]);
+        tmem_ld_wait();
+#pragma unroll
+        for (int a = 0; a < 3; ++a) touch16(r[a]);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const long long p5 = __float2int_rn(__uint_as_float(r[0][j]) * 2097152.0f);
+          const long long p6 = __float2int_rn(__uint_as_float(r[1][j]) * 268435456.0f);
+          const long long t8 = __float2ll_rn(__uint_as_float(r[2][j]) * 274877906944.0f);  // 2^38
+          I[c0 + j] += (p5 << 17) + (p6 << 10) + t8;
         }
       }
+      // the accumulators are in registers: the next tile's products may start
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&bars->tempty);
+      const int row = m0 + quad * 32 + lane;
+      if (row < m) {
+        const double rsc = alpha * rs[row];
+        const int nb0 = n0 + half * EC;
+        double* crow = C + (long long)row + (long long)nb0 * ldc;
+#pragma unroll
+        for (int c0 = 0; c0 < EC; c0 += 8) {
+          if (nb0 + c0 >= n) break;
+          const int ncol = min(8, n - (nb0 + c0));
+          double cv[8], sc[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            cv[j] = (j < ncol) ? crow[(long long)(c0 + j) * ldc] : 0.0;
+            sc[j] = (j < ncol) ? __ldg(cs + nb0 + c0 + j) : 0.0;
+          }
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            if (j < ncol) crow[(long long)(c0 + j) * ldc] = fma(rsc * sc[j], __ll2double_rn(I[c0 + j]), cv[j]);
+        }
+      }
+      if (s_fail) break;
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (s_fail && threadIdx.x == 0) {
-    // Drain A-slice copies that were issued but never consumed, then any B
-    // chunk still in flight (bounded waits).
-    for (int g = s_consumed; g < s_issued; ++g)
-      mbar_wait(&bars->afull[g % A_RING], (g / A_RING) & 1);
-    for (int kc = s_bconsumed; kc < s_bissued; ++kc)
-      mbar_wait(&bars->bfull[kc & 1], (kc >> 1) & 1);
+    // Drain copies that were issued but never consumed (bounded waits).
+    for (int g = s_acons; g < s_aiss; ++g) mbar_wait(&bars->afull[g % A_RING], (g / A_RING) & 1);
+    for (int c = s_bcons; c < s_biss; ++c) mbar_wait(&bars->bfull[c & 1], (c >> 1) & 1);
   }
   __syncthreads();
   if (warp == 0) {
@@ -450,7 +530,11 @@ cudaError_t oz_smem_once() {
 
 inline int round_up(int x, int q) { return (x + q - 1) / q * q; }
 
+int g_oz_tiles_per_cta = 4;
+
 }  // namespace
+
+void oz_set_tiles_per_cta(int t) { g_oz_tiles_per_cta = t < 1 ? 1 : (t > 4096 ? 4096 : t); }
 
 size_t oz_scratch_bytes(int m, int n, int k) {
   const size_t kp = (size_t)round_up(k < OZ_KMAX ? k : OZ_KMAX, OBK);
@@ -487,8 +571,13 @@ cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, con
         !make_slice_map(&tb, sb, OZ_S * n_pad, kpad, OBN))
       return cudaErrorInvalidResourceHandle;
     const int tiles = (m_pad / OBM) * (n_pad / OBN);
-    ozgemm_kernel<<<tiles, 128, oz_smem_bytes(), s>>>(ta, tb, m, n, kpad, m_pad, n_pad, rs, cs,
-                                                      alpha, C, ldc, status);
+    // a few tiles per CTA: enough to overlap one tile's epilogue with the
+    // next one's products, few enough that every SM gets work and SMs free
+    // up often
+    const int tpc = std::max(1, std::min(g_oz_tiles_per_cta, tiles / num_sms()));
+    const int grid = (tiles + tpc - 1) / tpc;
+    ozgemm_kernel<<<grid, OZ_THREADS, oz_smem_bytes(), s>>>(ta, tb, m, n, kpad, m_pad, n_pad, rs,
+                                                            cs, alpha, C, ldc, tpc, status);
     count_launches(2);
     SL_TRY(cudaGetLastError());
   }

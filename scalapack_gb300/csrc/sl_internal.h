@@ -55,6 +55,8 @@ struct OzScratch {
   size_t bytes = 0;
 };
 size_t oz_scratch_bytes(int m, int n, int k);
+// Output tiles each CTA of the sliced product takes in turn (default 4).
+void oz_set_tiles_per_cta(int t);
 bool oz_fits(const OzScratch& sc, int m, int n, int k);
 // C (m x n) += alpha * A (m x k) * B (k x n), FP64, column-major, on the BF16
 // tensor cores through exact 7-bit slices (needs oz_fits). B is read in full
