@@ -170,6 +170,7 @@ void release_all() {
   cudaFree(g_dev.dchain); cudaFree(g_dev.dsplitk); cudaFree(g_dev.daux); cudaFree(g_dev.ddinv);
   cudaFree(g_dev.dA2); cudaFree(g_dev.dX); cudaFree(g_dev.drw); cudaFree(g_dev.drc);
   cudaFree(g_dev.dipiv2); cudaFree(g_dev.doz); cudaFree(g_dev.doz2); cudaFree(g_dev.ddinv64);
+  cudaFree(g_dev.ddinvs);
   sl::splitk_scratch() = sl::SplitKScratch();
   if (g_dev.stream) cudaStreamDestroy(g_dev.stream);
   if (g_dev.aux) cudaStreamDestroy(g_dev.aux);
@@ -206,6 +207,8 @@ sl::LuWork make_work() {
   w.oz_aux.ptr = g_dev.doz2;
   w.oz_aux.bytes = g_dev.doz2 ? g_dev.capOz2 : 0;
   w.dinv64 = g_dev.ddinv64;
+  w.dinv_solve = g_dev.ddinvs;
+  w.dinv_solve_len = g_dev.ddinvs ? g_dev.capDinvs : 0;
   if (g_lookahead) {
     w.aux = g_dev.aux;
     w.ev_next = g_dev.ev_next;
@@ -217,7 +220,15 @@ sl::LuWork make_work() {
 cudaError_t ensure_solve_ws(int n, int nrhs) {
   cudaError_t e = grow(&g_dev.dperm, &g_dev.capPerm, (size_t)n);
   if (e != cudaSuccess) return e;
-  return grow(&g_dev.dbswap, &g_dev.capBs, (size_t)n * (size_t)nrhs);
+  e = grow(&g_dev.dbswap, &g_dev.capBs, (size_t)n * (size_t)nrhs);
+  if (e != cudaSuccess) return e;
+  if (sl::f64_update_get() == 1) {
+    // blocked solve with diagonal-block inverses and sliced updates (optional:
+    // without them the substitution solves run)
+    ensure_oz(n, nrhs, 128);
+    if (grow(&g_dev.ddinvs, &g_dev.capDinvs, sl::kSolveInvDoubles(n)) != cudaSuccess) cudaGetLastError();
+  }
+  return cudaSuccess;
 }
 
 // Reads the device status word and the first zero-pivot column after a

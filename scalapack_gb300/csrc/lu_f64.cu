@@ -276,6 +276,138 @@ cudaError_t gemm_update<double>(bool transa, int m, int n, int k, double alpha, 
   return dgemm(transa, m, n, k, alpha, A, lda, B, ldb, 1.0, C, ldc, s);
 }
 
+// Inverses of the 64x64 diagonal blocks of the unit-lower L (LOWER) or the
+// non-unit upper U of an n x n LU factor, for the blocked solves: block b at
+// D + b*4096, column-major with leading dimension 64 (D[c*64 + r] =
+// inv(T_bb)(r, c)); a partial last block is padded with the identity.
+// Thread t forms column t by substitution in FP64.
+template <bool LOWER>
+__global__ void __launch_bounds__(64)
+tri_inv64_kernel(int n, const double* __restrict__ A, long long lda, double* D) {
+  extern __shared__ double inv_smem[];  // Ts[64][65], X[64][65], rdiag[64]
+  double(*Ts)[65] = reinterpret_cast<double(*)[65]>(inv_smem);
+  double(*X)[65] = reinterpret_cast<double(*)[65]>(inv_smem + 64 * 65);
+  double* rd = inv_smem + 2 * 64 * 65;
+  const int b = blockIdx.x, t = threadIdx.x;
+  const int r0 = b * 64, rb = min(64, n - r0);
+  for (int c = 0; c < 64; ++c) {
+    double v = 0.0;
+    if (t < rb && c < rb && (LOWER ? c < t : c >= t)) v = A[(r0 + t) + (long long)(r0 + c) * lda];
+    Ts[t][c] = v;
+  }
+  for (int i = 0; i < 64; ++i) X[i][t] = 0.0;
+  __syncthreads();
+  if (LOWER) {
+    X[t][t] = 1.0;
+    for (int i = t + 1; i < 64; ++i) {
+      double acc = 0.0;
+      for (int q = t; q < i; ++q) acc = fma(Ts[i][q], X[q][t], acc);
+      X[i][t] = -acc;
+    }
+  } else {
+    rd[t] = (t < rb) ? 1.0 / Ts[t][t] : 1.0;
+    __syncthreads();
+    X[t][t] = rd[t];
+    for (int i = t - 1; i >= 0; --i) {
+      double acc = 0.0;
+      for (int q = i + 1; q <= t; ++q) acc = fma(Ts[i][q], X[q][t], acc);
+      X[i][t] = -acc * rd[i];
+    }
+  }
+  __syncthreads();
+  double* Db = D + (size_t)b * 4096;
+  for (int c = 0; c < 64; ++c) Db[c * 64 + t] = X[t][c];
+}
+
+// X(k0:k0+kb, c) = inv(T_bb) X(k0:k0+kb, c) for the 128-row block at k0 of
+// the unit-lower L (LOWER, forward) or the upper U (backward), from the
+// inverses of its two 64x64 diagonal blocks and its off-diagonal 64x64 block
+// read from A: one CTA per right-hand side, 128 threads.
+template <bool LOWER>
+__global__ void __launch_bounds__(128)
+diag_apply128_kernel(int kb, const double* __restrict__ A, long long lda, int k0,
+                     const double* __restrict__ D, double* X, long long ldx) {
+  __shared__ double xs[128], ys[128];
+  const int c = blockIdx.x, t = threadIdx.x;
+  double* x = X + k0 + (long long)c * ldx;
+  xs[t] = (t < kb) ? x[t] : 0.0;
+  __syncthreads();
+  const int b0 = k0 / 64;  // first 64-block
+  const int w0 = kb < 64 ? kb : 64, w1 = kb - w0;
+  const double* D0 = D + (size_t)b0 * 4096;
+  const double* D1 = D0 + 4096;
+  if (LOWER) {
+    // y0 = inv(L00) x0; x1 -= L10 y0; y1 = inv(L11) x1
+    if (t < 64) {
+      double acc = 0.0;
+      for (int i = 0; i < 64; ++i) acc = fma(D0[i * 64 + t], xs[i], acc);
+      ys[t] = acc;
+    }
+    __syncthreads();
+    if (t >= 64 && t - 64 < w1) {
+      double acc = xs[t];
+      for (int i = 0; i < w0; ++i) acc = fma(-A[(k0 + t) + (long long)(k0 + i) * lda], ys[i], acc);
+      xs[t] = acc;
+    }
+    __syncthreads();
+    if (t >= 64 && w1 > 0) {  // (no second 64-block when kb <= 64)
+      const int r = t - 64;
+      double acc = 0.0;
+      for (int i = 0; i < 64; ++i) acc = fma(D1[i * 64 + r], xs[64 + i], acc);
+      ys[t] = acc;
+    }
+  } else {
+    // y1 = inv(U11) x1; x0 -= U01 y1; y0 = inv(U00) x0
+    if (t >= 64 && w1 > 0) {
+      const int r = t - 64;
+      double acc = 0.0;
+      for (int i = 0; i < 64; ++i) acc = fma(D1[i * 64 + r], xs[64 + i], acc);
+      ys[t] = acc;
+    } else if (t >= 64) {
+      ys[t] = 0.0;
+    }
+    __syncthreads();
+    if (t < 64 && w1 > 0) {
+      double acc = xs[t];
+      for (int i = 0; i < w1; ++i) acc = fma(-A[(k0 + t) + (long long)(k0 + 64 + i) * lda], ys[64 + i], acc);
+      xs[t] = acc;
+    }
+    __syncthreads();
+    if (t < 64) {
+      double acc = 0.0;
+      for (int i = 0; i < 64; ++i) acc = fma(D0[i * 64 + t], xs[i], acc);
+      ys[t] = acc;
+    }
+  }
+  __syncthreads();
+  if (t < kb) x[t] = ys[t];
+}
+
+// Blocked NOTRAN solve with the diagonal-block inverses (ws.dinv_solve, L
+// blocks then U blocks) and the off-diagonal updates on the tensor cores:
+// 128-row blocks, each applied by inverse and then subtracted from the rest.
+static cudaError_t tri_solve_inv(bool lower, int n, int nrhs, const double* A, long long lda,
+                                 double* X, long long ldx, const LuWork& ws, cudaStream_t s) {
+  constexpr int KB = 128;
+  const int nblk = (n + KB - 1) / KB;
+  const double* D = ws.dinv_solve + (lower ? 0 : (size_t)((n + 63) / 64) * 4096);
+  for (int bi = 0; bi < nblk; ++bi) {
+    const int b = lower ? bi : nblk - 1 - bi;
+    const int k0 = b * KB, kb = (n - k0) < KB ? (n - k0) : KB;
+    if (lower) diag_apply128_kernel<true><<<nrhs, 128, 0, s>>>(kb, A, lda, k0, D, X, ldx);
+    else diag_apply128_kernel<false><<<nrhs, 128, 0, s>>>(kb, A, lda, k0, D, X, ldx);
+    count_launches(1);
+    SL_TRY(cudaGetLastError());
+    if (lower && k0 + kb < n)
+      SL_TRY(oz_dgemm(ws.oz, n - k0 - kb, nrhs, kb, -1.0, A + (k0 + kb) + (long long)k0 * lda, lda,
+                      X + k0, ldx, X + k0 + kb, ldx, ws.status, s));
+    else if (!lower && k0 > 0)
+      SL_TRY(oz_dgemm(ws.oz, k0, nrhs, kb, -1.0, A + (long long)k0 * lda, lda, X + k0, ldx, X, ldx,
+                      ws.status, s));
+  }
+  return cudaSuccess;
+}
+
 cudaError_t dgetrs_device(char trans, int n, int nrhs, const double* dA, long long ldda,
                           const int* dipiv, double* dB, long long lddb, const LuWork& ws,
                           cudaStream_t s) {
@@ -284,7 +416,27 @@ cudaError_t dgetrs_device(char trans, int n, int nrhs, const double* dA, long lo
   phase_begin(kPhSolve, s);
   SL_TRY(perm_compose(dipiv, n, ws.perm, s));
   double* X = ws.bswap;  // n x nrhs, ld = n
-  if (notran) {
+  const bool inv_path = g_f64_update == 1 && ws.dinv_solve && ws.dinv_solve_len >= kSolveInvDoubles(n) &&
+                        nrhs <= 64 && oz_fits(ws.oz, n, nrhs, 128);
+  if (notran && inv_path) {
+    SL_TRY((permute_rows<double, double>(dB, lddb, X, n, ws.perm, n, nrhs, 0, s)));
+    const int nb64 = (n + 63) / 64;
+    constexpr int kInvSmem = (2 * 64 * 65 + 64) * (int)sizeof(double);
+    static const cudaError_t a0 = cudaFuncSetAttribute(
+        tri_inv64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvSmem);
+    static const cudaError_t a1 = cudaFuncSetAttribute(
+        tri_inv64_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvSmem);
+    SL_TRY(a0);
+    SL_TRY(a1);
+    tri_inv64_kernel<true><<<nb64, 64, kInvSmem, s>>>(n, dA, ldda, ws.dinv_solve);
+    tri_inv64_kernel<false><<<nb64, 64, kInvSmem, s>>>(n, dA, ldda, ws.dinv_solve + (size_t)nb64 * 4096);
+    count_launches(2);
+    SL_TRY(cudaGetLastError());
+    SL_TRY(tri_solve_inv(true, n, nrhs, dA, ldda, X, n, ws, s));
+    SL_TRY(tri_solve_inv(false, n, nrhs, dA, ldda, X, n, ws, s));
+    SL_TRY(cudaMemcpy2DAsync(dB, lddb * sizeof(double), X, n * sizeof(double),
+                             n * sizeof(double), nrhs, cudaMemcpyDeviceToDevice, s));
+  } else if (notran) {
     SL_TRY((permute_rows<double, double>(dB, lddb, X, n, ws.perm, n, nrhs, 0, s)));
     SL_TRY(tri_solve<double>(true, false, true, n, nrhs, dA, ldda, X, n, s));
     SL_TRY(tri_solve<double>(false, false, false, n, nrhs, dA, ldda, X, n, s));

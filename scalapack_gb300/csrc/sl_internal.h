@@ -97,7 +97,12 @@ struct LuWork {
   // stream, and 64x64 FP64 blocks for the U12 solve (kDinv64Doubles).
   OzScratch oz, oz_aux;
   double* dinv64 = nullptr;
+  // Solve: inverses of the 64x64 diagonal blocks of L then of U
+  // (kSolveInvDoubles(n) doubles), or null for the substitution solves.
+  double* dinv_solve = nullptr;
+  size_t dinv_solve_len = 0;
 };
+inline size_t kSolveInvDoubles(int n) { return (size_t)2 * (size_t)((n + 63) / 64) * 64 * 64; }
 // Doubles of the U12 solve's diagonal-block inverses: NB <= 1024 in 64-row blocks.
 constexpr size_t kDinv64Doubles = (size_t)16 * 64 * 64;
 
