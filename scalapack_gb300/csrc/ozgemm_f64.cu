@@ -19,28 +19,31 @@
 // sum is an integer multiple of the diagonal's unit below 2^24. With
 // d = s + t, the update is
 //   (A B)(i,j) = 2^(e_i + f_j) sum_d 2^-7d P_d,   P_d = sum_{s+t=d} sum_k a_s b_t.
-// Diagonals d = 2..6 each get their own TMEM accumulator (exact: d <= 5 holds
-// at most 4 products; d = 6 holds 5, exact unless their sum passes 2^24, which
-// takes nearly all 1280 terms at full magnitude with one sign); d = 7..9 share
-// a sixth accumulator in plain FP32 (its rounding, 2^-24 relative to a term
-// already 2^-49 below the row and column scales, is far below FP64 rounding);
-// d >= 10 is dropped (below 2^-56 of the scales per term). 36 slice products.
+// Each diagonal d = 2..9 has its own TMEM accumulator (8 x 64 columns, all of
+// TMEM). d <= 5 holds at most 4 products: exact; d = 6 holds 5, exact unless
+// their sum passes 2^24, which takes nearly all 1280 terms at full magnitude
+// with one sign; d = 7..9 are summed in plain FP32 (their rounding, 2^-24
+// relative to terms already 2^-49 below the row and column scales, is far
+// below FP64 rounding); d >= 10 is dropped. 36 slice products, issued as 12
+// instructions per 16-wide k step: A slice s against B slices t = 0..7-s
+// (consecutive in shared memory) into accumulators s..7 (consecutive in TMEM)
+// in groups of up to 4 (N up to 256).
 //
-// Epilogue. P_2..P_6 are read back as exact integers, combined with the tail
-// into one 64-bit integer I = sum_d P_d 2^(52-7d) (|I| < 2^61), converted to
+// Epilogue. P_2..P_6 are read back as exact integers, combined with the FP32
+// sum of the tail diagonals into one 64-bit integer I = sum_d P_d 2^(52-7d) (|I| < 2^61), converted to
 // FP64 once, and C(i,j) = fma(alpha 2^(e_i+f_j-52), I, C(i,j)). The result is
 // within a few units of 2^-53 of |A(i,:)|_max |B(:,j)|_max of the exact
 // product, and independent of the accumulation order (run to run identical).
 // Rows or columns holding Inf or NaN give NaN in their row or column of C.
 //
 // Structure (one CTA per SM, a few 128 x 64 tiles of C per CTA, 10 warps):
-//   * warp 0 allocates all 512 TMEM columns (6 accumulators x 64 columns);
+//   * warp 0 allocates all 512 TMEM columns (8 accumulators x 64 columns);
 //   * one thread issues TMA loads: for each 64-wide k block, the eight 128x64
-//     A slices one at a time through a 4-deep ring and the eight 64x64 B
+//     A slices one at a time through a 6-deep ring and the eight 64x64 B
 //     slices into one half of a double buffer, half a block ahead (128-byte
 //     swizzle);
-//   * one thread issues tcgen05.mma.kind::f16 (M=128, N=64, K=16): A slice s
-//     against B slices t <= 9 - s into accumulator min(s+t-2, 5);
+//   * one thread issues tcgen05.mma.kind::f16 (M=128, N=64..256, K=16): A
+//     slice s against B slices t <= 9 - s into accumulators s+t-2;
 //   * 8 epilogue warps read the accumulators with tcgen05.ld (warp w owns
 //     lanes 32(w%4).. = tile rows, and half of the columns), combine them
 //     into integers, hand the TMEM
@@ -66,13 +69,13 @@ using namespace tc;
 
 constexpr int OZ_S = 8;          // slices per operand
 constexpr int OZ_BITS = 7;       // bits per slice
-constexpr int OZ_NACC = 6;       // accumulators: d = 2..6 exact, 7..9 tail
+constexpr int OZ_NACC = 8;       // accumulators, one per diagonal d = 2..9
 constexpr int OZ_KMAX = 256;     // exactness bound on K per pass
 constexpr int OBM = 128, OBN = 64, OBK = 64;
 constexpr int A_SLICE_BYTES = OBM * OBK * 2;          // 16 KB
 constexpr int B_SLICE_BYTES = OBN * OBK * 2;          // 8 KB
 constexpr int B_CHUNK_BYTES = OZ_S * B_SLICE_BYTES;   // 64 KB per k block
-constexpr int A_RING = 4;
+constexpr int A_RING = 6;
 constexpr int OZ_TMEM_COLS = 512;
 constexpr int GROUP_M = 8;       // tile raster: 8 row tiles sweep the columns together
 
@@ -90,10 +93,11 @@ size_t oz_smem_bytes() {
   return 1024 + (size_t)A_RING * A_SLICE_BYTES + 2 * (size_t)B_CHUNK_BYTES + sizeof(OzBars) + 64;
 }
 
-__host__ __device__ constexpr uint32_t oz_idesc() {
+// kind::f16 instruction descriptor, M = 128, N = nn (a multiple of 64 <= 256)
+__host__ __device__ constexpr uint32_t oz_idesc(int nn) {
   return (1u << 4)                       // D format: F32
          | (1u << 7) | (1u << 10)        // A, B: BF16
-         | ((uint32_t)(OBN >> 3) << 17)  // N / 8
+         | ((uint32_t)(nn >> 3) << 17)   // N / 8
          | ((uint32_t)(OBM >> 4) << 24); // M / 16
 }
 
@@ -228,12 +232,13 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
   } else if (warp == 1) {
     if (lane == 0) {
       // ---- MMA issuer ----
-      const uint32_t idesc = oz_idesc();
+      // A slice s against B slices t = 0 .. 7-s lands in accumulators s .. 7:
+      // consecutive TMEM columns and, in the B buffer, consecutive slices, so
+      // one instruction covers up to 4 of them (N up to 256).
       bool ok = true;
       for (int it = 0; ok && it < my_tiles; ++it) {
         if (it >= 1 && !mbar_wait(&bars->tempty, (it - 1) & 1)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        uint32_t written = 0;
         for (int kc = 0; ok && kc < nkc; ++kc) {
           const int c = it * nkc + kc, hb = c & 1;
           if (!mbar_wait(&bars->bfull[hb], (c >> 1) & 1)) { ok = false; break; }
@@ -244,15 +249,17 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
             if (!mbar_wait(&bars->afull[st], (g / A_RING) & 1)) { ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;");
             const unsigned char* aslice = sA + st * A_SLICE_BYTES;
-            for (int t = 0; t + sl < OZ_S; ++t) {  // s + t <= 9 (1-based)
-              const int acc = min(sl + t, OZ_NACC - 1);
-              const uint32_t dst = tmem + (uint32_t)(acc * OBN);
 #pragma unroll
-              for (int kk = 0; kk < OBK / 16; ++kk) {
-                const uint64_t ad = smem_desc_sw128(aslice + kk * 32);
-                const uint64_t bd = smem_desc_sw128(bchunk + t * B_SLICE_BYTES + kk * 32);
-                umma_f16(dst, ad, bd, idesc, (written >> acc) & 1u);
-                written |= 1u << acc;
+            for (int kk = 0; kk < OBK / 16; ++kk) {
+              const uint64_t ad = smem_desc_sw128(aslice + kk * 32);
+              // the very first products write every accumulator (s = 0 covers
+              // all eight); every later one adds
+              const uint32_t accum = (kc > 0 || sl > 0 || kk > 0) ? 1u : 0u;
+              for (int t0 = 0; t0 + sl < OZ_S; t0 += 4) {
+                const int cnt = min(4, OZ_S - sl - t0);
+                const uint32_t dst = tmem + (uint32_t)((sl + t0) * OBN);
+                const uint64_t bd = smem_desc_sw128(bchunk + t0 * B_SLICE_BYTES + kk * 32);
+                umma_f16(dst, ad, bd, oz_idesc(cnt * OBN), accum);
               }
             }
             umma_commit(&bars->aempty[st]);
@@ -289,32 +296,34 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
       long long I[EC];
 #pragma unroll
       for (int c0 = 0; c0 < EC; c0 += 16) {
-        // P_d = acc_d * 2^(7(d-2)) exactly; the tail keeps 3 fraction bits.
-        // Three accumulators at a time keep the register count down.
-        uint32_t r[3][16];
+        // P_d = acc_d * 2^(7(d-2)) exactly for d <= 6; the tail d = 7..9
+        // is summed in FP32 and keeps 3 fraction bits of P_7's unit. Four
+        // accumulators at a time keep the register count down.
+        uint32_t r[4][16];
 #pragma unroll
-        for (int a = 0; a < 3; ++a) tmem_ld16_nowait(trow + (uint32_t)(a * OBN + c0), r[a]);
+        for (int a = 0; a < 4; ++a) tmem_ld16_nowait(trow + (uint32_t)(a * OBN + c0), r[a]);
         tmem_ld_wait();
 #pragma unroll
-        for (int a = 0; a < 3; ++a) touch16(r[a]);
+        for (int a = 0; a < 4; ++a) touch16(r[a]);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const long long p2 = __float2int_rn(__uint_as_float(r[0][j]));
           const long long p3 = __float2int_rn(__uint_as_float(r[1][j]) * 128.0f);
           const long long p4 = __float2int_rn(__uint_as_float(r[2][j]) * 16384.0f);
-          I[c0 + j] = (p2 << 38) + (p3 << 31) + (p4 << 24);
+          const long long p5 = __float2int_rn(__uint_as_float(r[3][j]) * 2097152.0f);
+          I[c0 + j] = (p2 << 38) + (p3 << 31) + (p4 << 24) + (p5 << 17);
         }
 #pragma unroll
-        for (int a = 0; a < 3; ++a) tmem_ld16_nowait(trow + (uint32_t)((a + 3) * OBN + c0), r[a]);
+        for (int a = 0; a < 4; ++a) tmem_ld16_nowait(trow + (uint32_t)((a + 4) * OBN + c0), r[a]);
         tmem_ld_wait();
 #pragma unroll
-        for (int a = 0; a < 3; ++a) touch16(r[a]);
+        for (int a = 0; a < 4; ++a) touch16(r[a]);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const long long p5 = __float2int_rn(__uint_as_float(r[0][j]) * 2097152.0f);
-          const long long p6 = __float2int_rn(__uint_as_float(r[1][j]) * 268435456.0f);
-          const long long t8 = __float2ll_rn(__uint_as_float(r[2][j]) * 274877906944.0f);  // 2^38
-          I[c0 + j] += (p5 << 17) + (p6 << 10) + t8;
+          const long long p6 = __float2int_rn(__uint_as_float(r[0][j]) * 268435456.0f);
+          const float tail = (__uint_as_float(r[1][j]) + __uint_as_float(r[2][j])) + __uint_as_float(r[3][j]);
+          const long long t8 = __float2ll_rn(tail * 274877906944.0f);  // 2^38
+          I[c0 + j] += (p6 << 10) + t8;
         }
       }
       // the accumulators are in registers: the next tile's products may start
