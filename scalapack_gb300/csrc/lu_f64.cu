@@ -108,30 +108,55 @@ static cudaError_t lu_update(const OzScratch& sc, int m, int n, int k, double al
   return dgemm(false, m, n, k, alpha, A, lda, B, ldb, 1.0, C, ldc, s);
 }
 
+// Inverse of a 64x64 triangular block by column-oriented substitution, all
+// columns at once: X = I, then for each pivot row q in solve order, row q of
+// X is final (divided by T(q,q) for a non-unit upper T) and every later row
+// i loses T(i,q) X(q,:). 256 threads own 16 entries of X each, one shared
+// barrier per step: 64 steps instead of a 2000-long dependent chain.
+// Ts and X are 64 x 65 shared arrays; returns with X = inv(T).
+template <bool LOWER>
+__device__ __forceinline__ void tri_inv64_block(double (*Ts)[65], double (*X)[65], double* rd) {
+  const int t = threadIdx.x & 63, ib = threadIdx.x >> 6;  // column t, rows ib, ib+4, ...
+  if (LOWER) {
+    for (int q = 0; q < 63; ++q) {
+      const double xq = X[q][t];
+      if (t <= q)
+        for (int i = q + 1 + ((ib - (q + 1)) & 3); i < 64; i += 4) X[i][t] = fma(-Ts[i][q], xq, X[i][t]);
+      __syncthreads();
+    }
+  } else {
+    for (int q = 63; q >= 0; --q) {
+      if (threadIdx.x < 64 && t >= q) X[q][t] *= rd[q];
+      __syncthreads();
+      const double xq = X[q][t];
+      if (t >= q)
+        for (int i = ib; i < q; i += 4) X[i][t] = fma(-Ts[i][q], xq, X[i][t]);
+      __syncthreads();
+    }
+  }
+}
+
 // N_b = inv(L_bb) - I for the 64x64 diagonal blocks of the unit-lower L11
 // (jb x jb, leading dimension ldl): block b at Ninv + b*4096, column-major
 // with leading dimension 64; a partial last block is padded with the
-// identity. Thread t forms column t of the inverse by substitution in FP64.
-__global__ void __launch_bounds__(64)
+// identity.
+__global__ void __launch_bounds__(256)
 unit_lower_inv64_kernel(int jb, const double* __restrict__ L, long long ldl, double* Ninv) {
   extern __shared__ double inv_smem[];  // Ls[64][65] then X[64][65]
   double(*Ls)[65] = reinterpret_cast<double(*)[65]>(inv_smem);
   double(*X)[65] = reinterpret_cast<double(*)[65]>(inv_smem + 64 * 65);
-  const int b = blockIdx.x, t = threadIdx.x;
+  const int b = blockIdx.x;
   const int r0 = b * 64, rb = min(64, jb - r0);
-  for (int c = 0; c < 64; ++c)
-    Ls[t][c] = (t < rb && c < t) ? L[(r0 + t) + (long long)(r0 + c) * ldl] : 0.0;
-  for (int i = 0; i < 64; ++i) X[i][t] = (i == t) ? 1.0 : 0.0;
-  __syncthreads();
-  for (int i = t + 1; i < 64; ++i) {
-    double acc = 0.0;
-    for (int q = t; q < i; ++q) acc = fma(Ls[i][q], X[q][t], acc);
-    X[i][t] = -acc;
+  for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
+    const int r = idx & 63, c = idx >> 6;  // coalesced along rows
+    Ls[r][c] = (r < rb && c < r) ? L[(r0 + r) + (long long)(r0 + c) * ldl] : 0.0;
+    X[r][c] = (r == c) ? 1.0 : 0.0;
   }
   __syncthreads();
+  tri_inv64_block<true>(Ls, X, nullptr);
   double* Nb = Ninv + (size_t)b * 4096;
-  for (int q = 0; q < 64; ++q) {
-    const int i = t, c = q;  // coalesced along rows i
+  for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
+    const int i = idx & 63, c = idx >> 6;
     Nb[i + 64 * c] = (i > c) ? X[i][c] : 0.0;
   }
 }
@@ -193,7 +218,7 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
     static const cudaError_t attr = cudaFuncSetAttribute(
         unit_lower_inv64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvSmem);
     SL_TRY(attr);
-    unit_lower_inv64_kernel<<<(jb + 63) / 64, 64, kInvSmem, s>>>(jb, Ap(j, j), ldda, ws.dinv64);
+    unit_lower_inv64_kernel<<<(jb + 63) / 64, 256, kInvSmem, s>>>(jb, Ap(j, j), ldda, ws.dinv64);
     count_launches(1);
   }
   phase_end(kPhPanel, s, pflops, 16.0 * (double)(m - j) * jb);
@@ -280,43 +305,31 @@ cudaError_t gemm_update<double>(bool transa, int m, int n, int k, double alpha, 
 // non-unit upper U of an n x n LU factor, for the blocked solves: block b at
 // D + b*4096, column-major with leading dimension 64 (D[c*64 + r] =
 // inv(T_bb)(r, c)); a partial last block is padded with the identity.
-// Thread t forms column t by substitution in FP64.
 template <bool LOWER>
-__global__ void __launch_bounds__(64)
+__global__ void __launch_bounds__(256)
 tri_inv64_kernel(int n, const double* __restrict__ A, long long lda, double* D) {
   extern __shared__ double inv_smem[];  // Ts[64][65], X[64][65], rdiag[64]
   double(*Ts)[65] = reinterpret_cast<double(*)[65]>(inv_smem);
   double(*X)[65] = reinterpret_cast<double(*)[65]>(inv_smem + 64 * 65);
   double* rd = inv_smem + 2 * 64 * 65;
-  const int b = blockIdx.x, t = threadIdx.x;
+  const int b = blockIdx.x;
   const int r0 = b * 64, rb = min(64, n - r0);
-  for (int c = 0; c < 64; ++c) {
+  for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
+    const int r = idx & 63, c = idx >> 6;
     double v = 0.0;
-    if (t < rb && c < rb && (LOWER ? c < t : c >= t)) v = A[(r0 + t) + (long long)(r0 + c) * lda];
-    Ts[t][c] = v;
-  }
-  for (int i = 0; i < 64; ++i) X[i][t] = 0.0;
-  __syncthreads();
-  if (LOWER) {
-    X[t][t] = 1.0;
-    for (int i = t + 1; i < 64; ++i) {
-      double acc = 0.0;
-      for (int q = t; q < i; ++q) acc = fma(Ts[i][q], X[q][t], acc);
-      X[i][t] = -acc;
-    }
-  } else {
-    rd[t] = (t < rb) ? 1.0 / Ts[t][t] : 1.0;
-    __syncthreads();
-    X[t][t] = rd[t];
-    for (int i = t - 1; i >= 0; --i) {
-      double acc = 0.0;
-      for (int q = i + 1; q <= t; ++q) acc = fma(Ts[i][q], X[q][t], acc);
-      X[i][t] = -acc * rd[i];
-    }
+    if (r < rb && c < rb && (LOWER ? c < r : c >= r)) v = A[(r0 + r) + (long long)(r0 + c) * lda];
+    Ts[r][c] = v;
+    X[r][c] = (r == c) ? 1.0 : 0.0;
   }
   __syncthreads();
+  if (!LOWER && threadIdx.x < 64) rd[threadIdx.x] = (threadIdx.x < rb) ? 1.0 / Ts[threadIdx.x][threadIdx.x] : 1.0;
+  __syncthreads();
+  tri_inv64_block<LOWER>(Ts, X, rd);
   double* Db = D + (size_t)b * 4096;
-  for (int c = 0; c < 64; ++c) Db[c * 64 + t] = X[t][c];
+  for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
+    const int r = idx & 63, c = idx >> 6;
+    Db[c * 64 + r] = X[r][c];
+  }
 }
 
 // X(k0:k0+kb, c) = inv(T_bb) X(k0:k0+kb, c) for the 128-row block at k0 of
@@ -428,8 +441,8 @@ cudaError_t dgetrs_device(char trans, int n, int nrhs, const double* dA, long lo
         tri_inv64_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvSmem);
     SL_TRY(a0);
     SL_TRY(a1);
-    tri_inv64_kernel<true><<<nb64, 64, kInvSmem, s>>>(n, dA, ldda, ws.dinv_solve);
-    tri_inv64_kernel<false><<<nb64, 64, kInvSmem, s>>>(n, dA, ldda, ws.dinv_solve + (size_t)nb64 * 4096);
+    tri_inv64_kernel<true><<<nb64, 256, kInvSmem, s>>>(n, dA, ldda, ws.dinv_solve);
+    tri_inv64_kernel<false><<<nb64, 256, kInvSmem, s>>>(n, dA, ldda, ws.dinv_solve + (size_t)nb64 * 4096);
     count_launches(2);
     SL_TRY(cudaGetLastError());
     SL_TRY(tri_solve_inv(true, n, nrhs, dA, ldda, X, n, ws, s));

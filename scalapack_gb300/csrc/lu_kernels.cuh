@@ -438,15 +438,19 @@ laswp_kernel(T* A, long long lda, int k1, int k2, const int* __restrict__ ipiv, 
 // per panel, on the panel's stream; laswp_apply_kernel then only moves data.
 constexpr int LSW_HASH = 1024;
 static __global__ void laswp_plan_kernel(int k1, int k2, const int* __restrict__ ipiv, int* plan) {
-  __shared__ int s_row[2 * LSW_MAXP], s_src[2 * LSW_MAXP], s_tab[LSW_HASH];
+  __shared__ int s_row[2 * LSW_MAXP], s_src[2 * LSW_MAXP], s_tab[LSW_HASH], s_piv[LSW_MAXP];
   const int npiv = k2 - k1;
   for (int i = threadIdx.x; i < LSW_HASH; i += blockDim.x) s_tab[i] = -1;
-  for (int i = threadIdx.x; i < npiv; i += blockDim.x) { s_row[i] = k1 + i; s_src[i] = k1 + i; }
+  for (int i = threadIdx.x; i < npiv; i += blockDim.x) {
+    s_row[i] = k1 + i;
+    s_src[i] = k1 + i;
+    s_piv[i] = ipiv[k1 + i];  // staged: the replay below reads shared memory only
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     int cnt = npiv;
     for (int i = 0; i < npiv; ++i) {
-      const int p = ipiv[k1 + i];
+      const int p = s_piv[i];
       if (p == k1 + i) continue;
       int e;
       if (p >= k1 && p < k2) {
