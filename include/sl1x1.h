@@ -275,8 +275,8 @@ void sl1x1_set_lookahead(int on);
  * speed, not the results. */
 void sl1x1_set_panel_rows(int rows);
 /* Pipeline depth of the tcgen05 low-precision update used by the mixed
- * factorization and sl1x1_lowp_update_dev: 3 (default; one CTA per SM) or 2
- * (two CTAs per SM, one's epilogue overlapping the other's main loop). Changes
+ * factorization and sl1x1_lowp_update_dev: 2 (default; two CTAs per SM, one's
+ * epilogue overlapping the other's main loop) or 3 (one CTA per SM). Changes
  * only the speed, not the results. */
 void sl1x1_set_lowp_stages(int stages);
 /* Arithmetic of the FP64 factorization's trailing update (PDGEMM step of

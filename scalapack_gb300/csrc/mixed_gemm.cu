@@ -12,7 +12,7 @@
 // Blackwell-native structure, one 128 x 256 output tile per CTA (4 warps):
 //   * warp 0 allocates 256 TMEM columns (the FP32 accumulator, lane = row);
 //   * one thread issues TMA loads (cp.async.bulk.tensor, 128-byte swizzle) of
-//     the 128x64 A and 256x64 B k-blocks into a 3-stage shared-memory ring,
+//     the 128x64 A and 256x64 B k-blocks into a 2- or 3-stage shared-memory ring,
 //     completion tracked by mbarrier transaction counts;
 //   * one thread issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=256,
 //     K=16) per 16-wide k-slice and frees each stage with tcgen05.commit;
@@ -24,7 +24,7 @@
 //     element. When C's base or leading dimension does not meet the TMA
 //     alignment rules (16-byte base, ldc a multiple of 4) the epilogue falls
 //     back to coalesced loads and stores of C.
-// Two variants: 3 stages with one CTA per SM, or 2 stages with two CTAs per SM
+// Two variants: 2 stages with two CTAs per SM (the default), or 3 stages with one CTA per SM
 // (each holding 256 of the SM's 512 TMEM columns) so that one tile's epilogue
 // overlaps the other's main loop.
 // Every mbarrier wait is bounded; on timeout the CTA records kFlagTimeout in
@@ -381,7 +381,7 @@ bool make_map_c(CUtensorMap* map, float* C, int m, int n, long long ldc) {
   return r == CUDA_SUCCESS;
 }
 
-int g_lowp_stages = 3;  // 3: one CTA per SM; 2: two CTAs per SM
+int g_lowp_stages = 2;  // 2: two CTAs per SM (default); 3: one CTA per SM
 
 // Raises the kernel's dynamic shared-memory limit once per instantiation.
 template <int ST, int MB>
