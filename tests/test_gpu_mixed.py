@@ -141,6 +141,24 @@ def test_mixed_ir_conditioning_sweep(sl, orc, gpu_required, kappa):
             assert st["fell_back"] == 0, (fmt, st)
 
 
+def test_gmres_ir_converges_at_kappa_1e8_without_fallback(sl, orc, gpu_required):
+    # kappa = 1e8 is beyond classical refinement with BF16x3 (near-FP32) factors;
+    # GMRES-IR applies the preconditioner in FP64 vector arithmetic (double-FP32
+    # bulk products), a fixed operator, and reaches the FP64 backward error
+    # without falling back to the FP64 factorization.
+    import torch
+
+    n, nrhs = 1024, 4
+    A0 = orc.gen_conditioned(n, 1e8, nrefl=64, seed=1000)
+    B0 = orc.matgen(n, nrhs, 200, kind=0)
+    info, it, st, X, _ = _solve_ir(sl, torch, A0, B0, "bf16x3", nb=64)
+    assert info == 0
+    assert st["fell_back"] == 0, st
+    assert st["gmres_outer"] >= 1, st
+    assert st["sresid"] <= 1.0 + 1e-9, st
+    assert orc.sresid(A0, B0, X) < 16.0
+
+
 def test_mixed_ir_singular_falls_back_and_reports_info(sl, orc, gpu_required):
     import torch
     from lu_helpers import system

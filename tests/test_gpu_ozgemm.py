@@ -179,3 +179,23 @@ def test_lu_sliced_update_matches_dmma_pivots(sl, orc, torch_dev, n, nb):
         assert orc.fresid(LU, piv, A) < 16.0
     # the two factorizations agree to rounding
     assert np.max(np.abs(res[0][0] - res[1][0])) < 1e-10
+
+
+def test_tiles_per_cta_changes_only_speed(sl, torch_dev):
+    # every tile's products and epilogue are the same whichever CTA runs it
+    torch, dev = torch_dev
+    rng = np.random.default_rng(21)
+    m, n, k = 700, 500, 256
+    A = rng.uniform(-1, 1, (m, k))
+    B = rng.uniform(-1, 1, (k, n))
+    C = rng.uniform(-1, 1, (m, n))
+    L = sl.lib()
+    outs = []
+    try:
+        for t in (1, 4, 16):
+            L.sl1x1_set_ozgemm_tiles(t)
+            outs.append(run_oz(sl, torch, dev, A, B, C))
+    finally:
+        L.sl1x1_set_ozgemm_tiles(4)
+    np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
