@@ -672,11 +672,6 @@ trsv_chain_kernel(const TM* __restrict__ A, long long lda, int n, TV* X, long lo
   __shared__ TM Ds[KB][KB + 1];         // inverse of the diagonal block, Ds[r][i]
   __shared__ TM Ms[KB][KB + 1];         // M_b = inv(T_bb) T_bp, Ms[r][i]
   __shared__ TV xs[kChunk * KB][NRM];   // x of the blocks being applied
-  // FP64 vectors: the same x as FP32 pairs (hi, lo) for the bulk products,
-  // which run in double-FP32 arithmetic (exact products by FMA, compensated
-  // sums: about 2^-48 relative per term) on the FP32 pipe -- on GB300 some 70x
-  // wider than the FP64 one, which stays free for the critical-path products
-  __shared__ float2 xsf[(sizeof(TV) == 8) ? kChunk * KB : 1][NRM];
   __shared__ TV part[4][KB][NRM];       // partial sums of the 4 column groups
   __shared__ int s_b, s_fail, s_bad[kChunk];
   const uint32_t tag = (uint32_t)epoch;
@@ -732,13 +727,8 @@ trsv_chain_kernel(const TM* __restrict__ A, long long lda, int n, TV* X, long lo
     if (lane + 32 < rb) bx1 = X[(r0 + lane + 32) + (long long)warp * ldx];
   }
   TV acc[NRM];
-  float sh[NRM], slo[NRM];  // double-FP32 bulk sums (FP64 vectors only)
 #pragma unroll
-  for (int c = 0; c < NRM; ++c) {
-    acc[c] = (TV)0;
-    sh[c] = 0.f;
-    slo[c] = 0.f;
-  }
+  for (int c = 0; c < NRM; ++c) acc[c] = (TV)0;
   // Blocks 0 .. sidx-2 in solve order: chunks of the consecutive solved blocks
   // that are already published (at least the first one, waited for).
   int t = 0;
@@ -773,10 +763,6 @@ trsv_chain_kernel(const TM* __restrict__ A, long long lda, int n, TV* X, long lo
         s_bad[FORWARD ? blk : want - 1 - blk] = 1;               // solve order
       }
       xs[i][c] = v;
-      if constexpr (VW == 2) {
-        const float h = __double2float_rn((double)v);
-        xsf[i][c] = make_float2(h, __double2float_rn((double)v - (double)h));
-      }
     }
     __syncthreads();
     int av = 0;
@@ -793,43 +779,18 @@ trsv_chain_kernel(const TM* __restrict__ A, long long lda, int n, TV* X, long lo
     const int c0 = FORWARD ? 0 : (want - av) * KB;
     const int c1 = FORWARD ? min(av * KB, kn) : kn;
     if (r < rb) {
-      if constexpr (VW == 2) {
-        for (int g0 = c0 + q * 16; g0 < c1; g0 += 64) {
-          const int g1 = min(g0 + 16, c1);
-          for (int kk = g0; kk < g1; ++kk) {
-            const float a = (float)A[(r0 + r) + (long long)(k0 + kk) * lda];
+      for (int g0 = c0 + q * 16; g0 < c1; g0 += 64) {
+        const int g1 = min(g0 + 16, c1);
+        for (int kk = g0; kk < g1; ++kk) {
+          const TV a = (TV)A[(r0 + r) + (long long)(k0 + kk) * lda];
 #pragma unroll
-            for (int c = 0; c < NRM; ++c)
-              if (c < nrhs) {
-                const float2 x = xsf[kk][c];
-                const float pr = __fmul_rn(a, x.x);
-                const float pe = fmaf(a, x.x, -pr);  // a x.x = pr + pe exactly
-                const float ts = __fadd_rn(sh[c], pr);
-                const float bb = __fsub_rn(ts, sh[c]);
-                const float er = __fadd_rn(__fsub_rn(sh[c], __fsub_rn(ts, bb)), __fsub_rn(pr, bb));
-                sh[c] = ts;
-                slo[c] = __fadd_rn(slo[c], __fadd_rn(er, fmaf(a, x.y, pe)));
-              }
-          }
-        }
-      } else {
-        for (int g0 = c0 + q * 16; g0 < c1; g0 += 64) {
-          const int g1 = min(g0 + 16, c1);
-          for (int kk = g0; kk < g1; ++kk) {
-            const TV a = (TV)A[(r0 + r) + (long long)(k0 + kk) * lda];
-#pragma unroll
-            for (int c = 0; c < NRM; ++c)
-              if (c < nrhs) acc[c] = fma(a, xs[kk][c], acc[c]);
-          }
+          for (int c = 0; c < NRM; ++c)
+            if (c < nrhs) acc[c] = fma(a, xs[kk][c], acc[c]);
         }
       }
     }
     __syncthreads();
     t += av;
-  }
-  if constexpr (VW == 2) {
-#pragma unroll
-    for (int c = 0; c < NRM; ++c) acc[c] += (TV)((double)sh[c] + (double)slo[c]);
   }
 #pragma unroll
   for (int c = 0; c < NRM; ++c) part[q][r][c] = acc[c];
