@@ -249,8 +249,11 @@ long long round_ld(long long m) {
 }
 
 // ---- shared implementation of the host-ABI entry points ---------------------
+// With copy_stream set, the factors' copy back to A is only issued there (the
+// caller synchronizes it later, e.g. after running the solve beside it);
+// IPIV and INFO are always complete on return.
 int factor_host(int m, int n, double* A, int ia, int ja, const int* desca, int* ipiv,
-                cudaStream_t s, long long* ldda_out) {
+                cudaStream_t s, long long* ldda_out, cudaStream_t copy_stream) {
   const long long lld = desca[LLD_];
   const long long ldda = round_ld(m);
   const int mn = m < n ? m : n;
@@ -269,10 +272,11 @@ int factor_host(int m, int n, double* A, int ia, int ja, const int* desca, int* 
   int info = 0;
   read_factor_info(s, mn, &info);
   if (info <= -10000) return info;
-  // copy the factors and pivots back: IPIV(IA+k) = IA + p (global 1-based row)
+  // copy the factors and pivots back: IPIV(IA+k) = IA + p (global 1-based row);
+  // the factorization is complete (read_factor_info synchronized s)
   e = cudaMemcpy2DAsync(A + (ia - 1) + (long long)(ja - 1) * lld, lld * sizeof(double), g_dev.dA,
                         ldda * sizeof(double), (size_t)m * sizeof(double), n,
-                        cudaMemcpyDeviceToHost, s);
+                        cudaMemcpyDeviceToHost, copy_stream ? copy_stream : s);
   std::vector<int> hp((size_t)(mn > 0 ? mn : 1));
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(hp.data(), g_dev.dipiv, (size_t)mn * sizeof(int), cudaMemcpyDeviceToHost, s);
@@ -323,7 +327,7 @@ void pdgetrf_(const int* M, const int* N, double* A, const int* IA, const int* J
   if (DESCA[M_] == 1) { IPIV[0] = 1; return; }
   if (*M == 0 || *N == 0) return;
   if (!ensure_device()) { *INFO = cuda_info(cudaErrorNoDevice); return; }
-  *INFO = factor_host(*M, *N, A, *IA, *JA, DESCA, IPIV, g_dev.stream, nullptr);
+  *INFO = factor_host(*M, *N, A, *IA, *JA, DESCA, IPIV, g_dev.stream, nullptr, nullptr);
 }
 
 // ---------------------------------------------------------------- PDGETRS
@@ -454,11 +458,21 @@ void pdgesv_(const int* N, const int* NRHS, double* A, const int* IA, const int*
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) { *INFO = cuda_info(e); return; }
   } else {
-    *INFO = factor_host(n, n, A, ia, ja, DESCA, IPIV, g_dev.stream, &ldda);
+    // the factors go back to A on the second stream while the solve runs
+    *INFO = factor_host(n, n, A, ia, ja, DESCA, IPIV, g_dev.stream, &ldda, g_dev.aux);
   }
-  if (*INFO != 0) return;  // singular (or GPU failure): the solve is skipped (pdgesv.f:231)
-  if (nrhs == 0) return;
+  auto join_copy = [&]() {
+    if (DESCA[M_] != 1) {
+      cudaError_t e = cudaStreamSynchronize(g_dev.aux);
+      if (e != cudaSuccess && *INFO == 0) *INFO = cuda_info(e);
+    }
+  };
+  if (*INFO != 0 || nrhs == 0) {  // singular (or GPU failure): the solve is skipped (pdgesv.f:231)
+    join_copy();
+    return;
+  }
   *INFO = solve_host('N', n, nrhs, ldda, B, ib, jb, DESCB, g_dev.stream);
+  join_copy();
 }
 
 // ---------------------------------------------------------------- TOOLS

@@ -97,7 +97,7 @@ int read_factor_info(cudaStream_t s, int mn, int* out_info);
 long long round_ld(long long m);
 // Stages sub(A) into g_dev.dA, factors it, copies L\U and IPIV back.
 int factor_host(int m, int n, double* A, int ia, int ja, const int* desca, int* ipiv,
-                cudaStream_t s, long long* ldda_out);
+                cudaStream_t s, long long* ldda_out, cudaStream_t copy_stream = nullptr);
 
 // Grows a library-owned device buffer to at least `need` elements.
 template <class T>
