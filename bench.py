@@ -174,10 +174,19 @@ def cpu_solve_sample(A, B, nb, budget_s=25.0):
     t = time.perf_counter()
     LU, ipiv, X, info = orc.solve_reference(a, b, nb=nb)
     dt = time.perf_counter() - t
+    # second CPU reference: the host LAPACK's own dgetrf + dgetrs on the same sample
+    a = np.asfortranarray(A[:n, :n].copy())
+    b = np.asfortranarray(B[:n, :].copy())
+    t = time.perf_counter()
+    orc.lapack_dgesv(a, b)
+    dl = time.perf_counter() - t
     return {"value": flops_lu(n) / dt / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
             "sample": f"oracle PDGESV restatement (OpenBLAS, {cores} threads), N={n} NB={nb} "
                       f"NRHS={B.shape[1]}, one solve of {dt:.2f} s",
-            "blas_loaded": orc.blas_loaded(), "seconds": dt, "n": n}
+            "blas_loaded": orc.blas_loaded(), "seconds": dt, "n": n,
+            "host_lapack": {"value": flops_lu(n) / dl / 1e12, "unit": "TFLOP/s", "seconds": dl,
+                            "sample": f"host LAPACK dgetrf + dgetrs (OpenBLAS, {cores} threads) "
+                                      f"on the same N={n} sample"}}
 
 
 def torch_sresid(torch, A, B, X):
@@ -400,7 +409,8 @@ def run_reference(args):
         "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": cores, "kind": "port",
                          "sample": f"oracle PDGESV restatement on host BLAS (OpenBLAS, {cores} "
                                    f"threads), N={n} NB={args.nb} NRHS={args.nrhs} per step; the "
-                                   "Fortran/MPI reference cannot be compiled here"},
+                                   "Fortran/MPI reference cannot be compiled here",
+                         "host_lapack": probe.get("host_lapack")},
         "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -184,6 +184,18 @@ def lapack_dgetrf(A):
     return A, ipiv, info
 
 
+def lapack_dgesv(A, B):
+    """Host LAPACK dgetrf + dgetrs (the BLAS library's own LU, not the
+    restatement), in place on Fortran-ordered A and B. Returns (ipiv, info)."""
+    assert A.flags.f_contiguous and B.flags.f_contiguous
+    n = A.shape[0]
+    ipiv = np.zeros(n, dtype=np.int32)
+    info = lib().orc_lapack_dgetrf(n, n, _p(A), A.shape[0], _p(ipiv))
+    if info == 0:
+        lib().orc_lapack_dgetrs(b"N", n, B.shape[1], _p(A), A.shape[0], _p(ipiv), _p(B), B.shape[0])
+    return ipiv, info
+
+
 def dgemm(ta, tb, alpha, a, b, beta, c):
     m = c.shape[0]
     n = c.shape[1]
