@@ -183,6 +183,22 @@ def test_config_n2048_nb64(sl, orc, ctx):
     assert orc.sresid(A0, B0, X) < RESID_THRESH
 
 
+def test_config_n16384_nb256_full_size(sl, orc, ctx):
+    # The headline case at full size: plain FP64 PDGESV, N=16384, NB=256,
+    # NRHS=16, U[-0.5,0.5] from the tester's seeded generator. IPIV against
+    # the oracle's pdgetrf (all host cores), then both scaled residuals.
+    n, nb, nrhs = 16384, 256, 16
+    orc.set_threads(os.cpu_count() or 1)
+    A0, B0 = system(orc, n, nrhs)
+    info, LU, rel, X = run_pdgesv(sl, ctx, A0, B0, nb)
+    assert info == 0
+    bad, ties = compare_ipiv(orc, A0, rel, nb)
+    print(f"N={n}: {bad} pivot mismatches outside near ties; logged tie columns {ties}")
+    assert bad == 0, ties
+    assert orc.sresid(A0, B0, X) < RESID_THRESH
+    assert orc.fresid(LU, rel, A0) < RESID_THRESH
+
+
 @pytest.mark.parametrize("norm", ["M", "1", "O", "I", "F", "E"])
 def test_pdlange_norms(sl, orc, ctx, norm):
     m, n = 300, 170
