@@ -272,15 +272,19 @@ int factor_host(int m, int n, double* A, int ia, int ja, const int* desca, int* 
   int info = 0;
   read_factor_info(s, mn, &info);
   if (info <= -10000) return info;
-  // copy the factors and pivots back: IPIV(IA+k) = IA + p (global 1-based row);
-  // the factorization is complete (read_factor_info synchronized s)
-  e = cudaMemcpy2DAsync(A + (ia - 1) + (long long)(ja - 1) * lld, lld * sizeof(double), g_dev.dA,
-                        ldda * sizeof(double), (size_t)m * sizeof(double), n,
-                        cudaMemcpyDeviceToHost, copy_stream ? copy_stream : s);
+  // copy the pivots and factors back: IPIV(IA+k) = IA + p (global 1-based row);
+  // the factorization is complete (read_factor_info synchronized s). The
+  // pivots come first: a small device-to-host copy issued after the factors'
+  // would wait behind them for the copy engine, and so would the caller's
+  // solve on s.
   std::vector<int> hp((size_t)(mn > 0 ? mn : 1));
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(hp.data(), g_dev.dipiv, (size_t)mn * sizeof(int), cudaMemcpyDeviceToHost, s);
+  e = cudaMemcpyAsync(hp.data(), g_dev.dipiv, (size_t)mn * sizeof(int), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(A + (ia - 1) + (long long)(ja - 1) * lld, lld * sizeof(double), g_dev.dA,
+                          ldda * sizeof(double), (size_t)m * sizeof(double), n,
+                          cudaMemcpyDeviceToHost, copy_stream ? copy_stream : s);
+  if (e == cudaSuccess && !copy_stream) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_info(e);
   for (int k = 0; k < mn; ++k) ipiv[ia - 1 + k] = ia + hp[k];
   if (ldda_out) *ldda_out = ldda;
