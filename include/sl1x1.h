@@ -268,6 +268,12 @@ void sl1x1_set_default_nb(int nb);
 /* Look-ahead in the factorizations (default on): the next panel is factored
  * on a second stream while the trailing update runs. Same results either way. */
 void sl1x1_set_lookahead(int on);
+/* Column chunks of A's host-to-device copy in pdgetrf_ / pdgesv_ (1..16,
+ * default 8; 1 = one copy before the factorization): with more than one, A
+ * goes over in chunks of whole panels on a copy stream and step 0 of the
+ * factorization (panel 0, then its interchanges, U12 solve and update chunk by
+ * chunk) starts as soon as its columns are in place. Same results either way. */
+void sl1x1_set_copy_chunks(int chunks);
 /* Smallest row slice per CTA of the cooperative panel kernel (8..768; 0, the
  * default, picks 256 rows for the FP32 panel and 128 for the FP64 one, with
  * about 64 CTAs for tall panels): larger slices mean fewer CTAs in each

@@ -128,6 +128,7 @@ void chk1mat(int ma, int mapos0, int na, int napos0, int ia, int ja, const int* 
 DevState g_dev;
 int g_default_nb = 256;
 bool g_lookahead = true;
+int g_copy_chunks = 8;  // column chunks of A's host-to-device copy (<= 1: one copy)
 
 int cuda_info(cudaError_t e) { return -10000 - (int)e; }
 
@@ -151,6 +152,10 @@ bool ensure_device() {
     if (cudaStreamCreateWithPriority(&g_dev.aux, cudaStreamNonBlocking, hi) != cudaSuccess) return false;
     if (cudaEventCreateWithFlags(&g_dev.ev_next, cudaEventDisableTiming) != cudaSuccess) return false;
     if (cudaEventCreateWithFlags(&g_dev.ev_panel, cudaEventDisableTiming) != cudaSuccess) return false;
+    if (cudaStreamCreateWithFlags(&g_dev.h2d, cudaStreamNonBlocking) != cudaSuccess) return false;
+    if (cudaEventCreateWithFlags(&g_dev.ev_h2d, cudaEventDisableTiming) != cudaSuccess) return false;
+    for (cudaEvent_t& ev : g_dev.ev_cols)
+      if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return false;
   }
   if (cudaMalloc(&g_dev.dsmall, 16 * sizeof(int)) != cudaSuccess) return false;
   if (cudaMalloc(&g_dev.dcand, sl::panel_cand_doubles() * sizeof(double)) != cudaSuccess) return false;
@@ -176,6 +181,10 @@ void release_all() {
   if (g_dev.aux) cudaStreamDestroy(g_dev.aux);
   if (g_dev.ev_next) cudaEventDestroy(g_dev.ev_next);
   if (g_dev.ev_panel) cudaEventDestroy(g_dev.ev_panel);
+  if (g_dev.h2d) cudaStreamDestroy(g_dev.h2d);
+  if (g_dev.ev_h2d) cudaEventDestroy(g_dev.ev_h2d);
+  for (cudaEvent_t ev : g_dev.ev_cols)
+    if (ev) cudaEventDestroy(ev);
   g_dev = DevState();
 }
 
@@ -188,7 +197,8 @@ void ensure_oz(int m, int n, int nb) {
   if (need > g_dev.capOz || !g_dev.doz) e = grow(&g_dev.doz, &g_dev.capOz, need);
   if (e == cudaSuccess && (need2 > g_dev.capOz2 || !g_dev.doz2))
     e = grow(&g_dev.doz2, &g_dev.capOz2, need2);
-  if (e == cudaSuccess && !g_dev.ddinv64) e = cudaMalloc(&g_dev.ddinv64, sl::kDinv64Doubles * sizeof(double));
+  if (e == cudaSuccess && !g_dev.ddinv64)
+    e = cudaMalloc(&g_dev.ddinv64, 2 * sl::kDinv64Doubles * sizeof(double));
   if (e != cudaSuccess) cudaGetLastError();  // the DMMA update covers what is missing
 }
 
@@ -207,6 +217,7 @@ sl::LuWork make_work() {
   w.oz_aux.ptr = g_dev.doz2;
   w.oz_aux.bytes = g_dev.doz2 ? g_dev.capOz2 : 0;
   w.dinv64 = g_dev.ddinv64;
+  w.dinv64_step0 = g_dev.ddinv64 ? g_dev.ddinv64 + sl::kDinv64Doubles : nullptr;
   w.dinv_solve = g_dev.ddinvs;
   w.dinv_solve_len = g_dev.ddinvs ? g_dev.capDinvs : 0;
   if (g_lookahead) {
@@ -261,12 +272,47 @@ int factor_host(int m, int n, double* A, int ia, int ja, const int* desca, int* 
   if (e == cudaSuccess) e = grow(&g_dev.dipiv, &g_dev.capP, (size_t)(mn > 0 ? mn : 1));
   if (e != cudaSuccess) return cuda_info(e);
   const double* src = A + (ia - 1) + (long long)(ja - 1) * lld;
-  e = cudaMemcpy2DAsync(g_dev.dA, ldda * sizeof(double), src, lld * sizeof(double),
-                        (size_t)m * sizeof(double), n, cudaMemcpyHostToDevice, s);
-  if (e != cudaSuccess) return cuda_info(e);
   ensure_oz(m, n, desca[NB_]);
+  // With the look-ahead on and more than two panels, A goes over in column
+  // chunks of about n/g_copy_chunks (whole panels, the first holding panels 0
+  // and 1) on the copy stream, and step 0 of the factorization follows them.
+  const int nbk = desca[NB_] < 1024 ? desca[NB_] : 1024;
+  int col_end[sl::kMaxColChunks];
+  int nck = 0;
+  if (g_copy_chunks > 1 && g_lookahead && nbk > 0 && mn > 2 * nbk) {
+    const long long per = ((long long)n + g_copy_chunks - 1) / g_copy_chunks;
+    long long w = (per + nbk - 1) / nbk * nbk;
+    if (w < 2LL * nbk) w = 2LL * nbk;
+    e = cudaEventRecord(g_dev.ev_h2d, s);  // dA is free once s's earlier work is done
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(g_dev.h2d, g_dev.ev_h2d, 0);
+    for (long long a = 0; e == cudaSuccess && a < n; a += w) {
+      const long long b = (a + w >= n || nck == sl::kMaxColChunks - 1) ? n : a + w;
+      e = cudaMemcpy2DAsync(g_dev.dA + a * ldda, ldda * sizeof(double), src + a * lld,
+                            lld * sizeof(double), (size_t)m * sizeof(double), (size_t)(b - a),
+                            cudaMemcpyHostToDevice, g_dev.h2d);
+      if (e == cudaSuccess) e = cudaEventRecord(g_dev.ev_cols[nck], g_dev.h2d);
+      col_end[nck++] = (int)b;
+      if (b == n) break;
+    }
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(g_dev.h2d);
+      return cuda_info(e);
+    }
+  } else {
+    e = cudaMemcpy2DAsync(g_dev.dA, ldda * sizeof(double), src, lld * sizeof(double),
+                          (size_t)m * sizeof(double), n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_info(e);
+  }
   sl::LuWork w = make_work();
+  w.ncol_chunks = nck;
+  w.col_end = col_end;
+  w.ev_cols = g_dev.ev_cols;
   e = sl::dgetrf_device(m, n, g_dev.dA, ldda, g_dev.dipiv, desca[NB_], w, s);
+  // (every chunk has been waited for on s unless the factorization stopped early)
+  if (nck > 0) {
+    const cudaError_t e2 = cudaStreamSynchronize(g_dev.h2d);
+    if (e == cudaSuccess) e = e2;
+  }
   if (e == cudaErrorInvalidValue) return -30000;
   if (e != cudaSuccess) return cuda_info(e);
   int info = 0;
@@ -998,6 +1044,11 @@ void sl1x1_finalize(void) {
 void sl1x1_set_lookahead(int on) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_lookahead = (on != 0);
+}
+
+void sl1x1_set_copy_chunks(int chunks) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_copy_chunks = chunks < 1 ? 1 : (chunks > sl::kMaxColChunks ? sl::kMaxColChunks : chunks);
 }
 
 void sl1x1_set_panel_rows(int rows) {

@@ -27,6 +27,8 @@ struct DevState {
   cudaStream_t stream = nullptr;
   cudaStream_t aux = nullptr;       // look-ahead stream (higher priority)
   cudaEvent_t ev_next = nullptr, ev_panel = nullptr;
+  cudaStream_t h2d = nullptr;       // host-to-device copies of A in column chunks
+  cudaEvent_t ev_h2d = nullptr, ev_cols[sl::kMaxColChunks] = {};
   double* dA = nullptr; size_t capA = 0;
   double* dB = nullptr; size_t capB = 0;
   int* dipiv = nullptr; size_t capP = 0;
@@ -54,7 +56,7 @@ struct DevState {
   double* daux = nullptr; size_t capAux = 0;
   unsigned char* doz = nullptr; size_t capOz = 0;    // sliced-product scratch, caller's stream (bytes)
   unsigned char* doz2 = nullptr; size_t capOz2 = 0;  // sliced-product scratch, panel stream (bytes)
-  double* ddinv64 = nullptr;                          // U12 solve: inverses of L11's 64x64 blocks
+  double* ddinv64 = nullptr;  // U12 solve: inverses of L11's 64x64 blocks, then a copy for step 0
   double* ddinvs = nullptr; size_t capDinvs = 0;      // solve: inverses of the diagonal blocks
   int chain_epoch = 0;
   unsigned short* dA16 = nullptr; size_t capA16 = 0;

@@ -225,12 +225,79 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
   return cudaSuccess;
 }
 
+// Step 0 of the right-looking loop while the columns arrive in chunks (see
+// dgetrf_device; m, n > 2 nb, panel 0 factored): the next panel's columns
+// first, then the look-ahead panel on ws.aux, then the remaining columns of
+// each chunk once it has landed.
+template <typename WaitCols>
+static cudaError_t step0_by_chunks(int m, int n, double* dA, long long ldda, int* dipiv, int nb,
+                                   const LuWork& ws, cudaStream_t s, WaitCols& wait_cols) {
+  auto Ap = [&](long long i, long long c) { return dA + i + c * ldda; };
+  const int mn = m < n ? m : n;
+  const int jb = nb, jn = nb;
+  const int jb2 = (mn - jn) < nb ? (mn - jn) : nb;
+  // step 0 on columns [c0, c1): interchanges, U12 solve, trailing update
+  auto step_cols = [&](int c0, int c1, bool planned, const LuWork& w) -> cudaError_t {
+    if (c1 <= c0) return cudaSuccess;
+    const int nc = c1 - c0;
+    phase_begin(kPhLaswp, s);
+    if (planned) SL_TRY(laswp_planned<double>(dA, ldda, 0, jb, dipiv, w.swap_plan, 0, 0, c0, c1, s));
+    else SL_TRY(laswp<double>(dA, ldda, 0, jb, dipiv, 0, 0, c0, c1, s));
+    phase_end(kPhLaswp, s, 0.0, 32.0 * jb * (double)nc);
+    phase_begin(kPhTrsm, s);
+    SL_TRY(solve_u12(jb, nc, Ap(0, 0), ldda, Ap(0, c0), ldda, w, s));
+    phase_end(kPhTrsm, s, (double)jb * jb * nc, 8.0 * (0.5 * jb * jb + 2.0 * jb * nc));
+    if (jn < m) {
+      const double mr = (double)(m - jn);
+      phase_begin(kPhGemm, s);
+      SL_TRY(lu_update(w.oz, m - jn, nc, jb, -1.0, Ap(jn, 0), ldda, Ap(0, c0), ldda, Ap(jn, c0),
+                       ldda, w, s));
+      phase_end(kPhGemm, s, 2.0 * mr * nc * jb, 8.0 * (mr * jb + (double)jb * nc + 2.0 * mr * nc));
+    }
+    return cudaSuccess;
+  };
+  SL_TRY(wait_cols(jn + jb2));
+  SL_TRY(step_cols(jn, jn + jb2, true, ws));
+  // the look-ahead panel rewrites the interchange plan and ws.dinv64: the
+  // rest of step 0 reads dipiv and a copy of panel 0's inverses instead
+  LuWork w0 = ws;
+  w0.swap_plan = nullptr;
+  if (g_f64_update == 1 && ws.dinv64) {
+    SL_TRY(cudaMemcpyAsync(ws.dinv64_step0, ws.dinv64, (size_t)((jb + 63) / 64) * 4096 * sizeof(double),
+                           cudaMemcpyDeviceToDevice, s));
+    w0.dinv64 = ws.dinv64_step0;
+  }
+  SL_TRY(cudaEventRecord(ws.ev_next, s));
+  SL_TRY(cudaStreamWaitEvent(ws.aux, ws.ev_next, 0));
+  SL_TRY(factor_panel(m, dA, ldda, dipiv, jn, jb2, ws, ws.aux));
+  SL_TRY(cudaEventRecord(ws.ev_panel, ws.aux));
+  const int nck = ws.ncol_chunks < kMaxColChunks ? ws.ncol_chunks : kMaxColChunks;
+  for (int c = 0; c < nck; ++c) {
+    const int lo = c ? ws.col_end[c - 1] : 0, hi = ws.col_end[c];
+    const int a = lo > jn + jb2 ? lo : jn + jb2, b = hi < n ? hi : n;
+    if (b <= a) continue;
+    SL_TRY(wait_cols(b));
+    SL_TRY(step_cols(a, b, false, w0));
+  }
+  return wait_cols(INT_MAX);
+}
+
 // Right-looking blocked LU. With look-ahead resources in `ws`, the panel of
 // step j+1 is factored on ws.aux while the trailing update of step j runs on
 // s: the columns of the next panel are updated first (event ev_next), the
 // next panel starts as soon as they are ready, and step j+1 waits for it
 // (event ev_panel). Panel and update touch disjoint columns, and each element
 // is accumulated in the same order either way, so the factors are the same.
+//
+// With columns still arriving (ws.ncol_chunks > 0), s waits for each column
+// chunk just before the first operation on it: panel 0 starts when its
+// columns are in place, and step 0's interchanges, U12 solve and update run
+// chunk by chunk as the rest lands. Every one of those operations is
+// independent per column, so the factors are bitwise those of the whole-width
+// step. After the look-ahead panel is launched the step-0 operations must not
+// read the per-panel scratch that panel overwrites (the interchange plan and
+// L11's block inverses): they take the interchanges from dipiv and a copy of
+// the inverses (ws.dinv64_step0).
 cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, int nb,
                           const LuWork& ws, cudaStream_t s) {
   SL_TRY(cudaMemsetAsync(ws.status, 0, sizeof(int), s));
@@ -239,9 +306,26 @@ cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, 
   if (nb > 1024) nb = 1024;
   auto Ap = [&](long long i, long long j) { return dA + i + j * ldda; };
   const bool lookahead = ws.aux && ws.ev_next && ws.ev_panel && mn > 2 * nb;
+  // column chunks: s waits for every chunk that starts below column `upto`
+  const int nck = (ws.ncol_chunks > 0 && ws.col_end && ws.ev_cols)
+                      ? (ws.ncol_chunks < kMaxColChunks ? ws.ncol_chunks : kMaxColChunks) : 0;
+  int next_chunk = 0;
+  auto wait_cols = [&](int upto) -> cudaError_t {
+    while (next_chunk < nck && (next_chunk ? ws.col_end[next_chunk - 1] : 0) < upto) {
+      SL_TRY(cudaStreamWaitEvent(s, ws.ev_cols[next_chunk], 0));
+      ++next_chunk;
+    }
+    return cudaSuccess;
+  };
+  const bool stream_step0 = nck > 0 && lookahead && ws.dinv64_step0 && ws.col_end[nck - 1] >= n;
+  SL_TRY(wait_cols(stream_step0 ? nb : INT_MAX));
   if (mn > 0) SL_TRY(factor_panel(m, dA, ldda, dipiv, 0, (mn < nb ? mn : nb), ws, s));
   bool panel_on_aux = false;
-  for (int j = 0; j < mn; j += nb) {
+  if (stream_step0) {
+    SL_TRY(step0_by_chunks(m, n, dA, ldda, dipiv, nb, ws, s, wait_cols));
+    panel_on_aux = true;
+  }
+  for (int j = stream_step0 ? nb : 0; j < mn; j += nb) {
     const int jb = (mn - j) < nb ? (mn - j) : nb;
     if (panel_on_aux) SL_TRY(cudaStreamWaitEvent(s, ws.ev_panel, 0));
     panel_on_aux = false;

@@ -101,7 +101,18 @@ struct LuWork {
   // (kSolveInvDoubles(n) doubles), or null for the substitution solves.
   double* dinv_solve = nullptr;
   size_t dinv_solve_len = 0;
+  // Columns still arriving (ncol_chunks = 0: all of A is in place). Chunk c
+  // holds columns [c ? col_end[c-1] : 0, col_end[c]) and is in place once
+  // ev_cols[c] has completed; step 0 of the factorization follows the chunks
+  // (needs the look-ahead resources and dinv64_step0, a second
+  // kDinv64Doubles block; otherwise the factorization waits for all of them).
+  int ncol_chunks = 0;
+  const int* col_end = nullptr;
+  const cudaEvent_t* ev_cols = nullptr;
+  double* dinv64_step0 = nullptr;
 };
+// Most column chunks a streamed factorization takes.
+constexpr int kMaxColChunks = 16;
 inline size_t kSolveInvDoubles(int n) { return (size_t)2 * (size_t)((n + 63) / 64) * 64 * 64; }
 // Doubles of the U12 solve's diagonal-block inverses: NB <= 1024 in 64-row blocks.
 constexpr size_t kDinv64Doubles = (size_t)16 * 64 * 64;

@@ -183,6 +183,42 @@ def test_config_n2048_nb64(sl, orc, ctx):
     assert orc.sresid(A0, B0, X) < RESID_THRESH
 
 
+@pytest.mark.parametrize("m,n,nb", [(2048, 2048, 64), (1000, 1000, 64), (3000, 3000, 256),
+                                    (1500, 900, 64), (700, 1300, 64), (600, 600, 256)])
+def test_host_path_chunked_copy_bitwise(sl, orc, ctx, m, n, nb):
+    # pdgetrf_ / pdgesv_ copy A to the GPU in column chunks and run step 0 of
+    # the factorization chunk by chunk as they land; the device entry points
+    # get A whole. Every step-0 operation is per column, so factors, pivots
+    # and solution must be bitwise the same.
+    import torch
+
+    rng = np.random.default_rng(m * 7 + n + nb)
+    A0 = np.asfortranarray(rng.uniform(-0.5, 0.5, (m, n)))
+    dA = torch.from_numpy(np.ascontiguousarray(A0.T)).cuda()
+    mn = min(m, n)
+    dpiv = torch.zeros(mn, dtype=torch.int32, device="cuda")
+    assert sl.dgetrf_dev(m, n, dA.data_ptr(), m, dpiv.data_ptr(), nb) == 0
+    LU_dev = np.asfortranarray(dA.cpu().numpy().T)
+    piv_dev = dpiv.cpu().numpy()  # 1-based, as LAPACK's
+    LU = np.asfortranarray(A0.copy())
+    desca = np.array([1, ctx, m, n, nb, nb, 0, 0, m], np.int32)
+    ipiv = np.zeros(m + nb, np.int32)
+    assert sl.pdgetrf(m, n, LU, 1, 1, desca, ipiv) == 0
+    np.testing.assert_array_equal(ipiv[:mn], piv_dev)
+    np.testing.assert_array_equal(LU, LU_dev)
+    if m == n:
+        B0 = np.asfortranarray(rng.uniform(-0.5, 0.5, (n, 3)))
+        dA = torch.from_numpy(np.ascontiguousarray(A0.T)).cuda()
+        dB = torch.from_numpy(np.ascontiguousarray(B0.T)).cuda()
+        assert sl.dgesv_dev(n, 3, dA.data_ptr(), n, dpiv.data_ptr(), dB.data_ptr(), n, nb) == 0
+        X_dev = np.asfortranarray(dB.cpu().numpy().T)
+        LU2, X = np.asfortranarray(A0.copy()), np.asfortranarray(B0.copy())
+        descb = np.array([1, ctx, n, 3, nb, nb, 0, 0, n], np.int32)
+        assert sl.pdgesv(n, 3, LU2, 1, 1, desca, ipiv, X, 1, 1, descb) == 0
+        np.testing.assert_array_equal(LU2, LU_dev)
+        np.testing.assert_array_equal(X, X_dev)
+
+
 def test_config_n16384_nb256_full_size(sl, orc, ctx):
     # The headline case at full size: plain FP64 PDGESV, N=16384, NB=256,
     # NRHS=16, U[-0.5,0.5] from the tester's seeded generator. IPIV against
