@@ -274,6 +274,16 @@ void sl1x1_set_lookahead(int on);
  * factorization (panel 0, then its interchanges, U12 solve and update chunk by
  * chunk) starts as soon as its columns are in place. Same results either way. */
 void sl1x1_set_copy_chunks(int chunks);
+/* Test hook for the failure paths: the k-th next growth of a library-owned
+ * device buffer (k = 0: the next one) fails as if the device were out of
+ * memory, without allocating; the hook then disarms itself (k < 0 disarms it
+ * at once). Calls that need the buffer return INFO = -10002
+ * (-10000 - cudaErrorMemoryAllocation) and leave the library usable; the
+ * sliced-product scratch and the solve's block inverses are optional, and
+ * without them the FP64 DMMA update and the substitution solves run instead.
+ * Returns the hook's previous state: -1 once it has fired (or when it was
+ * off), else the growths it was still waiting for. */
+int sl1x1_debug_fail_alloc(int k);
 /* Smallest row slice per CTA of the cooperative panel kernel (8..768; 0, the
  * default, picks 256 rows for the FP32 panel and 128 for the FP64 one, with
  * about 64 CTAs for tall panels): larger slices mean fewer CTAs in each

@@ -138,6 +138,8 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_ozgemm_dev.restype = C.c_int
     L.sl1x1_set_lookahead.argtypes = [C.c_int]
     L.sl1x1_set_copy_chunks.argtypes = [C.c_int]
+    L.sl1x1_debug_fail_alloc.argtypes = [C.c_int]
+    L.sl1x1_debug_fail_alloc.restype = C.c_int
     L.sl1x1_device_ok.restype = C.c_int
     L.sl1x1_version.restype = C.c_char_p
     L.sl1x1_prof_enable.argtypes = [C.c_int]

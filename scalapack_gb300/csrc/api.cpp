@@ -128,6 +128,7 @@ void chk1mat(int ma, int mapos0, int na, int napos0, int ia, int ja, const int* 
 DevState g_dev;
 int g_default_nb = 256;
 bool g_lookahead = true;
+int g_fail_alloc_in = -1;
 int g_copy_chunks = 8;  // column chunks of A's host-to-device copy (<= 1: one copy)
 
 int cuda_info(cudaError_t e) { return -10000 - (int)e; }
@@ -736,10 +737,11 @@ int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, 
   if (keep_a) GROW(dAcopy, capAcopy, (size_t)ldf * n);
   GROW(dsplitk, capSplitk, (size_t)32 * 4 * n);  // split-K partials of the FP64 products
   GROW(ddinv, capDinv, (size_t)4 * ((n + 63) / 64) * 64 * 64);  // diagonal-block inverses and M_b
-  if (e == cudaSuccess) {
-    sl::splitk_scratch().ptr = g_dev.dsplitk;
-    sl::splitk_scratch().bytes = g_dev.capSplitk * sizeof(double);
-  }
+  // mirror the buffer whatever happened above: a failed grow freed it (null,
+  // capacity 0), and a stale pointer here would reach every later split-K
+  // product
+  sl::splitk_scratch().ptr = g_dev.dsplitk;
+  sl::splitk_scratch().bytes = g_dev.capSplitk * sizeof(double);
   {
     // ticket (64 bytes) + n x 8 values of the chained solves, each up to two
     // tagged 8-byte words (FP64 vectors)
@@ -1044,6 +1046,13 @@ void sl1x1_finalize(void) {
 void sl1x1_set_lookahead(int on) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_lookahead = (on != 0);
+}
+
+int sl1x1_debug_fail_alloc(int k) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  const int prev = g_fail_alloc_in;
+  g_fail_alloc_in = k < 0 ? -1 : k;
+  return prev;
 }
 
 void sl1x1_set_copy_chunks(int chunks) {

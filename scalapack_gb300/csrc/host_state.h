@@ -101,13 +101,19 @@ long long round_ld(long long m);
 int factor_host(int m, int n, double* A, int ia, int ja, const int* desca, int* ipiv,
                 cudaStream_t s, long long* ldda_out, cudaStream_t copy_stream = nullptr);
 
-// Grows a library-owned device buffer to at least `need` elements.
+// Test hook (sl1x1_debug_fail_alloc): the growth that finds it at 0 fails
+// as an exhausted device would; -1 is off.
+extern int g_fail_alloc_in;
+
+// Grows a library-owned device buffer to at least `need` elements. On
+// failure the buffer is gone (null, capacity 0).
 template <class T>
 cudaError_t grow(T** p, size_t* cap, size_t need) {
   if (need <= *cap && *p) return cudaSuccess;
   if (*p) cudaFree(*p);
   *p = nullptr;
   *cap = 0;
+  if (g_fail_alloc_in >= 0 && g_fail_alloc_in-- == 0) return cudaErrorMemoryAllocation;
   size_t n = need < 1 ? 1 : need;
   cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
   if (e == cudaSuccess) *cap = n;
