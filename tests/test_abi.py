@@ -245,3 +245,26 @@ def test_pdgetri_validation_and_query(sl, ctx):
     info, w0, iw0 = sl.pdgetri(8, a, 1, 1, d, ip, liwork=1)
     assert info == -10
     assert sl.pdgetri(0, a, 1, 1, d, ip)[0] == 0
+
+
+def test_alloc_failure_hook_state(sl):
+    # the hook counts growths down to the one that fails, then disarms itself;
+    # each call returns the previous state (-1: off or already fired)
+    L = sl.lib()
+    try:
+        assert L.sl1x1_debug_fail_alloc(3) == -1
+        assert L.sl1x1_debug_fail_alloc(0) == 3
+        assert L.sl1x1_debug_fail_alloc(-5) == 0
+        assert L.sl1x1_debug_fail_alloc(-1) == -1
+    finally:
+        L.sl1x1_debug_fail_alloc(-1)
+
+
+def test_speed_settings_accept_any_value(sl):
+    # speed-only settings clamp their argument and never fail
+    L = sl.lib()
+    for v in (-3, 0, 1, 8, 16, 99):
+        L.sl1x1_set_copy_chunks(v)
+    L.sl1x1_set_copy_chunks(8)
+    L.sl1x1_set_lookahead(0)
+    L.sl1x1_set_lookahead(1)
