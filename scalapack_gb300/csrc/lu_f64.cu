@@ -3,11 +3,18 @@
 // Structure follows PDGETRF on a 1x1 grid (SRC/pdgetrf.f:219-295):
 //   for each NB-wide block column j:
 //     panel      PDGETF2 (SRC/pdgetf2.f:206-237)  -> panel_kernel<double>, blocked by 32
-//     swaps      PDLASWP (SRC/pdlaswp.f:163-172)  -> laswp_kernel (left and right parts)
-//     U12        PDTRSM  (SRC/pdgetrf.f:280-282)  -> trsm_strip_kernel
-//     update     PDGEMM  (SRC/pdgetrf.f:288-290)  -> dgemm (DMMA, dgemm_f64.cu)
-// and PDGETRS (SRC/pdgetrs.f:250-284): pivots on B (PDLAPIV) as one composed
-// permutation, then unit-lower and non-unit-upper blocked solves.
+//     swaps      PDLASWP (SRC/pdlaswp.f:163-172)  -> laswp_apply_kernel (composite plan of
+//                                                    the panel's interchanges, both sides)
+//     U12        PDTRSM  (SRC/pdgetrf.f:280-282)  -> 64x64 block inverses of L11 and
+//                                                    sliced products (trsm_strip_kernel
+//                                                    in the DMMA mode)
+//     update     PDGEMM  (SRC/pdgetrf.f:288-290)  -> oz_dgemm (FP64 from exact BF16 slice
+//                                                    products, ozgemm_f64.cu; dgemm DMMA,
+//                                                    dgemm_f64.cu, in the DMMA mode)
+// with the next panel factored on a second stream (look-ahead), and PDGETRS
+// (SRC/pdgetrs.f:250-284): pivots on B (PDLAPIV) as one composed permutation,
+// then unit-lower and non-unit-upper blocked solves (diagonal-block inverses
+// and sliced products for NOTRAN, substitution strips otherwise).
 //
 // The NB-wide panel is factored as 32-column sub-panels; each sub-panel is one
 // cooperative kernel whose CTAs hold disjoint row slices of the sub-panel in

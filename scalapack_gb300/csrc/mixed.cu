@@ -17,7 +17,7 @@
 // pdlaschk.f:185-187) is at or below `tol`; when a step fails to halve it,
 // GMRES-IR takes over (GMRES on the left-preconditioned system (LU)^-1 A d =
 // (LU)^-1 r, classical Gram-Schmidt applied twice, Givens rotations). When
-// GMRES-IR also stalls, the FP64 factorization of the DMMA path is run and the
+// GMRES-IR also stalls, the plain FP64 factorization (dgetrf_device) is run and the
 // system is solved in plain FP64 (the reference's PDGERFS stall rule,
 // SRC/pdgerfs.f:552, motivates the halving test).
 #include <cuda_runtime.h>
@@ -645,7 +645,7 @@ cudaError_t dgesv_ir_device(int n, int nrhs, double* dA, long long lda, const do
     if (cst != 0) { st->dev_status = cst; return cudaSuccess; }
   }
   if (!converged) {
-    // FP64 fallback with the DMMA path: on a copy of A when one was provided
+    // FP64 fallback with the plain FP64 path: on a copy of A when one was provided
     // (A preserved, the residual is reported), else in place as LAPACK DSGESV
     // does (A returns the FP64 factors).
     st->fell_back = 1;

@@ -22,7 +22,7 @@ enum Phase {
   kPhPanel = 0,   // PDGETF2: sub-panel kernels and the in-panel swap/solve/update
   kPhLaswp = 1,   // PDLASWP on the left and right column blocks
   kPhTrsm = 2,    // PDTRSM for the U12 block row
-  kPhGemm = 3,    // PDGEMM trailing update (FP64 DMMA)
+  kPhGemm = 3,    // PDGEMM trailing update (sliced FP64 product, or FP64 DMMA)
   kPhSolve = 4,   // PDGETRS
   kPhMixedGemm = 5,  // low-precision trailing update (tcgen05)
   kPhMixedPanel = 6, // FP32 panel, swaps and solves of the mixed factorization
