@@ -238,8 +238,10 @@ void sl1x1_batch_plan_destroy(sl1x1_batch_plan plan);
  * sl1x1_dgetrf_dev with sl1x1_set_f64_update(0), and agree with the default
  * (sliced) factorization to rounding, with the same pivots.
  * The first call on a device looks up that array's address (make it before
- * any stream capture); calls whose GPU work overlaps race on the shared array.
- * M above 152 SMs x 768 rows is rejected with -30000 before any launch. */
+ * any stream capture); every call reads its status back and synchronizes its
+ * stream before it returns; calls whose GPU work overlaps race on the shared
+ * array. M above (SMs of the device) x 768 rows (152 x 768 on GB300) is
+ * rejected with -30000 before any launch. */
 int sl1x1_dgetrf_noalloc(int m, int n, double* dA, long long ldda, int* dipiv, int nb,
                          void* stream);
 

@@ -11,6 +11,8 @@
 //
 // C (m x n) = alpha * op(A) (m x k) * B (k x n) + beta * C, column-major.
 #include <cuda_runtime.h>
+
+#include <atomic>
 #include <stdint.h>
 #include "common.cuh"
 #include "sl_internal.h"
@@ -164,15 +166,26 @@ static cudaError_t launch_dmma(int m, int n, int k, double alpha, const double* 
   return cudaGetLastError();
 }
 
-// Number of SMs of the current device (cached).
+// Number of SMs of the current device, cached per device; 1 while no device
+// answers (not cached, so a later call on a working device gets its count).
 int num_sms() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
+  constexpr int kDevs = 64;
+  static std::atomic<int> cache[kDevs];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
   }
+  if (dev >= 0 && dev < kDevs) {
+    const int c = cache[dev].load(std::memory_order_relaxed);
+    if (c > 0) return c;
+  }
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    return 1;
+  }
+  if (dev >= 0 && dev < kDevs) cache[dev].store(n, std::memory_order_relaxed);
   return n;
 }
 

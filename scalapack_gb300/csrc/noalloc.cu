@@ -19,7 +19,9 @@
 //
 // Set-up: the first call on each device looks up the device address of that
 // array (cudaGetSymbolAddress, with that device current) and caches it; make
-// that first call before any stream capture. Every call shares the one array:
+// that first call before any stream capture. Every call reads its status
+// words back and synchronizes its stream before it returns. Every call
+// shares the one array:
 // the call re-initializes the status and zero-pivot words and every panel
 // launch clears its exchange area,
 // but two calls whose GPU work overlaps (on different streams or from
@@ -64,8 +66,8 @@ extern "C" int sl1x1_dgetrf_noalloc(int m, int n, double* dA, long long ldda, in
     if (m > max_rows) {
       std::fprintf(stderr,
                    "sl1x1_dgetrf_noalloc: M=%d exceeds the supported maximum of %d rows "
-                   "(152 SMs x 768 panel rows in shared memory); nothing was launched\n",
-                   m, max_rows);
+                   "(%d SMs x 768 panel rows in shared memory); nothing was launched\n",
+                   m, max_rows, max_rows / 768);
       return -30000;
     }
   }

@@ -23,6 +23,8 @@ struct PhaseRec {
 
 std::mutex g_pm;
 bool g_on = false;
+// Per host thread: a ProfSuppress on one thread leaves the timers of calls on
+// other threads untouched, so it needs no lock.
 thread_local bool g_suppressed = false;
 PhaseRec g_ph[kNumPhases];
 std::vector<cudaEvent_t> g_pool;

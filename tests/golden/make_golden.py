@@ -13,7 +13,7 @@
    does.  This is independent of the C oracle's 64-bit jump-ahead arithmetic,
    so the test that compares the two pins the oracle's generator.
 
-Usage: python tests/golden/make_golden.py [/path/to/reference]
+Usage: python tests/golden/make_golden.py /path/to/reference-tree
 """
 from __future__ import annotations
 
@@ -23,7 +23,9 @@ import sys
 from fractions import Fraction
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: make_golden.py /path/to/reference-tree (the ScaLAPACK source tree)")
+REF = sys.argv[1]
 
 
 def read_pdlaread(path):

@@ -143,8 +143,8 @@ def test_mixed_ir_conditioning_sweep(sl, orc, gpu_required, kappa):
 
 def test_gmres_ir_converges_at_kappa_1e8_without_fallback(sl, orc, gpu_required):
     # kappa = 1e8 is beyond classical refinement with BF16x3 (near-FP32) factors;
-    # GMRES-IR applies the preconditioner in FP64 vector arithmetic (double-FP32
-    # bulk products), a fixed operator, and reaches the FP64 backward error
+    # GMRES-IR applies the preconditioner (FP32 factors and block inverses) with
+    # FP64 vector arithmetic, a fixed operator, and reaches the FP64 backward error
     # without falling back to the FP64 factorization.
     import torch
 

@@ -74,3 +74,25 @@ def test_noalloc_rejects_oversized_m_before_any_launch(sl, capfd):
                                          None)
     assert info == -30000
     assert "exceeds the supported maximum" in capfd.readouterr().err
+
+
+@pytest.mark.gpu
+def test_noalloc_grows_no_library_buffer(sl, gpu_required):
+    """The promise itself: with every library buffer dropped and the
+    allocation-failure hook armed for the very next growth, the call
+    completes and the hook never fires (nothing was allocated)."""
+    rng = np.random.default_rng(9)
+    n, nb = 400, 64
+    A0 = np.asfortranarray(rng.uniform(-0.5, 0.5, size=(n, n)))
+    info_r, LU_r, piv_r = _factor_dev(sl, A0, nb, 0)
+    L = sl.lib()
+    L.sl1x1_finalize()
+    L.sl1x1_debug_fail_alloc(0)
+    try:
+        info, LU, piv = _factor(sl, sl.dgetrf_noalloc, A0, nb)
+    finally:
+        still_armed = L.sl1x1_debug_fail_alloc(-1)
+    assert still_armed >= 0  # -1 would mean a library buffer grew
+    assert info == info_r == 0
+    np.testing.assert_array_equal(piv, piv_r)
+    np.testing.assert_allclose(LU, LU_r, rtol=1e-12, atol=0)
