@@ -286,6 +286,14 @@ void sl1x1_set_copy_chunks(int chunks);
  * Returns the hook's previous state: -1 once it has fired (or when it was
  * off), else the growths it was still waiting for. */
 int sl1x1_debug_fail_alloc(int k);
+/* Test hook for the bounded device waits: the number of polls a panel CTA
+ * makes for another CTA's published pivot candidates before it gives up
+ * (polls < 0 restores the default, 2^24; 0 makes every wait run out at its
+ * first poll). A panel that gives up records a device timeout, writes the
+ * identity for the pivots it has not chosen and returns; the call then
+ * returns INFO = -20002 and the library stays usable. No counterpart in the
+ * reference, whose panel has no device waits. */
+void sl1x1_debug_set_spin_limit(long long polls);
 /* Smallest row slice per CTA of the cooperative panel kernel (8..768; 0, the
  * default, picks 256 rows for the FP32 panel and 128 for the FP64 one, with
  * about 64 CTAs for tall panels): larger slices mean fewer CTAs in each

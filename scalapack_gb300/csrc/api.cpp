@@ -1115,6 +1115,11 @@ int sl1x1_ozgemm_dev(int m, int n, int k, double alpha, const double* dA, long l
   return st ? -20000 - st : 0;
 }
 
+void sl1x1_debug_set_spin_limit(long long polls) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  sl::set_spin_limit(polls);
+}
+
 void sl1x1_set_default_nb(int nb) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (nb > 0) g_default_nb = nb;

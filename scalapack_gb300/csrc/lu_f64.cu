@@ -40,6 +40,10 @@ static_assert(kPanelCandDoubles == (size_t)PX_WORDS, "exchange area layout");
 // rounded down to a multiple of 8: 768 rows; one CTA per SM.
 int panel_max_rows() { return num_sms() * 768; }
 
+static long long g_spin_limit = kSpinLimit;
+long long spin_limit() { return g_spin_limit; }
+void set_spin_limit(long long polls) { g_spin_limit = polls < 0 ? kSpinLimit : polls; }
+
 static int g_panel_min_rows = 0;  // 0: automatic (FP32 256, FP64 128)
 int panel_min_rows() { return g_panel_min_rows; }
 void set_panel_min_rows(int rows) { g_panel_min_rows = rows <= 0 ? 0 : (rows < 8 ? 8 : (rows > 768 ? 768 : rows)); }

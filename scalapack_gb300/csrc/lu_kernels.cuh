@@ -96,10 +96,12 @@ __device__ __forceinline__ void st_value(unsigned long long* p, int j, T v, uint
   }
 }
 
-// Polls value j of a published row until its tag matches; false on timeout.
+// Polls value j of a published row until its tag matches, at most `limit`
+// times; false on timeout.
 template <typename T>
-__device__ __forceinline__ bool ld_value(const unsigned long long* p, int j, uint32_t tag, T& v) {
-  for (long long spins = 0; spins <= kSpinLimit; ++spins) {
+__device__ __forceinline__ bool ld_value(const unsigned long long* p, int j, uint32_t tag, T& v,
+                                         long long limit) {
+  for (long long spins = 0; spins < limit; ++spins) {
     if constexpr (sizeof(T) == 4) {
       const unsigned long long a = ld_tagged(p + j);
       if (tag_ok(a, tag)) { v = __uint_as_float(payload(a)); return true; }
@@ -153,11 +155,14 @@ __device__ __forceinline__ void warp_ikey(long long& k, int& r) {
 // Column k's words carry tag k+1 and the launch zeroes the area first. A word
 // of parity k&1 is rewritten only at column k+2, after every CTA has read
 // column k+1 -- which it can only do after finishing column k -- so two
-// parities suffice. Every poll is bounded.
+// parities suffice. Every poll is bounded (at most spin_limit polls); a CTA
+// that gives up records kFlagTimeout and returns, and block 0 then writes the
+// identity for the pivots it has not chosen, so the interchanges launched
+// after it stay inside the matrix.
 template <typename T>
 __global__ void __launch_bounds__(PT)
 panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ipiv,
-             int* info_col, double* cand, int* status) {
+             int* info_col, double* cand, int* status, long long spin_limit) {
   extern __shared__ __align__(16) unsigned char panel_smem[];
   T* tile = reinterpret_cast<T*>(panel_smem);  // [rpc][PLD]
   __shared__ T s_U[PW];
@@ -178,6 +183,11 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
   unsigned long long* diagw = words + PX_DIAG;
   unsigned long long* keyw = words + PX_KEYS;
   unsigned long long* valw = words + PX_VALS;
+  // block 0 on a timeout at column k: pivots k.. become the diagonal rows
+  auto give_up = [&](int k) {
+    if (b == 0)
+      for (int q = k + tid; q < kw; q += PT) ipiv[c0 + q] = r0 + q;
+  };
 
   // Sub-panel rows into shared memory, all w columns' loads in flight at once.
   for (int r = tid; r < nr; r += PT) {
@@ -239,6 +249,7 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
     if (tid < G) {
       long long spins = 0;
       for (;;) {
+        if (spins++ >= spin_limit) { atomicExch(status, (int)kFlagTimeout); s_fail = 1; break; }
         unsigned long long w0, w1, w2, w3;
         ld_tagged2(keyw + ((size_t)tid + (size_t)par * PMAXG) * 4, w0, w1);
         ld_tagged2(keyw + ((size_t)tid + (size_t)par * PMAXG) * 4 + 2, w2, w3);
@@ -248,17 +259,16 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
           row = rr >= (uint32_t)INT_MAX ? INT_MAX : (int)rr;
           break;
         }
-        if (++spins > kSpinLimit) { atomicExch(status, (int)kFlagTimeout); s_fail = 1; break; }
       }
     } else if (warp == PT / 32 - 1 && lane < w) {
       T v;
-      if (ld_value<T>(diagw + par * 2 * PW, lane, tag, v)) s_D[lane] = v;
+      if (ld_value<T>(diagw + par * 2 * PW, lane, tag, v, spin_limit)) s_D[lane] = v;
       else { atomicExch(status, (int)kFlagTimeout); s_fail = 1; }
     }
     warp_ikey(key, row);
     if (lane == 0) { s_wk[warp] = key; s_wr[warp] = row; }
     __syncthreads();
-    if (s_fail) return;
+    if (s_fail) { give_up(k); return; }
     if (warp == 0) {
       key = lane < PT / 32 ? s_wk[lane] : -2;
       row = lane < PT / 32 ? s_wr[lane] : INT_MAX;
@@ -275,12 +285,12 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
         s_U[tid] = s_D[tid];
       } else {
         T v;
-        if (ld_value<T>(valw + ((size_t)(piv / rpc) * 2 + par) * 2 * PW, tid, tag, v)) s_U[tid] = v;
+        if (ld_value<T>(valw + ((size_t)(piv / rpc) * 2 + par) * 2 * PW, tid, tag, v, spin_limit)) s_U[tid] = v;
         else { atomicExch(status, (int)kFlagTimeout); s_fail = 1; }
       }
     }
     __syncthreads();
-    if (s_fail) return;
+    if (s_fail) { give_up(k); return; }
     // --- row interchange inside the sub-panel (PDSWAP, pdgetf2.f:218) ---
     if (piv != d && tid < w) {
       if (d >= lo && d < lo + nr) tile[(d - lo) * PLD + tid] = s_U[tid];
@@ -977,8 +987,9 @@ inline cudaError_t launch_panel(T* A, long long lda, int m, int r0, int c0, int 
   // zero the diagonal rows and the G slots used (stale tags must not match)
   cudaError_t e = cudaMemsetAsync(ws.cand, 0, sizeof(unsigned long long) * ((size_t)PX_VALS + (size_t)G * 2 * 2 * PW), s);
   if (e != cudaSuccess) return e;
+  long long limit = spin_limit();
   void* args[] = {&A, &lda, &m, &r0, &c0, &w, (void*)&rpc, &ipiv, (void*)&ws.info_col,
-                  (void*)&ws.cand, (void*)&ws.status};
+                  (void*)&ws.cand, (void*)&ws.status, (void*)&limit};
   count_launches(1);
   return cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(PT), args, smem, s);
 }

@@ -130,6 +130,10 @@ int panel_max_rows();
 // default, means 256 rows for FP32 and 128 for FP64).
 int panel_min_rows();
 void set_panel_min_rows(int rows);
+// Polls a panel CTA makes for another CTA's published words before it gives
+// up (kSpinLimit by default; a test lowers it to make the waits run out).
+long long spin_limit();
+void set_spin_limit(long long polls);
 // Block size used when a caller passes nb <= 0.
 int default_nb();
 // While an instance lives on a thread, phase timers record nothing on it

@@ -103,3 +103,36 @@ def test_mixed_exhaustion_at_each_growth(sl, orc, ctx):
     finally:
         L.sl1x1_debug_fail_alloc(-1)
     assert failed >= 10, failed
+
+
+@pytest.mark.parametrize("polls", [0, 1])
+def test_panel_wait_runs_out_and_library_recovers(sl, orc, ctx, polls):
+    """A device wait that gives up: with the panel's poll limit at 0 or 1, the
+    cooperative panel's waits for the other CTAs' pivot candidates run out
+    (no trap, no fault: each CTA records the timeout and returns, block 0
+    writes identity pivots so the interchanges after it stay in range). The
+    call returns INFO = -20002 (-20000 - kFlagTimeout); with the default
+    limit restored the next call matches the oracle."""
+    from lu_helpers import compare_ipiv
+
+    n, nrhs, nb = 700, 2, 128  # 700 rows: six panel CTAs exchange candidates
+    A0, B0 = system(orc, n, nrhs)
+    L = sl.lib()
+    try:
+        L.sl1x1_debug_set_spin_limit(polls)
+        info, X = _pdgesv(sl, ctx, A0, B0, nb)
+        if polls == 0:
+            assert info == -20002
+        else:
+            assert info in (-20002, 0)
+    finally:
+        L.sl1x1_debug_set_spin_limit(-1)
+    A = np.asfortranarray(A0.copy())
+    X = np.asfortranarray(B0.copy())
+    desca = np.array([1, ctx, n, n, nb, nb, 0, 0, n], np.int32)
+    descb = np.array([1, ctx, n, nrhs, nb, nb, 0, 0, n], np.int32)
+    ipiv = np.zeros(n + nb, np.int32)
+    assert sl.pdgesv(n, nrhs, A, 1, 1, desca, ipiv, X, 1, 1, descb) == 0
+    bad, _ = compare_ipiv(orc, A0, ipiv[:n], nb)
+    assert bad == 0
+    assert orc.sresid(A0, B0, X) < RESID_THRESH
