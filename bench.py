@@ -460,6 +460,7 @@ def run_gpu(args):
     peak = float(L.sl1x1_dmma_peak_tflops())
     sl.prof_enable(True)
     launches0 = sl.launch_count()
+    routes0 = int(L.sl1x1_ozgemm_fp64_routes())
     barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -471,6 +472,7 @@ def run_gpu(args):
         barrier()
     ms = e0.elapsed_time(e1) / args.steps
     launches = sl.launch_count() - launches0
+    fp64_routes = int(L.sl1x1_ozgemm_fp64_routes()) - routes0
     phases = sl.prof_read()
     sl.prof_enable(False)
     if dist is not None:
@@ -607,6 +609,7 @@ def run_gpu(args):
             "e2e": e2e,
             "clocks": clk.summary(),
             "gpu_launches": launches,
+            "sliced_fp64_routes_per_step": fp64_routes / args.steps,
             "accuracy": {"sresid": sresid, "threshold": 16.0},
             "phases": phase_summary,
             "mixed_ir": mixed,

@@ -327,6 +327,13 @@ void sl1x1_set_ozgemm_tiles(int tiles_per_cta);
  * <= -20000 for a device timeout. */
 int sl1x1_ozgemm_dev(int m, int n, int k, double alpha, const double* dA, long long ldda,
                      const double* dB, long long lddb, double* dC, long long lddc, void* stream);
+/* Passes of the sliced FP64 product (trailing updates, U12 and PDGETRS
+ * products, sl1x1_ozgemm_dev) that the error-budget test sent to the FP64
+ * route on the current device since the library was loaded; -1 if the count
+ * cannot be read. Operands whose large entries a power-of-two balancing along
+ * k cannot line up take that route (no counterpart in the reference, whose
+ * DGEMM is FP64 throughout). */
+long long sl1x1_ozgemm_fp64_routes(void);
 /* 1 if the library found a usable sm_103 device, else 0. */
 int sl1x1_device_ok(void);
 /* Version string. */

@@ -136,6 +136,8 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_ozgemm_dev.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, vp, C.c_longlong, vp,
                                    C.c_longlong, vp, C.c_longlong, vp]
     L.sl1x1_ozgemm_dev.restype = C.c_int
+    L.sl1x1_ozgemm_fp64_routes.argtypes = []
+    L.sl1x1_ozgemm_fp64_routes.restype = C.c_longlong
     L.sl1x1_set_lookahead.argtypes = [C.c_int]
     L.sl1x1_set_copy_chunks.argtypes = [C.c_int]
     L.sl1x1_debug_fail_alloc.argtypes = [C.c_int]

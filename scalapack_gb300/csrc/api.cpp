@@ -1120,6 +1120,12 @@ void sl1x1_debug_set_spin_limit(long long polls) {
   sl::set_spin_limit(polls);
 }
 
+long long sl1x1_ozgemm_fp64_routes(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!ensure_device()) return -1;
+  return sl::oz_fp64_routes();
+}
+
 void sl1x1_set_default_nb(int nb) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (nb > 0) g_default_nb = nb;

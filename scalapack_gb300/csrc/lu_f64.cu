@@ -183,8 +183,8 @@ static cudaError_t solve_u12(int jb, int nr, const double* L11, long long ldl, d
     return trsm_strip<double, false, false, true>(jb, nr, L11, ldl, A12, lda, s);
   for (int r0 = 0; r0 < jb; r0 += 64) {
     const int w = (jb - r0) < 64 ? (jb - r0) : 64;
-    SL_TRY(oz_dgemm(ws.oz, w, nr, w, 1.0, ws.dinv64 + (size_t)(r0 / 64) * 4096, 64, A12 + r0, lda,
-                    A12 + r0, lda, ws.status, s));
+    SL_TRY(oz_dgemm_bside(ws.oz, w, nr, w, 1.0, ws.dinv64 + (size_t)(r0 / 64) * 4096, 64,
+                          A12 + r0, lda, A12 + r0, lda, ws.status, s));
     if (r0 + w < jb)
       SL_TRY(oz_dgemm(ws.oz, jb - r0 - w, nr, w, -1.0, L11 + (r0 + w) + (long long)r0 * ldl, ldl,
                       A12 + r0, lda, A12 + r0 + w, lda, ws.status, s));
@@ -303,9 +303,11 @@ static cudaError_t step0_by_chunks(int m, int n, double* dA, long long ldda, int
 // With columns still arriving (ws.ncol_chunks > 0), s waits for each column
 // chunk just before the first operation on it: panel 0 starts when its
 // columns are in place, and step 0's interchanges, U12 solve and update run
-// chunk by chunk as the rest lands. Every one of those operations is
-// independent per column, so the factors are bitwise those of the whole-width
-// step. After the look-ahead panel is launched the step-0 operations must not
+// chunk by chunk as the rest lands. The interchanges and the update are
+// independent per column; the U12 solve's first product balances its slices
+// by the row maxima of the columns it is given, so those rows agree with the
+// whole-width step to rounding (same pivots). After the look-ahead panel is
+// launched the step-0 operations must not
 // read the per-panel scratch that panel overwrites (the interchange plan and
 // L11's block inverses): they take the interchanges from dipiv and a copy of
 // the inverses (ws.dinv64_step0).

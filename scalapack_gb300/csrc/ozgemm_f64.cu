@@ -32,9 +32,40 @@
 // Epilogue. P_2..P_6 are read back as exact integers, combined with the FP32
 // sum of the tail diagonals into one 64-bit integer I = sum_d P_d 2^(52-7d) (|I| < 2^61), converted to
 // FP64 once, and C(i,j) = fma(alpha 2^(e_i+f_j-52), I, C(i,j)). The result is
-// within a few units of 2^-53 of |A(i,:)|_max |B(:,j)|_max of the exact
-// product, and independent of the accumulation order (run to run identical).
-// Rows or columns holding Inf or NaN give NaN in their row or column of C.
+// within a few units of 2^-53 of 2^(e_i + f_j) of the exact product, and
+// independent of the accumulation order (run to run identical). Rows or
+// columns holding Inf or NaN give NaN in their row or column of C.
+//
+// Balancing along k. A B = (A 2^-d)(2^d B) for any integers d_k, so the
+// scales are taken after an exact power-of-two balancing (ex x: |x| < 2^ex x,
+// over the k whose column of A and row of B are both nonzero):
+//   e_i = max_k (ex A(i,k) - d_k),   f_j = max_k (ex B(k,j) + d_k).
+// The shift goes into the slicing's shift counts; no scaled value is ever
+// formed. Side A (the default): d_k = c_k, the exponent of the largest
+// magnitude in column k of A. In the LU A = L21 (|L| <= 1, so c_k ~ 0 and
+// nothing moves on well-scaled data); on a row-graded matrix a block's pivots
+// differ widely in size, column k of L21 is ~2^-(s_pk) and row k of U12
+// ~2^(s_pk), and without the balancing the largest L21 and U12 entries of a
+// pair (i, j) sit at different k, so 2^(e_i + f_j) would exceed every term of
+// the product by the pivots' spread. Side B: d_k = -h_k, h_k the exponent of
+// the largest magnitude in row k of B -- for the U12 solve's product
+// (inv(L_bb) - I) A12_b, whose rows of B carry the pivots' scales while the
+// columns of the inverse do not.
+//
+// Error budget. With G = max_k (c_k + h_k), side A compares each row's error
+// bound 2^(e_i + G) with F_i = max_k (ex A(i,k) + h_k), the exponent of a
+// lower bound of max_j (|A| |B|)(i,j) (an FP64 GEMM's bound for that row);
+// side B compares each column's 2^(f_j + G) with F_j = max_k (c_k +
+// ex B(k,j)). Where any row (column) is more than OZ_BUDGET bits above it (a
+// row of A small exactly where a row of B holds an entry far above the rest),
+// or a scale leaves the normal FP64 range, the whole pass is computed in FP64
+// arithmetic instead (fixed order, every product an FMA) by the same
+// launches. Accuracy model: each row's (column's) error is within about
+// 2^OZ_BUDGET of the FP64 GEMM's error bound for its largest |A||B| term
+// (normwise per row or column); for inputs that are diagonal scalings of
+// well-scaled data that is the componentwise level. Operands whose large
+// entries cross (row i large at k1 only, column j large at k2 only) keep the
+// normwise bound but not a componentwise one.
 //
 // Structure (one CTA per SM, a few 128 x 64 tiles of C per CTA, 10 warps):
 //   * warp 0 allocates all 512 TMEM columns (8 accumulators x 64 columns);
@@ -57,6 +88,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 
 #include "common.cuh"
@@ -78,6 +110,18 @@ constexpr int B_CHUNK_BYTES = OZ_S * B_SLICE_BYTES;   // 64 KB per k block
 constexpr int A_RING = 6;
 constexpr int OZ_TMEM_COLS = 512;
 constexpr int GROUP_M = 8;       // tile raster: 8 row tiles sweep the columns together
+
+// Balancing / budget area at the start of the scratch: h keys [256] (rows of
+// B), c keys [256] (columns of A), the FP64-route flag. Each word is
+// (epoch << 12) | (exponent + OZ_EBIAS), so a pass ignores what earlier passes
+// left (epochs only grow) and nothing has to be cleared between passes.
+constexpr int OZ_KINFO_BYTES = 8192;
+constexpr int OZ_KI_H = 0, OZ_KI_C = OZ_KMAX, OZ_KI_FLAG = 2 * OZ_KMAX;
+constexpr int OZ_EBIAS = 1100;   // frexp exponents -1073 .. 1024 -> 27 .. 2124 (< 4096)
+constexpr int OZ_BUDGET = 8;     // bits above the FP64 GEMM's row (column) bound
+constexpr int OZ_NOEXP = INT_MIN / 4;
+
+__device__ unsigned long long g_oz_fp64_routes;  // passes that took the FP64 route
 
 struct __align__(8) OzBars {
   uint64_t afull[A_RING], aempty[A_RING];
@@ -140,6 +184,54 @@ __device__ __forceinline__ bool oz_issue_b(int c, int first, int nkc, int tiles_
   return true;
 }
 
+// The FP64 route of a pass whose slices would exceed the error budget: the
+// CTA's tiles computed directly from the FP64 operands. B's 64 columns of a
+// tile (kb <= 256 rows, 128 KB) are staged in shared memory before any of
+// them is written, so B may alias C where one tile covers all rows (m <= 128).
+// Threads 64.. own one row and 32 columns each; products accumulate in k
+// order with one FMA each, then C = fma(alpha, acc, C).
+__device__ __noinline__ void oz_fp64_tiles(unsigned char* smem, int m, int n, int kb,
+                                           const double* __restrict__ A, long long lda,
+                                           const double* B, long long ldb, double alpha,
+                                           double* C, long long ldc, int first_tile,
+                                           int my_tiles, int tiles_m, int tiles_n) {
+  double* sB = reinterpret_cast<double*>(smem);  // [kb][64]
+  const int tid = threadIdx.x;
+  for (int it = 0; it < my_tiles; ++it) {
+    int m0, n0;
+    oz_tile(first_tile + it, tiles_m, tiles_n, m0, n0);
+    __syncthreads();
+    for (int idx = tid; idx < kb * OBN; idx += OZ_THREADS) {
+      const int c = idx / kb, k = idx - c * kb;
+      sB[k * OBN + c] = (n0 + c < n) ? B[k + (long long)(n0 + c) * ldb] : 0.0;
+    }
+    __syncthreads();
+    if (tid >= 64) {
+      const int t = tid - 64, row = m0 + (t & (OBM - 1)), h = t >> 7;
+      if (row < m) {
+        double acc[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) acc[j] = 0.0;
+        const double* arow = A + row;
+        for (int k = 0; k < kb; ++k) {
+          const double a = arow[(long long)k * lda];
+          const double* bk = sB + k * OBN + h * 32;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) acc[j] = fma(a, bk[j], acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int col = n0 + h * 32 + j;
+          if (col < n) {
+            double* cp = C + row + (long long)col * ldc;
+            *cp = fma(alpha, acc[j], *cp);
+          }
+        }
+      }
+    }
+  }
+}
+
 // CTA b takes tiles b tpc .. b tpc + tpc - 1 of the raster (a few, so that
 // SMs turn over and the panel's kernels on the high-priority stream find
 // room between them). The TMA thread runs
@@ -154,7 +246,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 ozgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               int m, int n, int kpad, int m_pad, int n_pad, const double* __restrict__ rs,
               const double* __restrict__ cs, double alpha, double* C, long long ldc, int tpc,
-              int* status) {
+              int* status, const double* __restrict__ A64, long long lda, const double* B64,
+              long long ldb, int kb, const unsigned long long* kinfo, unsigned long long epoch) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* sA = base;                                   // A_RING x 16 KB
@@ -171,6 +264,13 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
   __shared__ int s_fail, s_aiss, s_acons, s_biss, s_bcons;
   // a CTA that timed out already marked the launch failed: skip the work
   if (*(volatile int*)status != 0) return;
+  // the slicing found the pass outside the error budget: FP64 route
+  if (*(volatile const unsigned long long*)(kinfo + OZ_KI_FLAG) == epoch) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&g_oz_fp64_routes, 1ULL);
+    oz_fp64_tiles(base, m, n, kb, A64, lda, B64, ldb, alpha, C, ldc, first_tile, my_tiles,
+                  tiles_m, tiles_n);
+    return;
+  }
 
   if (threadIdx.x == 0) {
     s_fail = 0;
@@ -374,6 +474,8 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
 // left by at most 3 bits, or right (dropping the bits below 2^-56 of the
 // scale). Slice s (1-based) is bits [56-7s, 63-7s) of U with the sign of x:
 // exactly the integer parts of the FP64 truncation x 2^-e = sum a_s 2^-7s.
+// With the balancing, A(i,k) is cut against e_i + d_k and B(k,j) against
+// f_j - d_k.
 constexpr unsigned long long kMagMask = 0x7fffffffffffffffULL;
 constexpr unsigned long long kInfBits = 0x7ff0000000000000ULL;
 
@@ -391,7 +493,8 @@ __device__ __forceinline__ unsigned long long oz_fixed(unsigned long long bits, 
   return m >> (-sh);
 }
 
-// frexp exponent of the largest magnitude (its bit pattern, finite, nonzero)
+// frexp exponent of a magnitude given by its bit pattern (finite, nonzero):
+// 2^(ex-1) <= |x| < 2^ex
 __device__ __forceinline__ int oz_scale_exp(unsigned long long kmax) {
   const int bexp = (int)(kmax >> 52);
   if (bexp != 0) return bexp - 1022;
@@ -399,13 +502,15 @@ __device__ __forceinline__ int oz_scale_exp(unsigned long long kmax) {
 }
 
 // 2^(e - 26) as a double (the epilogue's scale factor half), NaN for a
-// non-finite row or column, 0 for a zero one
-__device__ __forceinline__ double oz_scale_value(unsigned long long kmax, bool bad) {
+// non-finite row or column, 0 for a zero one; the caller has checked that
+// e - 26 is a normal exponent
+__device__ __forceinline__ double oz_scale_value(int e, bool bad) {
   if (bad) return __longlong_as_double(0x7ff8000000000000LL);
-  if (kmax == 0ULL) return 0.0;
-  const int be = oz_scale_exp(kmax) - 26 + 1023;
-  if (be >= 1 && be <= 2046) return __longlong_as_double((long long)((unsigned long long)be << 52));
-  return ldexp(1.0, oz_scale_exp(kmax) - 26);
+  if (e == OZ_NOEXP) return 0.0;
+  return __longlong_as_double((long long)((unsigned long long)(e - 26 + 1023) << 52));
+}
+__device__ __forceinline__ bool oz_scale_in_range(int e) {
+  return e == OZ_NOEXP || (e - 26 >= -1022 && e - 26 <= 1023);
 }
 
 __device__ __forceinline__ __nv_bfloat16 oz_slice_bf16(unsigned long long U, int s, bool neg) {
@@ -414,46 +519,159 @@ __device__ __forceinline__ __nv_bfloat16 oz_slice_bf16(unsigned long long U, int
   return __float2bfloat16_rn((neg ? -a : a) * __int_as_float((127 - OZ_BITS * s) << 23));
 }
 
-// Both operands in one launch. Blocks [0, m_pad/32): 32 rows of A (m x kb,
-// column-major) each, staged through shared memory 64 k at a time so that
-// the reads run along the columns; slices Sa[s][i][kk]. Blocks after that: 8
-// columns of B (kb x n, column-major, a column contiguous in k) each, one
-// warp per column; slices Sb[t][j][kk]. Padding rows, columns and k are zero.
+__device__ __forceinline__ int oz_warp_imax(int v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, off));
+  return v;
+}
+// biased exponent of a finite nonzero value (1 .. 4095), 0 otherwise
+__device__ __forceinline__ unsigned oz_ekey(double x) {
+  const unsigned long long mag = (unsigned long long)__double_as_longlong(x) & kMagMask;
+  return (mag != 0ULL && mag < kInfBits) ? (unsigned)(oz_scale_exp(mag) + OZ_EBIAS) : 0u;
+}
+// exponent held by a balancing word of this epoch, OZ_NOEXP if none
+__device__ __forceinline__ int oz_word_exp(unsigned long long w, unsigned long long epoch) {
+  return (w >> 12) == epoch ? (int)(w & 4095ULL) - OZ_EBIAS : OZ_NOEXP;
+}
+
+// Balancing exponents of one pass, both operands in one launch. Blocks
+// [0, nab): 32 rows of A (m x kb) each; warp w takes columns k = w, w+8, ...
+// (one coalesced 256-byte load per column), reduces the lanes' exponent keys
+// with one __reduce_max_sync and keeps the column's maximum in shared memory:
+// c_k. Blocks after that: 64 columns of B (kb x n) each; warp w takes columns
+// w, w+8, ..., lane l rows l, l+32, ...: h_k. Each block publishes its
+// maxima with atomicMax into the epoch-tagged words. Small blocks with many
+// independent loads, so the pass over both operands runs near copy speed.
+__global__ void __launch_bounds__(256)
+oz_kscale_kernel(const double* __restrict__ A, long long lda, int m, const double* __restrict__ B,
+                 long long ldb, int n, int kb, int nab, unsigned long long* kinfo,
+                 unsigned long long epoch) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ unsigned red[8][OZ_KMAX];
+  if ((int)blockIdx.x < nab) {
+    const int i = (int)blockIdx.x * 32 + lane;
+    const double* arow = A + i;
+#pragma unroll 8
+    for (int k = warp; k < kb; k += 8) {
+      const unsigned v = (i < m) ? oz_ekey(arow[(long long)k * lda]) : 0u;
+      const unsigned r = __reduce_max_sync(0xffffffffu, v);
+      if (lane == 0) red[0][k] = r;
+    }
+    __syncthreads();
+    const int k = threadIdx.x;
+    if (k < kb && red[0][k]) atomicMax(kinfo + OZ_KI_C + k, (epoch << 12) | red[0][k]);
+    return;
+  }
+  const int c0 = ((int)blockIdx.x - nab) * 64;
+  unsigned km[OZ_KMAX / 32];
+#pragma unroll
+  for (int r = 0; r < OZ_KMAX / 32; ++r) km[r] = 0u;
+#pragma unroll 2
+  for (int q = 0; q < 8; ++q) {
+    const int j = c0 + warp + 8 * q;
+    if (j < n) {
+      const double* col = B + (long long)j * ldb;
+#pragma unroll
+      for (int r = 0; r < OZ_KMAX / 32; ++r) {
+        const int k = lane + 32 * r;
+        if (k < kb) km[r] = max(km[r], oz_ekey(col[k]));
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < OZ_KMAX / 32; ++r) red[warp][lane + 32 * r] = km[r];
+  __syncthreads();
+  const int k = threadIdx.x;
+  if (k < kb) {
+    unsigned v = 0u;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) v = max(v, red[w][k]);
+    if (v) atomicMax(kinfo + OZ_KI_H + k, (epoch << 12) | v);
+  }
+}
+
+// Both operands in one launch, after oz_kscale_kernel. Blocks [0, m_pad/32):
+// 32 rows of A (m x kb, column-major) each, staged through shared memory 64 k
+// at a time so that the reads run along the columns; slices Sa[s][i][kk] cut
+// against e_i + d_k, and on side A the row's error-budget test. Blocks after
+// that: 8 columns of B (kb x n, column-major, a column contiguous in k) each,
+// one warp per column; slices Sb[t][j][kk] cut against f_j - d_k, and on side
+// B the column's test. Padding rows, columns and k are zero; so is every k
+// whose column of A or row of B is zero (its products vanish).
 __global__ void __launch_bounds__(256)
 oz_split_kernel(const double* __restrict__ A, long long lda, int m, const double* __restrict__ B,
                 long long ldb, int n, int kb, int kpad, int m_pad, int n_pad,
-                __nv_bfloat16* Sa, __nv_bfloat16* Sb, double* rs, double* cs) {
+                __nv_bfloat16* Sa, __nv_bfloat16* Sb, double* rs, double* cs,
+                unsigned long long* kinfo, unsigned long long epoch, int side_b) {
+  __shared__ int s_c[OZ_KMAX], s_h[OZ_KMAX], s_d[OZ_KMAX];
+  for (int k = threadIdx.x; k < OZ_KMAX; k += 256) {
+    int h = OZ_NOEXP, c = OZ_NOEXP;
+    if (k < kb) {
+      h = oz_word_exp(kinfo[OZ_KI_H + k], epoch);
+      c = oz_word_exp(kinfo[OZ_KI_C + k], epoch);
+      if (h == OZ_NOEXP || c == OZ_NOEXP) h = c = OZ_NOEXP;  // k contributes nothing
+    }
+    s_h[k] = h;
+    s_c[k] = c;
+    s_d[k] = (c == OZ_NOEXP) ? OZ_NOEXP : (side_b ? -h : c);
+  }
+  __syncthreads();
   const int nrb = m_pad / 32;
   if ((int)blockIdx.x < nrb) {
     __shared__ unsigned long long tile[64][33];
-    __shared__ unsigned long long red[8][33];
+    __shared__ int redE[8][33], redF[8][33];
     __shared__ int s_e[32];
     __shared__ int s_bad[32];
+    __shared__ int s_G;
     const int i0 = blockIdx.x * 32;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int i = i0 + tx;
-    unsigned long long km = 0ULL;
+    if (ty == 0) {  // G = max_k (c_k + h_k)
+      int g = OZ_NOEXP;
+      for (int q = 0; q < OZ_KMAX / 32; ++q) {
+        const int k = tx + 32 * q;
+        if (s_c[k] != OZ_NOEXP) g = max(g, s_c[k] + s_h[k]);
+      }
+      g = oz_warp_imax(g);
+      if (tx == 0) s_G = g;
+    }
+    int em = OZ_NOEXP, fm = OZ_NOEXP, bad = 0;
     if (i < m)
       for (int kk = ty; kk < kb; kk += 8) {
-        const unsigned long long key =
+        const unsigned long long mag =
             (unsigned long long)__double_as_longlong(A[i + (long long)kk * lda]) & kMagMask;
-        km = key > km ? key : km;
+        if (mag >= kInfBits) {
+          bad = 1;
+        } else if (mag != 0ULL && s_d[kk] != OZ_NOEXP) {
+          const int ex = oz_scale_exp(mag);
+          em = max(em, ex - s_d[kk]);
+          fm = max(fm, ex + s_h[kk]);
+        }
       }
-    red[ty][tx] = km;
+    redE[ty][tx] = bad ? INT_MAX : em;
+    redF[ty][tx] = fm;
     __syncthreads();
     if (ty == 0) {
-      unsigned long long r = 0ULL;
-      for (int q = 0; q < 8; ++q) r = red[q][tx] > r ? red[q][tx] : r;
-      const bool bad = r >= kInfBits;
-      s_bad[tx] = bad ? 1 : 0;
-      s_e[tx] = (bad || r == 0ULL) ? 0 : oz_scale_exp(r);
-      if (i < m_pad) rs[i] = (i < m) ? oz_scale_value(r, bad) : 0.0;
+      int r = OZ_NOEXP, F = OZ_NOEXP;
+      bool anybad = false;
+      for (int q = 0; q < 8; ++q) {
+        anybad |= redE[q][tx] == INT_MAX;
+        r = max(r, redE[q][tx] == INT_MAX ? OZ_NOEXP : redE[q][tx]);
+        F = max(F, redF[q][tx]);
+      }
+      s_bad[tx] = anybad ? 1 : 0;
+      s_e[tx] = r;
+      // side A: row i's bound 2^(e_i + G) against its largest |A||B| term 2^F
+      if (!anybad && r != OZ_NOEXP &&
+          (!oz_scale_in_range(r) || (!side_b && r + s_G - F > OZ_BUDGET)))
+        atomicMax(kinfo + OZ_KI_FLAG, epoch);
+      if (i < m_pad) rs[i] = (i < m) ? oz_scale_value(r, anybad) : 0.0;
     }
     __syncthreads();
     const int r = threadIdx.x >> 3, g = threadIdx.x & 7;  // row r, k group g (8 values)
     const int row = i0 + r;
     const int e = s_e[r];
-    const bool zero = s_bad[r] != 0;
+    const bool zero = s_bad[r] != 0 || e == OZ_NOEXP;
     for (int k0 = 0; k0 < kpad; k0 += 64) {
       for (int q = ty; q < 64; q += 8) {
         const int kk = k0 + q;
@@ -466,9 +684,11 @@ oz_split_kernel(const double* __restrict__ A, long long lda, int m, const double
       bool neg[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
+        const int kk = k0 + g * 8 + q;
         const unsigned long long bits = tile[g * 8 + q][r];
         neg[q] = (bits >> 63) != 0ULL;
-        U[q] = zero ? 0ULL : oz_fixed(bits & kMagMask, e);
+        const int d = s_d[kk];
+        U[q] = (zero || d == OZ_NOEXP) ? 0ULL : oz_fixed(bits & kMagMask, e + d);
       }
       if (row < m_pad) {
 #pragma unroll
@@ -489,28 +709,40 @@ oz_split_kernel(const double* __restrict__ A, long long lda, int m, const double
   const int lane = threadIdx.x & 31;
   if (j >= n_pad) return;
   unsigned long long bits[OZ_KMAX / 32];
-  unsigned long long km = 0ULL;
+  int f = OZ_NOEXP, F = OZ_NOEXP, gg = OZ_NOEXP, bad = 0;
 #pragma unroll
   for (int q = 0; q < OZ_KMAX / 32; ++q) {
     const int kk = lane + 32 * q;
     bits[q] = (j < n && kk < kb) ? (unsigned long long)__double_as_longlong(B[kk + (long long)j * ldb]) : 0ULL;
-    const unsigned long long key = bits[q] & kMagMask;
-    km = key > km ? key : km;
+    const unsigned long long mag = bits[q] & kMagMask;
+    if (s_d[kk] != OZ_NOEXP) gg = max(gg, s_c[kk] + s_h[kk]);
+    if (mag >= kInfBits) {
+      bad = 1;
+    } else if (mag != 0ULL && s_d[kk] != OZ_NOEXP) {
+      const int ex = oz_scale_exp(mag);
+      f = max(f, ex + s_d[kk]);
+      F = max(F, s_c[kk] + ex);
+    }
   }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const unsigned long long o = __shfl_xor_sync(0xffffffffu, km, off);
-    km = o > km ? o : km;
+  f = oz_warp_imax(f);
+  F = oz_warp_imax(F);
+  gg = oz_warp_imax(gg);
+  bad = __any_sync(0xffffffffu, bad) ? 1 : 0;
+  if (lane == 0) {
+    cs[j] = (j < n) ? oz_scale_value(f, bad != 0) : 0.0;
+    // side B: column j's bound 2^(f_j + G) against its largest |A||B| term 2^F
+    if (j < n && !bad && f != OZ_NOEXP &&
+        (!oz_scale_in_range(f) || (side_b && f + gg - F > OZ_BUDGET)))
+      atomicMax(kinfo + OZ_KI_FLAG, epoch);
   }
-  const bool bad = km >= kInfBits;
-  const int e = (bad || km == 0ULL) ? 0 : oz_scale_exp(km);
-  if (lane == 0) cs[j] = (j < n) ? oz_scale_value(km, bad) : 0.0;
 #pragma unroll
   for (int q = 0; q < OZ_KMAX / 32; ++q) {
     const int kk = lane + 32 * q;
     if (kk >= kpad) break;
     const bool neg = (bits[q] >> 63) != 0ULL;
-    const unsigned long long U = bad ? 0ULL : oz_fixed(bits[q] & kMagMask, e);
+    const int d = s_d[kk];
+    const unsigned long long U =
+        (bad || f == OZ_NOEXP || d == OZ_NOEXP) ? 0ULL : oz_fixed(bits[q] & kMagMask, f - d);
 #pragma unroll
     for (int sl = 0; sl < OZ_S; ++sl) Sb[((size_t)sl * n_pad + j) * kpad + kk] = oz_slice_bf16(U, sl, neg);
   }
@@ -548,18 +780,31 @@ void oz_set_tiles_per_cta(int t) { g_oz_tiles_per_cta = t < 1 ? 1 : (t > 4096 ? 
 size_t oz_scratch_bytes(int m, int n, int k) {
   const size_t kp = (size_t)round_up(k < OZ_KMAX ? k : OZ_KMAX, OBK);
   const size_t mp = (size_t)round_up(m, OBM), np = (size_t)round_up(n, OBN);
-  return OZ_S * (mp + np) * kp * 2 + (mp + np) * sizeof(double) + 1024;
+  return OZ_KINFO_BYTES + OZ_S * (mp + np) * kp * 2 + (mp + np) * sizeof(double) + 1024;
 }
 
 bool oz_fits(const OzScratch& sc, int m, int n, int k) {
   return sc.ptr && oz_scratch_bytes(m, n, k) <= sc.bytes;
 }
 
+// Passes that took the FP64 route on the current device since the library
+// loaded (the count lives in device memory).
+long long oz_fp64_routes() {
+  unsigned long long v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_oz_fp64_routes, sizeof(v)) != cudaSuccess) return -1;
+  return (long long)v;
+}
+
+// Epochs only grow (process-wide, 52 bits: no wrap in practice).
+static std::atomic<unsigned long long> g_oz_epochs{0};
+
 // C (m x n) += alpha * A (m x k) * B (k x n), all FP64 column-major, through
-// the sliced BF16 product; K is taken in passes of at most 256.
-cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, const double* A,
-                     long long lda, const double* B, long long ldb, double* C, long long ldc,
-                     int* status, cudaStream_t s) {
+// the sliced BF16 product; K is taken in passes of at most 256, each with its
+// own balancing, budget test and (when the test trips) FP64 route.
+static cudaError_t oz_dgemm_impl(int side_b, const OzScratch& sc, int m, int n, int k,
+                                 double alpha, const double* A, long long lda, const double* B,
+                                 long long ldb, double* C, long long ldc, int* status,
+                                 cudaStream_t s) {
   if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
   if (!oz_fits(sc, m, n, k)) return cudaErrorMemoryAllocation;
   SL_TRY(oz_smem_once());
@@ -567,14 +812,20 @@ cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, con
   for (int k0 = 0; k0 < k; k0 += OZ_KMAX) {
     const int kb = (k - k0) < OZ_KMAX ? (k - k0) : OZ_KMAX;
     const int kpad = round_up(kb, OBK);
+    const unsigned long long epoch = (g_oz_epochs.fetch_add(1) + 1) & ((1ULL << 52) - 1);
     unsigned char* p = reinterpret_cast<unsigned char*>(sc.ptr);
-    __nv_bfloat16* sa = reinterpret_cast<__nv_bfloat16*>(p);
+    unsigned long long* kinfo = reinterpret_cast<unsigned long long*>(p);
+    __nv_bfloat16* sa = reinterpret_cast<__nv_bfloat16*>(p + OZ_KINFO_BYTES);
     __nv_bfloat16* sb = sa + (size_t)OZ_S * m_pad * kpad;
     double* rs = reinterpret_cast<double*>(sb + (size_t)OZ_S * n_pad * kpad);
     double* cs = rs + m_pad;
-    oz_split_kernel<<<m_pad / 32 + n_pad / 8, 256, 0, s>>>(A + (long long)k0 * lda, lda, m, B + k0,
-                                                          ldb, n, kb, kpad, m_pad, n_pad, sa, sb,
-                                                          rs, cs);
+    const double* Ak = A + (long long)k0 * lda;
+    const double* Bk = B + k0;
+    const int nab = (m + 31) / 32, nbb = (n + 63) / 64;
+    oz_kscale_kernel<<<nab + nbb, 256, 0, s>>>(Ak, lda, m, Bk, ldb, n, kb, nab, kinfo, epoch);
+    oz_split_kernel<<<m_pad / 32 + n_pad / 8, 256, 0, s>>>(Ak, lda, m, Bk, ldb, n, kb, kpad, m_pad,
+                                                          n_pad, sa, sb, rs, cs, kinfo, epoch,
+                                                          side_b);
     CUtensorMap ta, tb;
     if (!make_slice_map(&ta, sa, OZ_S * m_pad, kpad, OBM) ||
         !make_slice_map(&tb, sb, OZ_S * n_pad, kpad, OBN))
@@ -586,11 +837,24 @@ cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, con
     const int tpc = std::max(1, std::min(g_oz_tiles_per_cta, tiles / num_sms()));
     const int grid = (tiles + tpc - 1) / tpc;
     ozgemm_kernel<<<grid, OZ_THREADS, oz_smem_bytes(), s>>>(ta, tb, m, n, kpad, m_pad, n_pad, rs,
-                                                            cs, alpha, C, ldc, tpc, status);
-    count_launches(2);
+                                                            cs, alpha, C, ldc, tpc, status, Ak,
+                                                            lda, Bk, ldb, kb, kinfo, epoch);
+    count_launches(3);
     SL_TRY(cudaGetLastError());
   }
   return cudaSuccess;
+}
+
+cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, const double* A,
+                     long long lda, const double* B, long long ldb, double* C, long long ldc,
+                     int* status, cudaStream_t s) {
+  return oz_dgemm_impl(0, sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, status, s);
+}
+
+cudaError_t oz_dgemm_bside(const OzScratch& sc, int m, int n, int k, double alpha,
+                           const double* A, long long lda, const double* B, long long ldb,
+                           double* C, long long ldc, int* status, cudaStream_t s) {
+  return oz_dgemm_impl(1, sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, status, s);
 }
 
 }  // namespace sl

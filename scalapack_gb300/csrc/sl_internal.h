@@ -59,11 +59,22 @@ size_t oz_scratch_bytes(int m, int n, int k);
 void oz_set_tiles_per_cta(int t);
 bool oz_fits(const OzScratch& sc, int m, int n, int k);
 // C (m x n) += alpha * A (m x k) * B (k x n), FP64, column-major, on the BF16
-// tensor cores through exact 7-bit slices (needs oz_fits). B is read in full
-// (sliced) before C is written, so B may alias C.
+// tensor cores through exact 7-bit slices (needs oz_fits), balanced by the
+// column maxima of A; a pass whose slices would exceed the error budget is
+// computed in FP64 arithmetic by the same launches. B may alias C when
+// m <= 128 (each tile covers all rows, and its columns of B are read before
+// any of them is written).
 cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, const double* A,
                      long long lda, const double* B, long long ldb, double* C, long long ldc,
                      int* status, cudaStream_t s);
+// The same balanced by the row maxima of B, with the budget tested per
+// column: for A = inv(T) - I of a unit-lower diagonal block T and B the rows
+// it updates (the U12 solve), whose rows carry the pivots' scales.
+cudaError_t oz_dgemm_bside(const OzScratch& sc, int m, int n, int k, double alpha,
+                           const double* A, long long lda, const double* B, long long ldb,
+                           double* C, long long ldc, int* status, cudaStream_t s);
+// Sliced-product passes that took the FP64 route on the current device.
+long long oz_fp64_routes();
 // Trailing-update arithmetic of the FP64 factorization: 0 = FP64 DMMA,
 // 1 = sliced BF16 tensor-core product (when its scratch is present).
 void f64_update_set(int mode);

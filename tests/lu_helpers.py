@@ -5,6 +5,7 @@ from __future__ import annotations
 
 import numpy as np
 
+PADVAL = -9923.0  # the tester's guard value (pdludriver.f:77-79)
 NEAR_TIE_REL = 1e-10  # columns whose top-2 |candidates| differ by less are logged
 RESID_THRESH = 16.0   # scaled-residual bar for every FP64 run
 
@@ -46,3 +47,35 @@ def compare_ipiv(orc, A0, gpu_ipiv_rel, nb, max_replays=4):
             continue
         return int(bad.size), sorted(set(logged))
     return int(np.count_nonzero(ip != g)), sorted(set(logged))
+
+
+def padded(a, pad_rows=3, pad_cols=2, ia=1, ja=1):
+    """Embed `a` at (ia, ja) of a larger Fortran array filled with PADVAL."""
+    m, n = a.shape
+    big = np.full((ia - 1 + m + pad_rows, ja - 1 + n + pad_cols), PADVAL, order="F")
+    big[ia - 1:ia - 1 + m, ja - 1:ja - 1 + n] = a
+    return big
+
+
+def guards_intact(big, ia, ja, m, n):
+    mask = np.ones(big.shape, dtype=bool)
+    mask[ia - 1:ia - 1 + m, ja - 1:ja - 1 + n] = False
+    return bool(np.all(big[mask] == PADVAL))
+
+
+def run_pdgesv(sl, ctx, A0, B0, nb, ia=1, ja=1):
+    n, nrhs = A0.shape[0], B0.shape[1]
+    Ab = padded(A0, ia=ia, ja=ja)
+    Bb = padded(B0, ia=ia, ja=1)
+    desca = np.array([1, ctx, Ab.shape[0], Ab.shape[1], nb, nb, 0, 0, Ab.shape[0]], np.int32)
+    descb = np.array([1, ctx, Bb.shape[0], Bb.shape[1], nb, nb, 0, 0, Bb.shape[0]], np.int32)
+    ipiv = np.full(Ab.shape[0] + nb + 4, -77, dtype=np.int32)
+    info = sl.pdgesv(n, nrhs, Ab, ia, ja, desca, ipiv, Bb, ia, 1, descb)
+    assert guards_intact(Ab, ia, ja, n, n)
+    assert guards_intact(Bb, ia, 1, n, nrhs)
+    # IPIV entries outside IPIV(IA:IA+N-1) are untouched
+    assert np.all(ipiv[:ia - 1] == -77) and np.all(ipiv[ia - 1 + n:] == -77)
+    LU = Ab[ia - 1:ia - 1 + n, ja - 1:ja - 1 + n]
+    X = Bb[ia - 1:ia - 1 + n, :nrhs]
+    rel = ipiv[ia - 1:ia - 1 + n] - (ia - 1)
+    return info, np.asfortranarray(LU), rel, np.asfortranarray(X)

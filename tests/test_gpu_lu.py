@@ -12,49 +12,14 @@ import os
 import numpy as np
 import pytest
 
-from lu_helpers import RESID_THRESH, compare_ipiv, system
+from lu_helpers import PADVAL, RESID_THRESH, compare_ipiv, guards_intact, padded, run_pdgesv, system
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
-PADVAL = -9923.0  # the tester's guard value (pdludriver.f:77-79)
-
-
 @pytest.fixture(scope="module")
 def ctx(sl, gpu_required):
     assert sl.lib().sl1x1_device_ok() == 1
     return sl.blacs_gridinit(1, 1)
-
-
-def padded(a, pad_rows=3, pad_cols=2, ia=1, ja=1):
-    """Embed `a` at (ia, ja) of a larger Fortran array filled with PADVAL."""
-    m, n = a.shape
-    big = np.full((ia - 1 + m + pad_rows, ja - 1 + n + pad_cols), PADVAL, order="F")
-    big[ia - 1:ia - 1 + m, ja - 1:ja - 1 + n] = a
-    return big
-
-
-def guards_intact(big, ia, ja, m, n):
-    mask = np.ones(big.shape, dtype=bool)
-    mask[ia - 1:ia - 1 + m, ja - 1:ja - 1 + n] = False
-    return bool(np.all(big[mask] == PADVAL))
-
-
-def run_pdgesv(sl, ctx, A0, B0, nb, ia=1, ja=1):
-    n, nrhs = A0.shape[0], B0.shape[1]
-    Ab = padded(A0, ia=ia, ja=ja)
-    Bb = padded(B0, ia=ia, ja=1)
-    desca = np.array([1, ctx, Ab.shape[0], Ab.shape[1], nb, nb, 0, 0, Ab.shape[0]], np.int32)
-    descb = np.array([1, ctx, Bb.shape[0], Bb.shape[1], nb, nb, 0, 0, Bb.shape[0]], np.int32)
-    ipiv = np.full(Ab.shape[0] + nb + 4, -77, dtype=np.int32)
-    info = sl.pdgesv(n, nrhs, Ab, ia, ja, desca, ipiv, Bb, ia, 1, descb)
-    assert guards_intact(Ab, ia, ja, n, n)
-    assert guards_intact(Bb, ia, 1, n, nrhs)
-    # IPIV entries outside IPIV(IA:IA+N-1) are untouched
-    assert np.all(ipiv[:ia - 1] == -77) and np.all(ipiv[ia - 1 + n:] == -77)
-    LU = Ab[ia - 1:ia - 1 + n, ja - 1:ja - 1 + n]
-    X = Bb[ia - 1:ia - 1 + n, :nrhs]
-    rel = ipiv[ia - 1:ia - 1 + n] - (ia - 1)
-    return info, np.asfortranarray(LU), rel, np.asfortranarray(X)
 
 
 # NB 320 exceeds the composite row-interchange table (256 pivots) and takes the
@@ -185,11 +150,14 @@ def test_config_n2048_nb64(sl, orc, ctx):
 
 @pytest.mark.parametrize("m,n,nb", [(2048, 2048, 64), (1000, 1000, 64), (3000, 3000, 256),
                                     (1500, 900, 64), (700, 1300, 64), (600, 600, 256)])
-def test_host_path_chunked_copy_bitwise(sl, orc, ctx, m, n, nb):
+def test_host_path_chunked_copy_matches_device_path(sl, orc, ctx, m, n, nb):
     # pdgetrf_ / pdgesv_ copy A to the GPU in column chunks and run step 0 of
     # the factorization chunk by chunk as they land; the device entry points
-    # get A whole. Every step-0 operation is per column, so factors, pivots
-    # and solution must be bitwise the same.
+    # get A whole. The interchanges and the trailing update are per column;
+    # the U12 solve's first product balances its slices by the row maxima of
+    # the columns it is given, so step 0's U12 rows agree to rounding rather
+    # than bitwise. Pivots must be identical, factors and solution equal to
+    # rounding.
     import torch
 
     rng = np.random.default_rng(m * 7 + n + nb)
@@ -205,7 +173,8 @@ def test_host_path_chunked_copy_bitwise(sl, orc, ctx, m, n, nb):
     ipiv = np.zeros(m + nb, np.int32)
     assert sl.pdgetrf(m, n, LU, 1, 1, desca, ipiv) == 0
     np.testing.assert_array_equal(ipiv[:mn], piv_dev)
-    np.testing.assert_array_equal(LU, LU_dev)
+    scale = np.max(np.abs(LU_dev), axis=1, keepdims=True)
+    assert np.max(np.abs(LU - LU_dev) / scale) < 1e-10
     if m == n:
         B0 = np.asfortranarray(rng.uniform(-0.5, 0.5, (n, 3)))
         dA = torch.from_numpy(np.ascontiguousarray(A0.T)).cuda()
@@ -215,8 +184,9 @@ def test_host_path_chunked_copy_bitwise(sl, orc, ctx, m, n, nb):
         LU2, X = np.asfortranarray(A0.copy()), np.asfortranarray(B0.copy())
         descb = np.array([1, ctx, n, 3, nb, nb, 0, 0, n], np.int32)
         assert sl.pdgesv(n, 3, LU2, 1, 1, desca, ipiv, X, 1, 1, descb) == 0
-        np.testing.assert_array_equal(LU2, LU_dev)
-        np.testing.assert_array_equal(X, X_dev)
+        assert np.max(np.abs(LU2 - LU_dev) / scale) < 1e-10
+        assert np.max(np.abs(X - X_dev)) <= 1e-10 * np.max(np.abs(X_dev))
+        assert orc.sresid(A0, B0, X) < RESID_THRESH
 
 
 def test_config_n16384_nb256_full_size(sl, orc, ctx):

@@ -10,7 +10,11 @@
   no worse than FP64 DMMA's on the same product;
 * K above 256 runs in passes; Inf and NaN poison their row or column;
 * the LU with the sliced update gives the same pivots as with the DMMA one
-  and the same scaled residuals bar.
+  and the same scaled residuals bar;
+* the power-of-two balancing along k keeps row-graded operands (an LU step
+  whose pivots span 2^+-20 .. 2^+-300) at componentwise FP64 accuracy, and
+  operands outside the error budget take the FP64 route (counted by
+  sl1x1_ozgemm_fp64_routes), pass by pass, with C aliasing B allowed.
 """
 import math
 from fractions import Fraction
@@ -44,14 +48,19 @@ def run_oz(sl, torch, dev, A, B, C, alpha=-1.0):
 def exact_update(A, B, C, alpha):
     """The sliced product's result for operands whose row / column slices are
     all exact (<= 21 bits below each scale): one pass per 256 columns of K,
-    I = 2^52 (A B)_ij / 2^(e_i + f_j) rounded once to FP64, then one FMA."""
+    I = 2^52 (A B)_ij / 2^(e_i + f_j) rounded once to FP64, then one FMA,
+    with e_i, f_j the balanced scale exponents (tests/oz_model.py)."""
+    from oz_model import scales
+
     m, k = A.shape
     n = B.shape[1]
     out = C.copy()
     for k0 in range(0, k, 256):
         Ak, Bk = A[:, k0:k0 + 256], B[k0:k0 + 256, :]
-        e = [math.frexp(float(np.max(np.abs(Ak[i]))))[1] if np.any(Ak[i]) else 0 for i in range(m)]
-        f = [math.frexp(float(np.max(np.abs(Bk[:, j]))))[1] if np.any(Bk[:, j]) else 0 for j in range(n)]
+        e, f, tripped, _ = scales(Ak, Bk)
+        assert not tripped
+        e = [0 if v is None else v for v in e]
+        f = [0 if v is None else v for v in f]
         Af = [[Fraction(float(x)) for x in Ak[i]] for i in range(m)]
         Bf = [[Fraction(float(x)) for x in Bk[:, j]] for j in range(n)]
         for i in range(m):
@@ -199,3 +208,123 @@ def test_tiles_per_cta_changes_only_speed(sl, torch_dev):
         L.sl1x1_set_ozgemm_tiles(4)
     np.testing.assert_array_equal(outs[0], outs[1])
     np.testing.assert_array_equal(outs[0], outs[2])
+
+
+def _routes(sl):
+    r = sl.lib().sl1x1_ozgemm_fp64_routes()
+    assert r >= 0
+    return r
+
+
+def _componentwise_ok(got, A, B, C, alpha, c):
+    """|got - exact| <= c K eps (|A||B|)_ij + 2 eps |exact|, exact in wide
+    arithmetic; returns the worst ratio to that bound."""
+    ref = _wide(C) + alpha * (_wide(A) @ _wide(B))
+    absab = np.abs(A) @ np.abs(B)
+    k = A.shape[1]
+    eps = 2.0 ** -53
+    err = np.abs((got.astype(np.longdouble) - ref).astype(np.float64))
+    tol = c * k * eps * absab + 2 * eps * np.abs(ref.astype(np.float64)) + 1e-300
+    return float(np.max(err / tol))
+
+
+@pytest.mark.parametrize("spread", [20, 60, 300])
+def test_row_graded_operands_componentwise(sl, torch_dev, spread):
+    """L21 / U12 of a row-graded LU step (pivots spanning 2^+-spread inside one
+    block): the balancing keeps every entry within a few units of 2^-53 of
+    its own |A||B| (without it the error scale would exceed the terms by
+    more than the spread, in bits), and no pass takes the FP64 route."""
+    from oz_model import graded_lu_operands, scales
+
+    torch, dev = torch_dev
+    rng = np.random.default_rng(spread)
+    m, k, n = 300, 256, 200
+    A, B = graded_lu_operands(rng, m, k, n, spread)
+    assert not scales(A, B)[2]
+    C = (np.abs(A) @ np.abs(B)) * rng.uniform(-1, 1, (m, n))
+    r0 = _routes(sl)
+    got = run_oz(sl, torch, dev, A, B, C, alpha=-1.0)
+    assert _routes(sl) == r0
+    assert _componentwise_ok(got, A, B, C, -1.0, c=2.0) <= 1.0
+
+
+@pytest.mark.parametrize("spread", [0, 40])
+def test_column_and_row_scaled_operands(sl, torch_dev, spread):
+    """Operands scaled by powers of two on both sides (D1 A D2, D2^-1 B D3):
+    the result is that of the unscaled product to componentwise accuracy."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(100 + spread)
+    m, k, n = 257, 190, 130
+    d = np.exp2(rng.integers(-spread, spread + 1, size=k))
+    A = rng.uniform(-1, 1, (m, k)) * d[None, :]
+    A *= np.exp2(rng.integers(-spread, spread + 1, size=(m, 1)))
+    B = rng.uniform(-1, 1, (k, n)) / d[:, None]
+    B *= np.exp2(rng.integers(-spread, spread + 1, size=(1, n)))
+    C = np.zeros((m, n))
+    r0 = _routes(sl)
+    got = run_oz(sl, torch, dev, A, B, C, alpha=1.0)
+    assert _routes(sl) == r0
+    assert _componentwise_ok(got, A, B, C, 1.0, c=2.0) <= 1.0
+
+
+def test_spike_operands_take_fp64_route(sl, torch_dev):
+    """A row of B with one entry 2^40 above the rest, met by a 2^-50 entry of
+    A: the row budget test trips, the pass runs in FP64 arithmetic, and every
+    entry is within the FP64 GEMM's componentwise bound."""
+    from oz_model import scales, spike_operands
+
+    torch, dev = torch_dev
+    rng = np.random.default_rng(31)
+    m, k, n = 300, 200, 150
+    A, B = spike_operands(rng, m, k, n)
+    assert scales(A, B)[2]
+    C = rng.uniform(-1, 1, (m, n))
+    r0 = _routes(sl)
+    got = run_oz(sl, torch, dev, A, B, C, alpha=-1.0)
+    assert _routes(sl) == r0 + 1
+    assert _componentwise_ok(got, A, B, C, -1.0, c=1.0) <= 1.0
+    # the next product is sliced again: the route flag belongs to its pass
+    A2 = rng.uniform(-1, 1, (m, k))
+    B2 = rng.uniform(-1, 1, (k, n))
+    got2 = run_oz(sl, torch, dev, A2, B2, C, alpha=-1.0)
+    assert _routes(sl) == r0 + 1
+    assert _componentwise_ok(got2, A2, B2, C, -1.0, c=4.0) <= 1.0
+
+
+def test_fp64_route_per_pass_of_k(sl, torch_dev):
+    """K = 300 runs in two passes; only the second is outside the budget."""
+    from oz_model import spike_operands
+
+    torch, dev = torch_dev
+    rng = np.random.default_rng(32)
+    m, n = 200, 100
+    A1 = rng.uniform(-1, 1, (m, 256))
+    B1 = rng.uniform(-1, 1, (256, n))
+    A2, B2 = spike_operands(rng, m, 44, n)
+    A = np.hstack([A1, A2])
+    B = np.vstack([B1, B2])
+    C = rng.uniform(-1, 1, (m, n))
+    r0 = _routes(sl)
+    got = run_oz(sl, torch, dev, A, B, C, alpha=-1.0)
+    assert _routes(sl) == r0 + 1
+    assert _componentwise_ok(got, A, B, C, -1.0, c=4.0) <= 1.0
+
+
+def test_fp64_route_with_c_aliasing_b(sl, torch_dev):
+    """The U12 solve's form C = B, m = k <= 128: on the FP64 route each tile
+    reads its columns of B before writing them."""
+    from oz_model import spike_operands
+
+    torch, dev = torch_dev
+    rng = np.random.default_rng(33)
+    k, n = 64, 300
+    A, B = spike_operands(rng, k, k, n)
+    dA = torch.from_numpy(np.ascontiguousarray(A.T)).to(dev)
+    dB = torch.from_numpy(np.ascontiguousarray(B.T)).to(dev)
+    r0 = _routes(sl)
+    rc = sl.ozgemm_dev(k, n, k, 1.0, dA.data_ptr(), k, dB.data_ptr(), k, dB.data_ptr(), k)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert _routes(sl) == r0 + 1
+    got = dB.cpu().numpy().T
+    assert _componentwise_ok(got, A, B, B, 1.0, c=1.0) <= 1.0

@@ -101,3 +101,75 @@ def test_combined_integer_fits_int64():
     assert worst + tail < 2 ** 63
     # and the conversion to FP64 rounds once: the value has at most 61 significant bits
     assert (worst + tail).bit_length() <= 62
+
+
+# ---- balancing along k and the error budget (tests/oz_model.py) ----------
+
+def test_balancing_removes_the_pivot_spread_of_a_graded_step():
+    """Row-graded LU step: without the balancing the error scale 2^(e_i+f_j)
+    exceeds the largest term of some entry by more than the spread of the
+    block's pivots (in bits); with it, by a couple of bits, and the pass stays
+    inside the budget."""
+    import oz_model as M
+
+    rng = np.random.default_rng(3)
+    for spread in (20, 60, 300):
+        A, B = M.graded_lu_operands(rng, 120, 64, 90, spread)
+        assert M.bound_gap_bits(A, B, balance=False) > spread
+        assert M.bound_gap_bits(A, B) < 3.0
+        assert not M.scales(A, B)[2]
+
+
+def test_side_b_for_the_graded_inverse_product():
+    """(inv(L_bb) - I) A12_b on a graded block: balancing by A's columns
+    leaves rows whose terms sit far below their scale (the budget trips),
+    balancing by B's rows lines every term up."""
+    import oz_model as M
+
+    rng = np.random.default_rng(7)
+    A, B = M.graded_inverse_operands(rng, 64, 80, 60)
+    assert M.scales(A, B, side="A")[2]
+    assert not M.scales(A, B, side="B")[2]
+    # entrywise, side B's error scale sits about the pivots' spread closer
+    # to the terms than side A's
+    assert M.bound_gap_bits(A, B, side="B") < M.bound_gap_bits(A, B, side="A") - 20
+
+
+def test_budget_passes_well_scaled_and_diagonally_scaled_operands():
+    import oz_model as M
+
+    rng = np.random.default_rng(4)
+    A = rng.uniform(-0.5, 0.5, (300, 256))
+    B = rng.uniform(-0.5, 0.5, (256, 200)) * 40
+    assert not M.scales(A, B)[2]
+    d = np.exp2(rng.integers(-200, 200, size=256))
+    assert not M.scales(A / d[None, :], B * d[:, None])[2]  # any scaling along k
+    r = np.exp2(rng.integers(-200, 200, size=300))
+    c = np.exp2(rng.integers(-200, 200, size=200))
+    assert not M.scales(A * r[:, None], B * c[None, :])[2]
+
+
+def test_budget_trips_where_no_balancing_helps():
+    """A row of B with one entry 2^40 above the rest, met by a 2^-50 entry of
+    A: row 0's largest term needs the k = 0 product in full, but row 0's
+    scale is set by the other k, so the slices keep only 6 of its bits."""
+    import oz_model as M
+
+    rng = np.random.default_rng(5)
+    A, B = M.spike_operands(rng, 60, 32, 40)
+    e, f, tripped, info = M.scales(A, B)
+    assert tripped
+    assert info["gap"][0] > 30
+    big = np.abs(A[:, 0]) >= 0.5  # rows whose k = 0 entry is near column 0's maximum pass
+    assert np.all(info["gap"][big] <= M.BUDGET)
+    assert M.bound_gap_bits(A, B) > 30
+
+
+def test_budget_trips_when_a_scale_leaves_the_normal_range():
+    import oz_model as M
+
+    rng = np.random.default_rng(6)
+    A = rng.uniform(-1, 1, (10, 8)) * 2.0 ** -1000
+    B = rng.uniform(-1, 1, (8, 6))
+    assert M.scales(A, B)[2]  # e_i - 26 below the normal range
+    assert not M.scales(A * 2.0 ** 1000, B)[2]
