@@ -172,13 +172,74 @@ unit_lower_inv64_kernel(int jb, const double* __restrict__ L, long long ldl, dou
   }
 }
 
-// U12 = L11^-1 A12 (jb x nr, in place). With the sliced product and the
-// diagonal-block inverses of L11 at hand (formed at the end of its panel):
-// per 64-row block b, X_b = A12_b + (inv(L_bb) - I) A12_b, then the rows below
-// lose L(below, b) X_b -- every product on the tensor cores. Otherwise the
+// Largest NB whose whole inv(L11) - I is formed at the end of the panel (the
+// U12 solve is then one product); larger blocks use 64-row inverses.
+constexpr int kFullInvMax = 256;
+
+// X = inv(L) - I for a unit-lower jb x jb L (jb <= 256), one warp per column
+// c: x = e_c, then for q = c, c+1, ... x_q is final and every row i > q loses
+// L(i,q) x_q -- forward substitution in the order of a strip solve, with x_q
+// passed by a shuffle from the lane that owns row q (lane l owns rows l, l+32,
+// ..., in registers). The CTA's 8 warps stage L 32 columns at a time in
+// shared memory (rows from the chunk's first column down), so the 32 steps of
+// a chunk read shared memory only and no block barrier sits inside them.
+constexpr int kInvColsSmem = 32 * 257 * (int)sizeof(double);
+__global__ void __launch_bounds__(256)
+unit_lower_inv_cols_kernel(int jb, const double* __restrict__ L, long long ldl, double* X,
+                           int ldx) {
+  extern __shared__ double inv_ls[];  // Ls[l * 257 + i] = L(i, 32 tq + l)
+  const int lane = threadIdx.x & 31;
+  const int c = (int)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int cmin = (int)blockIdx.x * 8;
+  double xr[8];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) xr[t] = (lane + 32 * t == c) ? 1.0 : 0.0;
+#pragma unroll
+  for (int tq = 0; tq < 8; ++tq) {
+    const int q0 = 32 * tq;
+    if (q0 >= jb) break;
+    if (q0 + 31 < cmin) continue;  // no column of this CTA starts before the chunk ends
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < 32 * 256; idx += 256) {
+      const int l = idx >> 8, i = idx & 255;
+      if (q0 + l < jb && i > q0 + l && i < jb) inv_ls[l * 257 + i] = L[i + (long long)(q0 + l) * ldl];
+    }
+    __syncthreads();
+    if (c < jb && q0 + 31 >= c) {
+      for (int l = 0; l < 32; ++l) {
+        const int q = q0 + l;
+        if (q >= jb) break;
+        const double xq = __shfl_sync(0xffffffffu, xr[tq], l);
+        if (q < c) continue;
+        const double* Lq = inv_ls + l * 257;
+#pragma unroll
+        for (int t = tq; t < 8; ++t) {
+          const int i = lane + 32 * t;
+          if (i > q && i < jb) xr[t] = fma(-Lq[i], xq, xr[t]);
+        }
+      }
+    }
+  }
+  if (c < jb) {
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int i = lane + 32 * t;
+      if (i < jb) X[i + (long long)c * ldx] = (i > c) ? xr[t] : 0.0;
+    }
+  }
+}
+
+// U12 = L11^-1 A12 (jb x nr, in place). With the sliced product and inverses
+// of L11 at hand (formed at the end of its panel): for jb <= 256,
+// U12 = A12 + (inv(L11) - I) A12 as one product; otherwise per 64-row block
+// b, X_b = A12_b + (inv(L_bb) - I) A12_b, then the rows below lose
+// L(below, b) X_b -- every product on the tensor cores, the inverse products
+// balanced by the rows of A12, which carry the pivots' scales. Otherwise the
 // FP64 strip solve.
 static cudaError_t solve_u12(int jb, int nr, const double* L11, long long ldl, double* A12,
                              long long lda, const LuWork& ws, cudaStream_t s) {
+  if (g_f64_update == 1 && ws.dinv64 && jb <= kFullInvMax && oz_fits(ws.oz, jb, nr, jb))
+    return oz_dgemm_bside(ws.oz, jb, nr, jb, 1.0, ws.dinv64, jb, A12, lda, A12, lda, ws.status, s);
   if (!(g_f64_update == 1 && ws.dinv64 && jb <= 1024 && oz_fits(ws.oz, jb, nr, 64)))
     return trsm_strip<double, false, false, true>(jb, nr, L11, ldl, A12, lda, s);
   for (int r0 = 0; r0 < jb; r0 += 64) {
@@ -224,7 +285,16 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
   const int npiv = (m - j) < jb ? (m - j) : jb;
   if (ws.swap_plan && npiv <= LSW_MAXP) SL_TRY(laswp_plan(j, j + npiv, dipiv, ws.swap_plan, s));
   // inverses of L11's diagonal blocks for the U12 solve of this step
-  if (g_f64_update == 1 && ws.dinv64 && npiv == jb && jb <= 1024) {
+  if (g_f64_update == 1 && ws.dinv64 && npiv == jb && jb <= kFullInvMax) {
+    // inv(L11) - I whole (jb x jb, leading dimension jb)
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        unit_lower_inv_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvColsSmem);
+    SL_TRY(attr);
+    unit_lower_inv_cols_kernel<<<(jb + 7) / 8, 256, kInvColsSmem, s>>>(jb, Ap(j, j), ldda,
+                                                                      ws.dinv64, jb);
+    count_launches(1);
+    SL_TRY(cudaGetLastError());
+  } else if (g_f64_update == 1 && ws.dinv64 && npiv == jb && jb <= 1024) {
     constexpr int kInvSmem = 2 * 64 * 65 * (int)sizeof(double);
     static const cudaError_t attr = cudaFuncSetAttribute(
         unit_lower_inv64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvSmem);
@@ -274,7 +344,8 @@ static cudaError_t step0_by_chunks(int m, int n, double* dA, long long ldda, int
   LuWork w0 = ws;
   w0.swap_plan = nullptr;
   if (g_f64_update == 1 && ws.dinv64) {
-    SL_TRY(cudaMemcpyAsync(ws.dinv64_step0, ws.dinv64, (size_t)((jb + 63) / 64) * 4096 * sizeof(double),
+    SL_TRY(cudaMemcpyAsync(ws.dinv64_step0, ws.dinv64,
+                           (jb <= kFullInvMax ? (size_t)jb * jb : (size_t)((jb + 63) / 64) * 4096) * sizeof(double),
                            cudaMemcpyDeviceToDevice, s));
     w0.dinv64 = ws.dinv64_step0;
   }

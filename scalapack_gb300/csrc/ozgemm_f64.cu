@@ -187,24 +187,36 @@ __device__ __forceinline__ bool oz_issue_b(int c, int first, int nkc, int tiles_
 // The FP64 route of a pass whose slices would exceed the error budget: the
 // CTA's tiles computed directly from the FP64 operands. B's 64 columns of a
 // tile (kb <= 256 rows, 128 KB) are staged in shared memory before any of
-// them is written, so B may alias C where one tile covers all rows (m <= 128).
-// Threads 64.. own one row and 32 columns each; products accumulate in k
-// order with one FMA each, then C = fma(alpha, acc, C).
+// them is written. When B aliases C (whole_cols) a CTA takes whole column
+// blocks instead -- tile t of the CTA is column block t with every row tile --
+// so no other CTA writes the columns it reads. Threads 64.. own one row and
+// 32 columns each; products accumulate in k order with one FMA each, then
+// C = fma(alpha, acc, C).
 __device__ __noinline__ void oz_fp64_tiles(unsigned char* smem, int m, int n, int kb,
                                            const double* __restrict__ A, long long lda,
                                            const double* B, long long ldb, double alpha,
                                            double* C, long long ldc, int first_tile,
-                                           int my_tiles, int tiles_m, int tiles_n) {
+                                           int my_tiles, int tiles_m, int tiles_n,
+                                           int whole_cols) {
   double* sB = reinterpret_cast<double*>(smem);  // [kb][64]
   const int tid = threadIdx.x;
-  for (int it = 0; it < my_tiles; ++it) {
+  const int nsub = whole_cols ? tiles_m : 1;
+  for (int it = 0; it < my_tiles * nsub; ++it) {
     int m0, n0;
-    oz_tile(first_tile + it, tiles_m, tiles_n, m0, n0);
-    __syncthreads();
-    for (int idx = tid; idx < kb * OBN; idx += OZ_THREADS) {
-      const int c = idx / kb, k = idx - c * kb;
-      sB[k * OBN + c] = (n0 + c < n) ? B[k + (long long)(n0 + c) * ldb] : 0.0;
+    if (whole_cols) {
+      const int t = first_tile + it / nsub;
+      if (t >= tiles_n) break;
+      n0 = t * OBN;
+      m0 = (it % nsub) * OBM;
+    } else {
+      oz_tile(first_tile + it, tiles_m, tiles_n, m0, n0);
     }
+    __syncthreads();
+    if (!whole_cols || (it % nsub) == 0)
+      for (int idx = tid; idx < kb * OBN; idx += OZ_THREADS) {
+        const int c = idx / kb, k = idx - c * kb;
+        sB[k * OBN + c] = (n0 + c < n) ? B[k + (long long)(n0 + c) * ldb] : 0.0;
+      }
     __syncthreads();
     if (tid >= 64) {
       const int t = tid - 64, row = m0 + (t & (OBM - 1)), h = t >> 7;
@@ -268,7 +280,7 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
   if (*(volatile const unsigned long long*)(kinfo + OZ_KI_FLAG) == epoch) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&g_oz_fp64_routes, 1ULL);
     oz_fp64_tiles(base, m, n, kb, A64, lda, B64, ldb, alpha, C, ldc, first_tile, my_tiles,
-                  tiles_m, tiles_n);
+                  tiles_m, tiles_n, B64 == C ? 1 : 0);
     return;
   }
 

@@ -61,9 +61,9 @@ bool oz_fits(const OzScratch& sc, int m, int n, int k);
 // C (m x n) += alpha * A (m x k) * B (k x n), FP64, column-major, on the BF16
 // tensor cores through exact 7-bit slices (needs oz_fits), balanced by the
 // column maxima of A; a pass whose slices would exceed the error budget is
-// computed in FP64 arithmetic by the same launches. B may alias C when
-// m <= 128 (each tile covers all rows, and its columns of B are read before
-// any of them is written).
+// computed in FP64 arithmetic by the same launches. B may alias C (same
+// pointer and leading dimension): the slices are cut before C is written, and
+// the FP64 route takes whole column blocks per CTA.
 cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, const double* A,
                      long long lda, const double* B, long long ldb, double* C, long long ldc,
                      int* status, cudaStream_t s);

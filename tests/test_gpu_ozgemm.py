@@ -310,14 +310,16 @@ def test_fp64_route_per_pass_of_k(sl, torch_dev):
     assert _componentwise_ok(got, A, B, C, -1.0, c=4.0) <= 1.0
 
 
-def test_fp64_route_with_c_aliasing_b(sl, torch_dev):
-    """The U12 solve's form C = B, m = k <= 128: on the FP64 route each tile
-    reads its columns of B before writing them."""
+@pytest.mark.parametrize("k", [64, 256])
+def test_fp64_route_with_c_aliasing_b(sl, torch_dev, k):
+    """The U12 solve's form C = B (m = k, up to 256 rows: two row tiles): on
+    the FP64 route each CTA takes whole column blocks and reads its columns
+    of B before writing them."""
     from oz_model import spike_operands
 
     torch, dev = torch_dev
-    rng = np.random.default_rng(33)
-    k, n = 64, 300
+    rng = np.random.default_rng(33 + k)
+    n = 300
     A, B = spike_operands(rng, k, k, n)
     dA = torch.from_numpy(np.ascontiguousarray(A.T)).to(dev)
     dB = torch.from_numpy(np.ascontiguousarray(B.T)).to(dev)
