@@ -212,38 +212,61 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
   }
   __syncthreads();
 
+  // Column k's rank-1 update is applied in two parts: right after its pivot,
+  // only column k+1 (which gives the next pivot search its keys); the rest
+  // (columns k+2..) after column k+1's key has been published, while the
+  // other CTAs' keys are on their way. Every element still receives the
+  // updates of columns 0, 1, ... in order, as one fma each.
+  auto finish_update = [&](int kp) {  // columns kp+2 .. w-1 of the rows below kp
+    for (int r = max(0, kp + 1 - lo) + tid; r < nr; r += PT) {
+      T* rp = tile + r * PLD;
+      const T l = rp[kp];
+#pragma unroll 4
+      for (int j = kp + 2; j < w; ++j) rp[j] = fma(-l, s_U[j], rp[j]);
+    }
+  };
+
   for (int k = 0; k < kw; ++k) {
     const int d = k;  // diagonal row relative to r0
     const int par = k & 1;
     const uint32_t tag = (uint32_t)(k + 1);
-    // --- this CTA's candidate: IDAMAX over its rows >= d ---
+    // --- this CTA's candidate: IDAMAX over its rows >= d; its key goes out
+    //     at once ---
     if (warp == 0) {
       long long key = lane < PT / 32 ? s_wk[lane] : -2;
       int row = lane < PT / 32 ? s_wr[lane] : INT_MAX;
       warp_ikey(key, row);
-      if (lane == 0) { s_lrow = row; s_lkey = key; }
-    }
-    __syncthreads();
-    {
-      // publish the candidate row, the diagonal row (if owned) and the key
-      const int lr = s_lrow;
-      if (tid < w)
-        st_value<T>(valw + ((size_t)b * 2 + par) * 2 * PW, tid,
-                    lr != INT_MAX ? tile[(lr - lo) * PLD + tid] : (T)0, tag);
-      if (d >= lo && d < lo + nr && tid < w)
-        st_value<T>(diagw + par * 2 * PW, tid, tile[(d - lo) * PLD + tid], tag);
-      if (tid == 0) {
-        const unsigned long long kb = (unsigned long long)s_lkey;
+      if (lane == 0) {
+        s_lrow = row;
+        s_lkey = key;
+        const unsigned long long kb = (unsigned long long)key;
         unsigned long long* kw4 = keyw + ((size_t)par * PMAXG + b) * 4;
         st_tagged(kw4 + 0, (uint32_t)kb, tag);
         st_tagged(kw4 + 1, (uint32_t)(kb >> 32), tag);
-        st_tagged(kw4 + 2, (uint32_t)lr, tag);
+        st_tagged(kw4 + 2, (uint32_t)row, tag);
+      }
+    }
+    __syncthreads();
+    {
+      // the rest of column k-1's update, then the candidate row and the
+      // diagonal row (if owned), each published by its owner warp
+      if (k > 0) finish_update(k - 1);
+      // finish_update(k-1) hands row r (of this CTA) to thread (r - st) % PT
+      const int st = max(0, k - lo);
+      const int lr = s_lrow;
+      if (lr != INT_MAX && lr - lo >= st && lr - lo < nr && (((lr - lo - st) % PT) >> 5) == warp) {
+        __syncwarp();
+        if (lane < w) st_value<T>(valw + ((size_t)b * 2 + par) * 2 * PW, lane, tile[(lr - lo) * PLD + lane], tag);
+      }
+      if (d - lo >= st && d - lo < nr && (((d - lo - st) % PT) >> 5) == warp) {
+        __syncwarp();
+        if (lane < w) st_value<T>(diagw + par * 2 * PW, lane, tile[(d - lo) * PLD + lane], tag);
       }
     }
 
     // --- poll every CTA's key (thread q <- CTA q) and the diagonal row (warp 7);
     //     the polls spin without sleeping (a sleep costs more than it saves
-    //     here), bounded by kSpinLimit ---
+    //     here), bounded by spin_limit ---
     long long key = -2;
     int row = INT_MAX;
     if (tid < G) {
@@ -306,8 +329,9 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
       }
     }
     __syncthreads();
-    // --- scale (PDSCAL) and rank-1 update (PDGER), one thread per row; the
-    //     row's next-column entry gives its IDAMAX key for column k+1 ---
+    // --- scale (PDSCAL) and the first column of the rank-1 update (PDGER),
+    //     one thread per row; the row's next-column entry gives its IDAMAX
+    //     key for column k+1 ---
     const bool scale = s_scale != 0;
     const T rinv = s_rinv;
     const int kn = k + 1;
@@ -318,8 +342,7 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
       T l = rp[k];
       if (scale) l *= rinv;
       rp[k] = l;
-#pragma unroll 4
-      for (int j = kn; j < w; ++j) rp[j] = fma(-l, s_U[j], rp[j]);
+      if (kn < w) rp[kn] = fma(-l, s_U[kn], rp[kn]);
       if (kn < kw) ikey_combine(nkey, nrow, amax_ikey(rp[kn]), lo + r);
     }
     if (kn < kw) {
@@ -328,6 +351,10 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
     }
     __syncthreads();
   }
+  // the last column's remaining update (columns beyond kw when the panel has
+  // fewer rows than columns)
+  if (kw > 0) finish_update(kw - 1);
+  __syncthreads();
 
   for (int r = tid; r < nr; r += PT) {
     T* dst = A + (long long)(r0 + lo + r) + (long long)c0 * lda;
