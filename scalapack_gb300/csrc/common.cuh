@@ -30,6 +30,31 @@ __device__ __forceinline__ void st_release_gpu(int* p, int v) {
 }
 
 
+// Balancing keys of the sliced FP64 product (ozgemm_f64.cu), also published
+// by kernels that produce its operands: (epoch << 12) | (frexp exponent +
+// kOzEbias) of a finite nonzero value, 0 for zero or non-finite values.
+constexpr int kOzEbias = 1100;  // frexp exponents -1073 .. 1024 -> 27 .. 2124 (< 4096)
+__device__ __forceinline__ unsigned long long oz_key_word(double x, unsigned long long epoch) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+  if (b == 0ULL || b >= 0x7ff0000000000000ULL) return 0ULL;
+  const int bexp = (int)(b >> 52);
+  const int ex = bexp ? bexp - 1022 : (63 - __clzll((long long)b)) - 1073;
+  return (epoch << 12) | (unsigned long long)(ex + kOzEbias);
+}
+
+// The balancing keys a kernel publishes for a following sliced product:
+// column maxima of L (lrows x lcols from L, column-major) into ckeys, row
+// maxima of the kernel's own output into hkeys, with one epoch; a null
+// ckeys / hkeys turns that part off.
+struct OzKeyJob {
+  unsigned long long* ckeys = nullptr;
+  unsigned long long* hkeys = nullptr;
+  unsigned long long epoch = 0ULL;
+  const double* L = nullptr;
+  long long ldl = 0;
+  int lrows = 0, lcols = 0;
+};
+
 // IDAMAX ordering key. Reference BLAS IDAMAX keeps the first maximal |x| and a
 // NaN never replaces the running maximum, so NaN entries are mapped below every
 // real magnitude. (The first element is handled separately by the callers.)

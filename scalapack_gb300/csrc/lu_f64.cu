@@ -183,10 +183,17 @@ constexpr int kFullInvMax = 256;
 // ..., in registers). The CTA's 8 warps stage L 32 columns at a time in
 // shared memory (rows from the chunk's first column down), so the 32 steps of
 // a chunk read shared memory only and no block barrier sits inside them.
+// With a plan to make (plan != null), one extra block computes the panel's
+// interchange plan (laswp_plan_block) in the same launch: both only read the
+// finished panel.
 constexpr int kInvColsSmem = 32 * 257 * (int)sizeof(double);
 __global__ void __launch_bounds__(256)
 unit_lower_inv_cols_kernel(int jb, const double* __restrict__ L, long long ldl, double* X,
-                           int ldx) {
+                           int ldx, int k1, int k2, const int* __restrict__ ipiv, int* plan) {
+  if (plan != nullptr && (int)blockIdx.x == (jb + 7) / 8) {
+    laswp_plan_block(k1, k2, ipiv, plan);
+    return;
+  }
   extern __shared__ double inv_ls[];  // Ls[l * 257 + i] = L(i, 32 tq + l)
   const int lane = threadIdx.x & 31;
   const int c = (int)blockIdx.x * 8 + (threadIdx.x >> 5);
@@ -270,10 +277,28 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
     for (int k = 0; k < kw; ++k) pflops += 2.0 * (double)(m - r0 - k - 1) * (w - k - 1) + (m - r0 - k - 1);
     SL_TRY(laswp<double>(dA, ldda, r0, r0 + kw, dipiv, j, r0, r0 + w, j + jb, s));
     if (c + w < jb) {
+      // The strip solve also publishes the balancing keys of the product that
+      // follows it: the row maxima of its own output (U) and, in extra blocks
+      // of the same launch, the column maxima of the sub-panel's L.
+      const bool keyed = r0 + kw < m && g_f64_update == 1 && oz_fits(sc, m - r0 - kw, jb - c - w, kw);
+      OzKeyJob kj;
+      if (keyed) {
+        kj.epoch = oz_new_epoch();
+        kj.ckeys = oz_ckeys(sc);
+        kj.hkeys = oz_hkeys(sc);
+        kj.L = Ap(r0 + kw, r0);
+        kj.ldl = ldda;
+        kj.lrows = m - r0 - kw;
+        kj.lcols = kw;
+      }
       SL_TRY((trsm_strip<double, false, false, true>(kw, jb - c - w, Ap(r0, r0), ldda,
-                                                      Ap(r0, r0 + w), ldda, s)));
+                                                      Ap(r0, r0 + w), ldda, s, kj)));
       pflops += (double)kw * kw * (jb - c - w);
-      if (r0 + kw < m) {
+      if (keyed) {
+        SL_TRY(oz_dgemm_keyed(sc, kj.epoch, m - r0 - kw, jb - c - w, kw, -1.0, Ap(r0 + kw, r0),
+                              ldda, Ap(r0, r0 + w), ldda, Ap(r0 + kw, r0 + w), ldda, ws.status, s));
+        pflops += 2.0 * (double)(m - r0 - kw) * (jb - c - w) * kw;
+      } else if (r0 + kw < m) {
         SL_TRY(lu_update(sc, m - r0 - kw, jb - c - w, kw, -1.0, Ap(r0 + kw, r0), ldda,
                          Ap(r0, r0 + w), ldda, Ap(r0 + kw, r0 + w), ldda, ws, s));
         pflops += 2.0 * (double)(m - r0 - kw) * (jb - c - w) * kw;
@@ -283,18 +308,24 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
   // the panel's interchanges in composite form, for the row interchanges of
   // the other columns (computed here, on the panel's stream)
   const int npiv = (m - j) < jb ? (m - j) : jb;
-  if (ws.swap_plan && npiv <= LSW_MAXP) SL_TRY(laswp_plan(j, j + npiv, dipiv, ws.swap_plan, s));
+  const bool want_plan = ws.swap_plan && npiv <= LSW_MAXP;
   // inverses of L11's diagonal blocks for the U12 solve of this step
   if (g_f64_update == 1 && ws.dinv64 && npiv == jb && jb <= kFullInvMax) {
-    // inv(L11) - I whole (jb x jb, leading dimension jb)
+    // inv(L11) - I whole (jb x jb, leading dimension jb), and the interchange
+    // plan in the same launch
     static const cudaError_t attr = cudaFuncSetAttribute(
         unit_lower_inv_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvColsSmem);
     SL_TRY(attr);
-    unit_lower_inv_cols_kernel<<<(jb + 7) / 8, 256, kInvColsSmem, s>>>(jb, Ap(j, j), ldda,
-                                                                      ws.dinv64, jb);
+    if (want_plan && npiv <= 0) SL_TRY(cudaMemsetAsync(ws.swap_plan, 0, sizeof(int), s));
+    const bool fused = want_plan && npiv > 0;
+    unit_lower_inv_cols_kernel<<<(jb + 7) / 8 + (fused ? 1 : 0), 256, kInvColsSmem, s>>>(
+        jb, Ap(j, j), ldda, ws.dinv64, jb, j, j + npiv, dipiv, fused ? ws.swap_plan : nullptr);
     count_launches(1);
     SL_TRY(cudaGetLastError());
-  } else if (g_f64_update == 1 && ws.dinv64 && npiv == jb && jb <= 1024) {
+  } else if (want_plan) {
+    SL_TRY(laswp_plan(j, j + npiv, dipiv, ws.swap_plan, s));
+  }
+  if (g_f64_update == 1 && ws.dinv64 && npiv == jb && jb > kFullInvMax && jb <= 1024) {
     constexpr int kInvSmem = 2 * 64 * 65 * (int)sizeof(double);
     static const cudaError_t attr = cudaFuncSetAttribute(
         unit_lower_inv64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvSmem);

@@ -474,7 +474,8 @@ laswp_kernel(T* A, long long lda, int k1, int k2, const int* __restrict__ ipiv, 
 // the cost is a few shared-memory operations per interchange. Computed once
 // per panel, on the panel's stream; laswp_apply_kernel then only moves data.
 constexpr int LSW_HASH = 1024;
-static __global__ void laswp_plan_kernel(int k1, int k2, const int* __restrict__ ipiv, int* plan) {
+static __device__ __noinline__ void laswp_plan_block(int k1, int k2, const int* __restrict__ ipiv,
+                                                    int* plan) {
   __shared__ int s_row[2 * LSW_MAXP], s_src[2 * LSW_MAXP], s_tab[LSW_HASH], s_piv[LSW_MAXP];
   const int npiv = k2 - k1;
   for (int i = threadIdx.x; i < LSW_HASH; i += blockDim.x) s_tab[i] = -1;
@@ -517,6 +518,10 @@ static __global__ void laswp_plan_kernel(int k1, int k2, const int* __restrict__
       }
     plan[0] = np;
   }
+}
+
+static __global__ void laswp_plan_kernel(int k1, int k2, const int* __restrict__ ipiv, int* plan) {
+  laswp_plan_block(k1, k2, ipiv, plan);
 }
 
 // Applies a plan of laswp_plan_kernel to the columns [cb1,ce1) and
@@ -563,8 +568,21 @@ constexpr int TRSM_EB = 32;
 template <typename T, bool UPPER, bool TRANS, bool UNIT, int NC>
 __global__ void __launch_bounds__(256)
 trsm_strip_kernel(int w, int ncols, int eb, const T* __restrict__ Tm, long long ldt, T* B,
-                  long long ldb) {
+                  long long ldb, OzKeyJob kj) {
   constexpr bool FORWARD = (UPPER == TRANS);
+  const int nsolve = (ncols + NC - 1) / NC;
+  if ((int)blockIdx.x >= nsolve) {
+    // extra blocks: column maxima of kj.L, 32 rows each (warp w: columns w,
+    // w+8, ...; one coalesced load per column)
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const int i = ((int)blockIdx.x - nsolve) * 32 + lane;
+    for (int c = wp; c < kj.lcols; c += 8) {
+      const unsigned long long v = (i < kj.lrows) ? oz_key_word(kj.L[i + (long long)c * kj.ldl], kj.epoch) : 0ULL;
+      const unsigned hi = __reduce_max_sync(0xffffffffu, (unsigned)(v >> 12 == kj.epoch ? (v & 4095ULL) : 0ULL));
+      if (lane == 0 && hi) atomicMax(kj.ckeys + c, (kj.epoch << 12) | hi);
+    }
+    return;
+  }
   constexpr int RG = 256 / NC;  // row groups
   extern __shared__ __align__(16) unsigned char strip_smem[];
   T* Bs = reinterpret_cast<T*>(strip_smem);  // [w][NC+1]
@@ -609,6 +627,19 @@ trsm_strip_kernel(int w, int ncols, int eb, const T* __restrict__ Tm, long long 
   for (int i = tid; i < w * NC; i += 256) {
     int r = i % w, cc = i / w;
     if (cc < nc) B[r + (col0 + cc) * ldb] = Bs[r * LD + cc];
+  }
+  // row maxima of this strip of the solution: the balancing keys of the
+  // product that takes it as its right operand
+  if constexpr (sizeof(T) == 8) {
+    if (kj.hkeys != nullptr)
+      for (int r = tid; r < w; r += 256) {
+        unsigned long long km = 0ULL;
+        for (int cc = 0; cc < nc; ++cc) {
+          const unsigned long long v = oz_key_word(Bs[r * LD + cc], kj.epoch);
+          km = v > km ? v : km;
+        }
+        if (km) atomicMax(kj.hkeys + r, km);
+      }
   }
 }
 
@@ -1067,7 +1098,7 @@ inline cudaError_t laswp_planned(T* A, long long lda, int k1, int k2, const int*
 
 template <typename T, bool UPPER, bool TRANS, bool UNIT, int NC = 8>
 inline cudaError_t trsm_strip(int w, int ncols, const T* Tm, long long ldt, T* B, long long ldb,
-                              cudaStream_t s) {
+                              cudaStream_t s, const OzKeyJob& kj = OzKeyJob()) {
   if (w <= 0 || ncols <= 0) return cudaSuccess;
   // staged triangle columns per block: up to 32, within 200 KB of shared memory
   constexpr size_t kBudget = 200 * 1024;
@@ -1078,8 +1109,8 @@ inline cudaError_t trsm_strip(int w, int ncols, const T* Tm, long long ldt, T* B
   const size_t smem = bbytes + (size_t)eb * ecol;
   auto kern = trsm_strip_kernel<T, UPPER, TRANS, UNIT, NC>;
   SL_TRY(smem_attr_once((const void*)kern, (int)kBudget));
-  dim3 grid((ncols + NC - 1) / NC);
-  kern<<<grid, 256, smem, s>>>(w, ncols, eb, Tm, ldt, B, ldb);
+  dim3 grid((ncols + NC - 1) / NC + (kj.ckeys ? (kj.lrows + 31) / 32 : 0));
+  kern<<<grid, 256, smem, s>>>(w, ncols, eb, Tm, ldt, B, ldb, kj);
   count_launches(1);
   return cudaGetLastError();
 }

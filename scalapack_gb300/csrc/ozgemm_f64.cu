@@ -117,7 +117,7 @@ constexpr int GROUP_M = 8;       // tile raster: 8 row tiles sweep the columns t
 // left (epochs only grow) and nothing has to be cleared between passes.
 constexpr int OZ_KINFO_BYTES = 8192;
 constexpr int OZ_KI_H = 0, OZ_KI_C = OZ_KMAX, OZ_KI_FLAG = 2 * OZ_KMAX;
-constexpr int OZ_EBIAS = 1100;   // frexp exponents -1073 .. 1024 -> 27 .. 2124 (< 4096)
+constexpr int OZ_EBIAS = kOzEbias;
 constexpr int OZ_BUDGET = 8;     // bits above the FP64 GEMM's row (column) bound
 constexpr int OZ_NOEXP = INT_MIN / 4;
 
@@ -810,21 +810,32 @@ long long oz_fp64_routes() {
 // Epochs only grow (process-wide, 52 bits: no wrap in practice).
 static std::atomic<unsigned long long> g_oz_epochs{0};
 
+unsigned long long oz_new_epoch() {
+  return (g_oz_epochs.fetch_add(1) + 1) & ((1ULL << 52) - 1);
+}
+unsigned long long* oz_ckeys(const OzScratch& sc) {
+  return sc.ptr ? reinterpret_cast<unsigned long long*>(sc.ptr) + OZ_KI_C : nullptr;
+}
+unsigned long long* oz_hkeys(const OzScratch& sc) {
+  return sc.ptr ? reinterpret_cast<unsigned long long*>(sc.ptr) + OZ_KI_H : nullptr;
+}
+
 // C (m x n) += alpha * A (m x k) * B (k x n), all FP64 column-major, through
 // the sliced BF16 product; K is taken in passes of at most 256, each with its
 // own balancing, budget test and (when the test trips) FP64 route.
-static cudaError_t oz_dgemm_impl(int side_b, const OzScratch& sc, int m, int n, int k,
-                                 double alpha, const double* A, long long lda, const double* B,
-                                 long long ldb, double* C, long long ldc, int* status,
-                                 cudaStream_t s) {
+static cudaError_t oz_dgemm_impl(int side_b, unsigned long long keyed_epoch, const OzScratch& sc,
+                                 int m, int n, int k, double alpha, const double* A, long long lda,
+                                 const double* B, long long ldb, double* C, long long ldc,
+                                 int* status, cudaStream_t s) {
   if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
   if (!oz_fits(sc, m, n, k)) return cudaErrorMemoryAllocation;
+  if (keyed_epoch && k > OZ_KMAX) return cudaErrorInvalidValue;
   SL_TRY(oz_smem_once());
   const int m_pad = round_up(m, OBM), n_pad = round_up(n, OBN);
   for (int k0 = 0; k0 < k; k0 += OZ_KMAX) {
     const int kb = (k - k0) < OZ_KMAX ? (k - k0) : OZ_KMAX;
     const int kpad = round_up(kb, OBK);
-    const unsigned long long epoch = (g_oz_epochs.fetch_add(1) + 1) & ((1ULL << 52) - 1);
+    const unsigned long long epoch = keyed_epoch ? keyed_epoch : oz_new_epoch();
     unsigned char* p = reinterpret_cast<unsigned char*>(sc.ptr);
     unsigned long long* kinfo = reinterpret_cast<unsigned long long*>(p);
     __nv_bfloat16* sa = reinterpret_cast<__nv_bfloat16*>(p + OZ_KINFO_BYTES);
@@ -834,7 +845,10 @@ static cudaError_t oz_dgemm_impl(int side_b, const OzScratch& sc, int m, int n, 
     const double* Ak = A + (long long)k0 * lda;
     const double* Bk = B + k0;
     const int nab = (m + 31) / 32, nbb = (n + 63) / 64;
-    oz_kscale_kernel<<<nab + nbb, 256, 0, s>>>(Ak, lda, m, Bk, ldb, n, kb, nab, kinfo, epoch);
+    if (!keyed_epoch) {
+      oz_kscale_kernel<<<nab + nbb, 256, 0, s>>>(Ak, lda, m, Bk, ldb, n, kb, nab, kinfo, epoch);
+      count_launches(1);
+    }
     oz_split_kernel<<<m_pad / 32 + n_pad / 8, 256, 0, s>>>(Ak, lda, m, Bk, ldb, n, kb, kpad, m_pad,
                                                           n_pad, sa, sb, rs, cs, kinfo, epoch,
                                                           side_b);
@@ -851,7 +865,7 @@ static cudaError_t oz_dgemm_impl(int side_b, const OzScratch& sc, int m, int n, 
     ozgemm_kernel<<<grid, OZ_THREADS, oz_smem_bytes(), s>>>(ta, tb, m, n, kpad, m_pad, n_pad, rs,
                                                             cs, alpha, C, ldc, tpc, status, Ak,
                                                             lda, Bk, ldb, kb, kinfo, epoch);
-    count_launches(3);
+    count_launches(2);
     SL_TRY(cudaGetLastError());
   }
   return cudaSuccess;
@@ -860,13 +874,19 @@ static cudaError_t oz_dgemm_impl(int side_b, const OzScratch& sc, int m, int n, 
 cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, const double* A,
                      long long lda, const double* B, long long ldb, double* C, long long ldc,
                      int* status, cudaStream_t s) {
-  return oz_dgemm_impl(0, sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, status, s);
+  return oz_dgemm_impl(0, 0ULL, sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, status, s);
+}
+
+cudaError_t oz_dgemm_keyed(const OzScratch& sc, unsigned long long epoch, int m, int n, int k,
+                           double alpha, const double* A, long long lda, const double* B,
+                           long long ldb, double* C, long long ldc, int* status, cudaStream_t s) {
+  return oz_dgemm_impl(0, epoch, sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, status, s);
 }
 
 cudaError_t oz_dgemm_bside(const OzScratch& sc, int m, int n, int k, double alpha,
                            const double* A, long long lda, const double* B, long long ldb,
                            double* C, long long ldc, int* status, cudaStream_t s) {
-  return oz_dgemm_impl(1, sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, status, s);
+  return oz_dgemm_impl(1, 0ULL, sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, status, s);
 }
 
 }  // namespace sl

@@ -73,6 +73,15 @@ cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, con
 cudaError_t oz_dgemm_bside(const OzScratch& sc, int m, int n, int k, double alpha,
                            const double* A, long long lda, const double* B, long long ldb,
                            double* C, long long ldc, int* status, cudaStream_t s);
+// The same (side A) with the balancing keys of its single pass (k <= 256)
+// already published with `epoch` (from oz_new_epoch) into oz_ckeys(sc) and
+// oz_hkeys(sc) by the kernels that produced A and B: one launch fewer.
+cudaError_t oz_dgemm_keyed(const OzScratch& sc, unsigned long long epoch, int m, int n, int k,
+                           double alpha, const double* A, long long lda, const double* B,
+                           long long ldb, double* C, long long ldc, int* status, cudaStream_t s);
+unsigned long long oz_new_epoch();
+unsigned long long* oz_ckeys(const OzScratch& sc);
+unsigned long long* oz_hkeys(const OzScratch& sc);
 // Sliced-product passes that took the FP64 route on the current device.
 long long oz_fp64_routes();
 // Trailing-update arithmetic of the FP64 factorization: 0 = FP64 DMMA,
