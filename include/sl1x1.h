@@ -191,18 +191,31 @@ int sl1x1_lowp_update_dev(int fmt, int m, int n, int k, const float* dL, long lo
  * accumulation; X is
  * refined in FP64 (classical refinement, then GMRES-IR when a step fails to
  * halve the scaled residual) until ||b-Ax||/(||A|| ||x|| N eps) <= tol
- * (tol <= 0: 1.0). If refinement stalls, the FP64 factorization is used.
+ * (tol <= 0: 1.0). If refinement stalls (a classical step that does not
+ * halve the scaled residual, then a GMRES-IR step that does not cut it by
+ * 10 %), or when GMRES's convergence rate predicts more remaining time than
+ * the plain FP64 solve would take (estimated as 3.5 x the measured
+ * low-precision factorization time), the FP64 factorization is used.
  * dipiv receives the pivots of the factorization that produced X (0-based
  * rows). keep_a = 1 keeps A intact in every case (an FP64 copy is made for the
  * fallback); keep_a = 0 lets the fallback factor A in place (DSGESV).
  * *iter (DSGESV convention): >= 0 refinement steps taken; -1 the low-precision
  * factorization failed; -3 refinement did not converge (fallback used).
  * stats[8] = {classical steps, GMRES-IR outer steps, GMRES inner iterations,
- * fell back (0/1), final scaled residual, ||A||_inf, factor ms, refine ms}.
+ * fell back (0; 1 after a stall; 2 on the predicted cost), final scaled
+ * residual, ||A||_inf, factor ms, refine ms}.
  * Returns INFO (> 0: A is exactly singular in FP64). */
 int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, const double* dB,
                        long long lddb, double* dX, long long lddx, int fmt, int nb, double tol,
                        int keep_a, int* iter, double* stats, void* stream);
+
+/* Cost rule of sl1x1_dgesv_ir_dev: the plain FP64 solve is estimated at
+ * `ratio` times the measured low-precision factorization time (default 3.5,
+ * the ratio measured at N=32768 on GB300); refinement falls back to it once
+ * GMRES's convergence rate predicts a longer remaining time. ratio <= 0 turns
+ * the rule off (refinement then stops only on a stall). No counterpart in the
+ * reference. */
+void sl1x1_set_ir_cost_ratio(double ratio);
 
 /* ---- Batched solver (no single routine of the reference; each system is a
  * PDGESV on a 1x1 grid). A plan describes `batch` independent systems

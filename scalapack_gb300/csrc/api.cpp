@@ -127,6 +127,7 @@ void chk1mat(int ma, int mapos0, int na, int napos0, int ia, int ja, const int* 
 // ------------------------------------------------------------- device state
 DevState g_dev;
 int g_default_nb = 256;
+double g_ir_cost_ratio = 3.5;  // mixed solver: FP64 cost / low-precision factor time
 bool g_lookahead = true;
 int g_fail_alloc_in = -1;
 int g_copy_chunks = 8;  // column chunks of A's host-to-device copy (<= 1: one copy)
@@ -712,6 +713,7 @@ int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, 
   opt.nb = nb > 0 ? nb : 256;
   opt.nb_fp64 = g_default_nb;
   if (tol > 0) opt.tol = tol;
+  opt.fp64_cost_ratio = g_ir_cost_ratio;
   ensure_oz(n, n, opt.nb_fp64);  // the FP64 fallback factorization
   const long long ldf = round_ld(n);
   const int kpad = sl::lowp_kpad(opt.nb) * sl::lowp_kmult(fmt);
@@ -773,7 +775,7 @@ int sl1x1_dgesv_ir_dev(int n, int nrhs, double* dA, long long ldda, int* dipiv, 
   if (e != cudaSuccess) return cuda_info(e);
   if (stats) {
     stats[0] = st.classical; stats[1] = st.gmres_outer; stats[2] = st.gmres_inner;
-    stats[3] = st.fell_back; stats[4] = st.sresid; stats[5] = st.anorm;
+    stats[3] = st.fell_back ? (st.gave_up ? 2 : 1) : 0; stats[4] = st.sresid; stats[5] = st.anorm;
     stats[6] = st.factor_ms; stats[7] = st.refine_ms;
   }
   if (st.dev_status) return -20000 - st.dev_status;
@@ -1118,6 +1120,11 @@ int sl1x1_ozgemm_dev(int m, int n, int k, double alpha, const double* dA, long l
 void sl1x1_debug_set_spin_limit(long long polls) {
   std::lock_guard<std::mutex> lk(g_mu);
   sl::set_spin_limit(polls);
+}
+
+void sl1x1_set_ir_cost_ratio(double ratio) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_ir_cost_ratio = ratio > 0.0 ? ratio : 0.0;
 }
 
 long long sl1x1_ozgemm_fp64_routes(void) {

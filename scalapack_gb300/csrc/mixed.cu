@@ -22,6 +22,8 @@
 // SRC/pdgerfs.f:552, motivates the halving test).
 #include <cuda_runtime.h>
 
+#include <chrono>
+
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -464,10 +466,18 @@ static cudaError_t scaled_residuals(int n, int ncols, const double* R, const dou
 }
 
 // GMRES on (LU)^-1 A d = (LU)^-1 r for one column; d overwritten (starts 0).
-// Returns the number of inner iterations in *its.
+// Returns the number of inner iterations in *its. From the fourth iteration
+// on, the residual estimate's geometric rate (over the last four iterations
+// from the eighth on, so that stagnation shows at once) predicts the
+// iterations still needed to reach rtol; when those, at the iterations'
+// measured host time, would take longer than budget_ms, the cycle stops and
+// *gave_up is set (the caller then solves in FP64: refining on would cost
+// more). budget_ms <= 0 turns the prediction off.
 static cudaError_t gmres_column(int n, const double* A, long long lda, const double* r, double* d,
                                 const float* F, long long ldf, const MixedWork& mw, int mmax,
-                                double rtol, int* its, cudaStream_t s) {
+                                double rtol, int* its, cudaStream_t s, double budget_ms,
+                                bool* gave_up) {
+  const auto t_start = std::chrono::steady_clock::now();
   double* V = mw.V;  // n x (mmax+1)
   const long long ldv = n;
   double* w = mw.w;
@@ -536,6 +546,15 @@ static cudaError_t gmres_column(int n, const double* A, long long lda, const dou
     for (int i = 0; i <= k; ++i) H[(size_t)i + (size_t)k * (mmax + 1)] = hcol[i];
     *its = k + 1;
     if (std::fabs(g[k + 1]) <= rtol * beta || !(hk1 > 0.0)) { ++k; break; }
+    if (k >= 3 && budget_ms > 0.0) {
+      const double el = std::chrono::duration<double, std::milli>(
+                            std::chrono::steady_clock::now() - t_start).count();
+      const double gk = std::fabs(g[k + 1]);
+      const double rate = k >= 7 ? std::pow(gk / std::fabs(g[k - 3]), 0.25)
+                                 : std::pow(gk / beta, 1.0 / (double)(k + 1));
+      const double need = (rate < 1.0 && gk > 0.0) ? std::log(rtol * beta / gk) / std::log(rate) : 1e30;
+      if (need * el / (double)(k + 1) > budget_ms - el) { *gave_up = true; ++k; break; }
+    }
   }
   // y = H(0:k,0:k)^-1 g ; d = V y
   std::vector<double> y(k, 0.0);
@@ -579,6 +598,19 @@ cudaError_t dgesv_ir_device(int n, int nrhs, double* dA, long long lda, const do
   SL_TRY(cudaMemcpyAsync(hstat, ws.status, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
   SL_TRY(cudaStreamSynchronize(s));
   cudaEventRecord(e1, s);
+  // refinement budget: the estimated cost of the plain FP64 solve
+  const auto t_ref0 = std::chrono::steady_clock::now();
+  float fms = 0.f;
+  SL_TRY(cudaEventSynchronize(e1));
+  cudaEventElapsedTime(&fms, e0, e1);
+  const double budget_ms = opt.fp64_cost_ratio * (double)fms;
+  auto budget_left = [&]() {
+    if (!(budget_ms > 0.0)) return 0.0;  // rule off
+    const double left = budget_ms - std::chrono::duration<double, std::milli>(
+                                        std::chrono::steady_clock::now() - t_ref0).count();
+    return left > 1e-3 ? left : 1e-3;
+  };
+  bool gave_up = false;
   st->anorm = anorm;
   bool ok_factor = (hstat[0] == 0) && !(hstat[1] >= 0 && hstat[1] < n);
   bool converged = false;
@@ -610,7 +642,7 @@ cudaError_t dgesv_ir_device(int n, int nrhs, double* dA, long long lda, const do
     }
     if (use_gmres && !converged) {
       prev.clear();
-      for (int outer = 0; outer < opt.max_gmres_outer; ++outer) {
+      for (int outer = 0; outer < opt.max_gmres_outer && !gave_up; ++outer) {
         double worst = *std::max_element(sres.begin(), sres.end());
         if (std::isfinite(worst) && worst <= opt.tol) { converged = true; break; }
         if (!prev.empty()) {
@@ -622,7 +654,7 @@ cudaError_t dgesv_ir_device(int n, int nrhs, double* dA, long long lda, const do
           if (sres[c] <= opt.tol) continue;
           int its = 0;
           SL_TRY(gmres_column(n, dA, lda, mw.R + (long long)c * n, mw.D, mw.F, mw.ldf, mw,
-                              opt.gmres_m, opt.gmres_rtol, &its, s));
+                              opt.gmres_m, opt.gmres_rtol, &its, s, budget_left(), &gave_up));
           st->gmres_inner += its;
           axpy1_kernel<<<blocks_for(n), 256, 0, s>>>(n, mw.D, dX + (long long)c * ldx);  // x_c += d
           count_launches(1);
@@ -637,6 +669,7 @@ cudaError_t dgesv_ir_device(int n, int nrhs, double* dA, long long lda, const do
       }
     }
   }
+  st->gave_up = (gave_up && !converged) ? 1 : 0;
   phase_end(kPhRefine, s, 0.0, 0.0);
   if (mw.status) {
     int cst = 0;

@@ -224,9 +224,14 @@ struct IrOptions {
   int gmres_m = 100;        // GMRES iterations per outer step
   double gmres_rtol = 1e-10;
   double tol = 1.0;         // target scaled residual
+  // Estimated time of the plain FP64 solve as a multiple of the measured
+  // low-precision factorization time: refinement gives up (and the FP64
+  // solve runs) once its predicted remaining time exceeds that estimate.
+  double fp64_cost_ratio = 3.5;
 };
 struct IrStats {
   int classical = 0, gmres_outer = 0, gmres_inner = 0, fell_back = 0, converged = 0;
+  int gave_up = 0;  // refinement stopped on its predicted cost, not on a stall
   int info = 0, dev_status = 0;
   double sresid = 0.0, anorm = 0.0, factor_ms = 0.0, refine_ms = 0.0;
 };

@@ -108,9 +108,18 @@ def _solve_ir(sl, torch, A0, B0, fmt, tol=1.0, nb=256):
     return info, it, st, np.asfortranarray(dX.cpu().numpy().T), A_after
 
 
+@pytest.fixture
+def no_cost_rule(sl):
+    """Refinement without the cost rule (it stops only on a stall), for tests
+    of what the refinement itself reaches."""
+    sl.lib().sl1x1_set_ir_cost_ratio(0.0)
+    yield
+    sl.lib().sl1x1_set_ir_cost_ratio(3.5)
+
+
 @pytest.mark.parametrize("fmt", ["bf16", "fp16", "bf16x3"])
 @pytest.mark.parametrize("n,nrhs,nb", [(64, 1, 32), (1000, 2, 256), (2500, 1, 256), (700, 3, 128)])
-def test_mixed_ir_reaches_fp64_backward_error(sl, orc, gpu_required, fmt, n, nrhs, nb):
+def test_mixed_ir_reaches_fp64_backward_error(sl, orc, gpu_required, no_cost_rule, fmt, n, nrhs, nb):
     import torch
     from lu_helpers import system
 
@@ -126,7 +135,7 @@ def test_mixed_ir_reaches_fp64_backward_error(sl, orc, gpu_required, fmt, n, nrh
 
 
 @pytest.mark.parametrize("kappa", [1e2, 1e4, 1e6, 1e8])
-def test_mixed_ir_conditioning_sweep(sl, orc, gpu_required, kappa):
+def test_mixed_ir_conditioning_sweep(sl, orc, gpu_required, no_cost_rule, kappa):
     # A = U diag(s) V^T with seeded Householder reflectors, s geometric 1 -> 1/kappa
     import torch
 
@@ -141,7 +150,7 @@ def test_mixed_ir_conditioning_sweep(sl, orc, gpu_required, kappa):
             assert st["fell_back"] == 0, (fmt, st)
 
 
-def test_gmres_ir_converges_at_kappa_1e8_without_fallback(sl, orc, gpu_required):
+def test_gmres_ir_converges_at_kappa_1e8_without_fallback(sl, orc, gpu_required, no_cost_rule):
     # kappa = 1e8 is beyond classical refinement with BF16x3 (near-FP32) factors;
     # GMRES-IR applies the preconditioner (FP32 factors and block inverses) with
     # FP64 vector arithmetic, a fixed operator, and reaches the FP64 backward error
@@ -169,3 +178,26 @@ def test_mixed_ir_singular_falls_back_and_reports_info(sl, orc, gpu_required):
     info, it, st, X, _ = _solve_ir(sl, torch, A0, B0, "bf16", nb=64)
     assert info == 18
     assert st["fell_back"] == 1 and it == -1
+
+
+def test_cost_rule_falls_back_early_and_stays_correct(sl, orc, gpu_required):
+    """BF16 factors of a kappa = 1e8 matrix: GMRES-IR would need many
+    iterations; with the cost rule on (a small ratio, so that any slow
+    convergence counts) refinement gives up within its first cycle, reports
+    fell_back = 2 and the FP64 solve gives the FP64 backward error."""
+    import torch
+
+    n, nrhs = 1024, 2
+    A0 = orc.gen_conditioned(n, 1e8, nrefl=64, seed=1000)
+    B0 = orc.matgen(n, nrhs, 200, kind=0)
+    L = sl.lib()
+    L.sl1x1_set_ir_cost_ratio(0.5)
+    try:
+        info, it, st, X, _ = _solve_ir(sl, torch, A0, B0, "bf16", nb=64)
+    finally:
+        L.sl1x1_set_ir_cost_ratio(3.5)
+    assert info == 0
+    assert st["fell_back"] == 2, st
+    assert it == -3
+    assert st["gmres_inner"] < 100, st
+    assert orc.sresid(A0, B0, X) < 16.0
