@@ -150,7 +150,23 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_solve_sample(A, B, nb, budget_s=25.0):
+def cpu_time_estimate(A, B, nb):
+    """Seconds the oracle's PDGESV restatement (all host cores) takes on the
+    full workload, extrapolated (n^3) from a 2048 block."""
+    from oracle import oracle as orc
+
+    orc.lib()
+    orc.set_threads(os.cpu_count() or 1)
+    n0 = min(2048, A.shape[0])
+    a0 = np.asfortranarray(A[:n0, :n0].copy())
+    b0 = np.asfortranarray(B[:n0, :].copy())
+    orc.solve_reference(a0, b0, nb=nb)  # first call: threads, page-in
+    t = time.perf_counter()
+    orc.solve_reference(a0, b0, nb=nb)
+    return (time.perf_counter() - t) * (A.shape[0] / n0) ** 3
+
+
+def cpu_solve_sample(A, B, nb, budget_s=30.0):
     """Time the oracle's PDGESV restatement (host BLAS, all cores) on a bounded
     sample of the workload: the full matrix when its estimated time fits the
     budget, else the leading n x n block with n scaled down to fit."""
@@ -213,9 +229,11 @@ def mixed_section(sl, torch, dev, args, stream):
     w = n
     sl.dgesv_ir_dev(w, 1, At.data_ptr(), n, piv.data_ptr(), Bt.data_ptr(), n, Xt.data_ptr(), n,
                     fmt="bf16x3", keep_a=True, stream=stream.cuda_stream)
+    peaks = measured_peaks()
     for fmt in [f for f in args.mixed_fmts.split(",") if f]:
         Xt.zero_()
         torch.cuda.synchronize(dev)
+        sl.prof_enable(True)
         e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         info, it, st = sl.dgesv_ir_dev(n, 1, At.data_ptr(), n, piv.data_ptr(), Bt.data_ptr(), n,
@@ -224,6 +242,19 @@ def mixed_section(sl, torch, dev, args, stream):
         e1.record(stream)
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1)
+        ph = sl.prof_read()
+        sl.prof_enable(False)
+        g_launch, g_ms, g_flops, _ = ph["mixed_gemm"]
+        kmul = 3.0 if fmt == "bf16x3" else 1.0  # BF16x3: three 16-bit products along K
+        ach = kmul * g_flops / (g_ms * 1e-3) / 1e12 if g_ms > 0 else None
+        pk = peaks.get("bf16_tflops_sustained", 1700.0)
+        roof = {"bound": "tensor", "kernel": "lowp_gemm_kernel (tcgen05 kind::f16 trailing update)",
+                "achieved": ach, "peak": pk, "unit": "TFLOP/s",
+                "frac": (ach / pk) if ach else None,
+                "peak_source": f"bf16_tflops_sustained ({'of measured' if peaks.get('source') == 'measured' else 'of fallback'})",
+                "achieved_def": f"{'3 x ' if kmul > 1 else ''}sum 2*m*n*k of the update calls / their phase time (operand packing + tcgen05 GEMM)",
+                "update_ms": g_ms, "launches": g_launch,
+                "panel_ms": ph["mixed_panel"][1]}
         out["runs"][fmt] = {"info": info, "iter": it, "time_to_solution_ms": ms,
                             "factor_ms": st["factor_ms"], "refine_ms": st["refine_ms"],
                             "classical_steps": int(st["classical"]),
@@ -231,7 +262,8 @@ def mixed_section(sl, torch, dev, args, stream):
                             "gmres_inner": int(st["gmres_inner"]),
                             "fell_back_to_fp64": bool(st["fell_back"]),
                             "sresid": torch_sresid(torch, A, B, Xt.T),
-                            "tflops_2n3_3": 2.0 * n ** 3 / 3.0 / (ms * 1e-3) / 1e12}
+                            "tflops_2n3_3": 2.0 * n ** 3 / 3.0 / (ms * 1e-3) / 1e12,
+                            "roofline": roof}
     # plain FP64 GPU solve of the same system
     Ac = At.clone()
     Bc = Bt.clone()
@@ -307,6 +339,29 @@ def conditioned_section(sl, torch, dev, args, stream):
     return out
 
 
+def batched_cpu_baseline(dA, dB, budget_s=10.0):
+    """Host LAPACK dgesv (OpenBLAS, all cores) on the batch's systems in order,
+    as many as fit the budget: solves per second."""
+    from oracle import oracle as orc
+
+    orc.lib()
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    done, t_total = 0, 0.0
+    for a, b in zip(dA, dB):
+        A = np.asfortranarray(a.cpu().numpy().T)
+        B = np.asfortranarray(b.cpu().numpy().T)
+        t = time.perf_counter()
+        orc.lapack_dgesv(A, B)
+        t_total += time.perf_counter() - t
+        done += 1
+        if t_total > budget_s:
+            break
+    return {"value": done / t_total, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": f"host LAPACK dgesv (OpenBLAS, {cores} threads) on the first {done} systems "
+                      f"of the batch, one at a time ({t_total:.1f} s)"}
+
+
 def batched_section(sl, torch, dev, args, stream):
     """Config: 4096 independent FP64 systems, N ~ U{16..512}, NRHS ~ U{1..8}, entries
     U[-0.5,0.5] plus a diagonal shift N/4 on half the batch; FP64 and FP32-factor +
@@ -356,7 +411,18 @@ def batched_section(sl, torch, dev, args, stream):
             "sresid_max": float(srv.max()), "sresid_median": float(np.median(srv)),
             "refine_steps_mean": float(itv[itv >= 0].mean()) if mode == 1 else 0.0,
             "fp64_pass_systems": int(np.count_nonzero(itv == -1)) if mode == 1 else 0}
+        if mode == 0 and args.dmma_peak:
+            # SIMT FP64 factor + solve: against the FP64 peak measured live
+            ach = flops / (ms * 1e-3) / 1e12
+            out["modes"][name]["roofline"] = {
+                "bound": "fp64 pipe", "kernel": "batched persistent FP64 kernel",
+                "achieved": ach, "peak": args.dmma_peak, "unit": "TFLOP/s",
+                "frac": ach / args.dmma_peak,
+                "peak_source": "register-only FP64 DMMA loop measured in this run (sl1x1_dmma_peak_tflops)",
+                "achieved_def": "sum over systems of 2n^3/3 / batch time"}
         plan.close()
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = batched_cpu_baseline(dA, dB)
     del dA, dB, dX
     torch.cuda.empty_cache()
     return out
@@ -385,14 +451,21 @@ def run_reference(args):
     orc.lib()
     cores = os.cpu_count() or 1
     orc.set_threads(cores)
-    # bounded sample per step so that W + K steps end within a few minutes
-    per_step_budget = max(5.0, 150.0 / max(1, args.steps + args.warmup))
-    probe = cpu_solve_sample(A, B, args.nb, budget_s=per_step_budget)
+    # Each timed step solves the full workload when the K steps fit about six
+    # minutes, else a bounded leading block; the W warm-up steps (threads,
+    # page-in) run on a 2048 block. The probe also times the host LAPACK.
+    est = cpu_time_estimate(A, B, args.nb)
+    n = args.n if est * args.steps <= 360.0 else \
+        max(2048, int(args.n * (360.0 / (est * args.steps)) ** (1 / 3)) // args.nb * args.nb)
+    probe = cpu_solve_sample(A, B, args.nb, budget_s=est * (n / args.n) ** 3 * 1.05 + 1.0)
     n = probe["n"]
     a0 = np.asfortranarray(A[:n, :n].copy())
     b0 = np.asfortranarray(B[:n, :].copy())
+    w0 = min(2048, n)
+    aw = np.asfortranarray(A[:w0, :w0].copy())
+    bw = np.asfortranarray(B[:w0, :].copy())
     for _ in range(args.warmup):
-        orc.solve_reference(a0, b0, nb=args.nb)
+        orc.solve_reference(aw, bw, nb=args.nb)
     t = time.perf_counter()
     for _ in range(args.steps):
         orc.solve_reference(a0, b0, nb=args.nb)
@@ -404,8 +477,9 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": f"synthetic: A, B iid U[-0.5,0.5] (numpy PCG64 seed {args.seed})",
         "config": {"workload": f"plain FP64 PDGESV (1x1 grid) N={args.n} NB={args.nb} "
-                               f"NRHS={args.nrhs}; CPU sample N={n}", "n": args.n, "nb": args.nb,
-                   "nrhs": args.nrhs, "sample_n": n},
+                               f"NRHS={args.nrhs}" + ("" if n == args.n else f"; CPU sample N={n}"),
+                   "n": args.n, "nb": args.nb, "nrhs": args.nrhs, "sample_n": n,
+                   "same_config": n == args.n, "warmup_n": w0},
         "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": cores, "kind": "port",
                          "sample": f"oracle PDGESV restatement on host BLAS (OpenBLAS, {cores} "
                                    f"threads), N={n} NB={args.nb} NRHS={args.nrhs} per step; the "
@@ -458,6 +532,7 @@ def run_gpu(args):
     for _ in range(max(3, args.warmup)):
         step()
     peak = float(L.sl1x1_dmma_peak_tflops())
+    args.dmma_peak = peak
     sl.prof_enable(True)
     launches0 = sl.launch_count()
     routes0 = int(L.sl1x1_ozgemm_fp64_routes())
