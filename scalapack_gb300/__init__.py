@@ -450,9 +450,9 @@ class BatchPlan:
                       P(*[s[6] for s in systems]), I(*[s[7] for s in systems]))
         n, r, a, lda, b, ldb, x, ldx = self._keep
         self.plan = C.c_void_p()
-        info = lib().sl1x1_batch_plan_create(C.byref(self.plan), k, n, r, a, lda, b, ldb, x, ldx,
-                                             mode, float(tol), 1 if autotune else 0,
-                                             _stream_ptr(stream))
+        info = lib().sl1x1_batch_plan_create(C.byref(self.plan), C.c_int(k), n, r, a, lda, b, ldb,
+                                             x, ldx, C.c_int(mode), C.c_double(float(tol)),
+                                             C.c_int(1 if autotune else 0), _stream_ptr(stream))
         if info != 0:
             raise RuntimeError(f"sl1x1_batch_plan_create INFO={info}")
         self.stream = stream

@@ -127,11 +127,15 @@ def test_batched_singular_and_edges(sl, orc, gpu_required, mode):
 
 def test_batched_plan_rejects_bad_sizes(sl):
     L = sl.lib()
+    saved = L.sl1x1_batch_plan_create.argtypes
     L.sl1x1_batch_plan_create.argtypes = None
-    k = 1
-    n = (C.c_int * k)(600)
-    r = (C.c_int * k)(1)
-    p = C.c_void_p()
-    P = (C.c_void_p * k)(None)
-    assert L.sl1x1_batch_plan_create(C.byref(p), k, n, r, P, n, P, n, P, n, 0, C.c_double(1.0), 0,
-                                     None) == -3
+    try:
+        k = 1
+        n = (C.c_int * k)(600)
+        r = (C.c_int * k)(1)
+        p = C.c_void_p()
+        P = (C.c_void_p * k)(None)
+        assert L.sl1x1_batch_plan_create(C.byref(p), k, n, r, P, n, P, n, P, n, 0, C.c_double(1.0),
+                                         0, None) == -3
+    finally:
+        L.sl1x1_batch_plan_create.argtypes = saved
