@@ -178,6 +178,7 @@ void release_all() {
   cudaFree(g_dev.dA2); cudaFree(g_dev.dX); cudaFree(g_dev.drw); cudaFree(g_dev.drc);
   cudaFree(g_dev.dipiv2); cudaFree(g_dev.doz); cudaFree(g_dev.doz2); cudaFree(g_dev.ddinv64);
   cudaFree(g_dev.ddinvs);
+  cudaFree(g_dev.dptile);
   sl::splitk_scratch() = sl::SplitKScratch();
   if (g_dev.stream) cudaStreamDestroy(g_dev.stream);
   if (g_dev.aux) cudaStreamDestroy(g_dev.aux);
@@ -191,6 +192,11 @@ void release_all() {
 }
 
 void ensure_oz(int m, int n, int nb) {
+  // panels taller than the SMs' shared memory holds keep their rows in a
+  // global buffer (optional: without it such an M is rejected with -30000)
+  if (m > sl::panel_max_rows() && n > 0 &&
+      grow(&g_dev.dptile, &g_dev.capPtile, sl::panel_tile_doubles(m)) != cudaSuccess)
+    cudaGetLastError();
   if (sl::f64_update_get() != 1 || m <= 0 || n <= 0) return;
   if (nb <= 0) nb = g_default_nb;
   const size_t need = sl::oz_scratch_bytes(m, n, nb);
@@ -222,6 +228,8 @@ sl::LuWork make_work() {
   w.dinv64_step0 = g_dev.ddinv64 ? g_dev.ddinv64 + sl::kDinv64Doubles : nullptr;
   w.dinv_solve = g_dev.ddinvs;
   w.dinv_solve_len = g_dev.ddinvs ? g_dev.capDinvs : 0;
+  w.ptile = g_dev.dptile;
+  w.ptile_len = g_dev.dptile ? g_dev.capPtile : 0;
   if (g_lookahead) {
     w.aux = g_dev.aux;
     w.ev_next = g_dev.ev_next;

@@ -57,6 +57,7 @@ struct DevState {
   unsigned char* doz = nullptr; size_t capOz = 0;    // sliced-product scratch, caller's stream (bytes)
   unsigned char* doz2 = nullptr; size_t capOz2 = 0;  // sliced-product scratch, panel stream (bytes)
   double* ddinv64 = nullptr;  // U12 solve: inverses of L11's 64x64 blocks, then a copy for step 0
+  double* dptile = nullptr; size_t capPtile = 0;  // rows of panels taller than shared memory holds
   double* ddinvs = nullptr; size_t capDinvs = 0;      // solve: inverses of the diagonal blocks
   int chain_epoch = 0;
   unsigned short* dA16 = nullptr; size_t capA16 = 0;

@@ -39,6 +39,10 @@ static_assert(kPanelCandDoubles == (size_t)PX_WORDS, "exchange area layout");
 // Rows per CTA are capped by 200 KB of shared memory (rpc * 33 doubles),
 // rounded down to a multiple of 8: 768 rows; one CTA per SM.
 int panel_max_rows() { return num_sms() * 768; }
+// Global rows of a tall panel: every CTA's slice (rows rounded up to 8).
+size_t panel_tile_doubles(int m) {
+  return ((size_t)m + (size_t)8 * PMAXG) * PW;
+}
 
 static long long g_spin_limit = kSpinLimit;
 long long spin_limit() { return g_spin_limit; }

@@ -159,12 +159,22 @@ __device__ __forceinline__ void warp_ikey(long long& k, int& r) {
 // that gives up records kFlagTimeout and returns, and block 0 then writes the
 // identity for the pivots it has not chosen, so the interchanges launched
 // after it stay inside the matrix.
-template <typename T>
+//
+// GTILE: for panels taller than the CTAs' shared memory holds (more than 768
+// FP64 rows per CTA on every SM), each CTA's rows live in a global buffer
+// instead (gtile, column-major per CTA: rpc rows x PW columns, so a warp's
+// row walk is one coalesced access); the algorithm is unchanged.
+template <typename T, bool GTILE = false>
 __global__ void __launch_bounds__(PT)
 panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ipiv,
-             int* info_col, double* cand, int* status, long long spin_limit) {
+             int* info_col, double* cand, int* status, long long spin_limit, T* gtile) {
   extern __shared__ __align__(16) unsigned char panel_smem[];
-  T* tile = reinterpret_cast<T*>(panel_smem);  // [rpc][PLD]
+  // element (r, c) of this CTA's rows: [rpc][PLD] in shared memory, or
+  // column-major rpc x PW in the global buffer
+  T* tile = GTILE ? gtile + (size_t)blockIdx.x * (size_t)rpc * PW : reinterpret_cast<T*>(panel_smem);
+  auto tix = [&](int r, int c) -> size_t {
+    return GTILE ? (size_t)c * (size_t)rpc + (size_t)r : (size_t)r * PLD + (size_t)c;
+  };
   __shared__ T s_U[PW];
   __shared__ T s_D[PW];
   __shared__ long long s_wk[PT / 32];
@@ -197,7 +207,7 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
     for (int c = 0; c < PW; ++c) v[c] = (c < w) ? src[(long long)c * lda] : (T)0;
 #pragma unroll
     for (int c = 0; c < PW; ++c)
-      if (c < w) tile[r * PLD + c] = v[c];
+      if (c < w) tile[tix(r, c)] = v[c];
   }
   if (tid == 0) s_fail = 0;
 
@@ -206,7 +216,7 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
   {
     long long key = -2;
     int row = INT_MAX;
-    for (int r = tid; r < nr; r += PT) ikey_combine(key, row, amax_ikey(tile[r * PLD]), lo + r);  // own rows
+    for (int r = tid; r < nr; r += PT) ikey_combine(key, row, amax_ikey(tile[tix(r, 0)]), lo + r);  // own rows
     warp_ikey(key, row);
     if (lane == 0) { s_wk[warp] = key; s_wr[warp] = row; }
   }
@@ -219,10 +229,9 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
   // updates of columns 0, 1, ... in order, as one fma each.
   auto finish_update = [&](int kp) {  // columns kp+2 .. w-1 of the rows below kp
     for (int r = max(0, kp + 1 - lo) + tid; r < nr; r += PT) {
-      T* rp = tile + r * PLD;
-      const T l = rp[kp];
+      const T l = tile[tix(r, kp)];
 #pragma unroll 4
-      for (int j = kp + 2; j < w; ++j) rp[j] = fma(-l, s_U[j], rp[j]);
+      for (int j = kp + 2; j < w; ++j) tile[tix(r, j)] = fma(-l, s_U[j], tile[tix(r, j)]);
     }
   };
 
@@ -256,11 +265,11 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
       const int lr = s_lrow;
       if (lr != INT_MAX && lr - lo >= st && lr - lo < nr && (((lr - lo - st) % PT) >> 5) == warp) {
         __syncwarp();
-        if (lane < w) st_value<T>(valw + ((size_t)b * 2 + par) * 2 * PW, lane, tile[(lr - lo) * PLD + lane], tag);
+        if (lane < w) st_value<T>(valw + ((size_t)b * 2 + par) * 2 * PW, lane, tile[tix(lr - lo, lane)], tag);
       }
       if (d - lo >= st && d - lo < nr && (((d - lo - st) % PT) >> 5) == warp) {
         __syncwarp();
-        if (lane < w) st_value<T>(diagw + par * 2 * PW, lane, tile[(d - lo) * PLD + lane], tag);
+        if (lane < w) st_value<T>(diagw + par * 2 * PW, lane, tile[tix(d - lo, lane)], tag);
       }
     }
 
@@ -316,8 +325,8 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
     if (s_fail) { give_up(k); return; }
     // --- row interchange inside the sub-panel (PDSWAP, pdgetf2.f:218) ---
     if (piv != d && tid < w) {
-      if (d >= lo && d < lo + nr) tile[(d - lo) * PLD + tid] = s_U[tid];
-      if (piv >= lo && piv < lo + nr) tile[(piv - lo) * PLD + tid] = s_D[tid];
+      if (d >= lo && d < lo + nr) tile[tix(d - lo, tid)] = s_U[tid];
+      if (piv >= lo && piv < lo + nr) tile[tix(piv - lo, tid)] = s_D[tid];
     }
     if (tid == 0) {
       const T gmax = s_U[k];
@@ -338,12 +347,11 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
     long long nkey = -2;
     int nrow = INT_MAX;
     for (int r = max(0, d + 1 - lo) + tid; r < nr; r += PT) {
-      T* rp = tile + r * PLD;
-      T l = rp[k];
+      T l = tile[tix(r, k)];
       if (scale) l *= rinv;
-      rp[k] = l;
-      if (kn < w) rp[kn] = fma(-l, s_U[kn], rp[kn]);
-      if (kn < kw) ikey_combine(nkey, nrow, amax_ikey(rp[kn]), lo + r);
+      tile[tix(r, k)] = l;
+      if (kn < w) tile[tix(r, kn)] = fma(-l, s_U[kn], tile[tix(r, kn)]);
+      if (kn < kw) ikey_combine(nkey, nrow, amax_ikey(tile[tix(r, kn)]), lo + r);
     }
     if (kn < kw) {
       warp_ikey(nkey, nrow);
@@ -360,7 +368,7 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
     T* dst = A + (long long)(r0 + lo + r) + (long long)c0 * lda;
     T v[PW];
 #pragma unroll
-    for (int c = 0; c < PW; ++c) v[c] = (c < w) ? tile[r * PLD + c] : (T)0;
+    for (int c = 0; c < PW; ++c) v[c] = (c < w) ? tile[tix(r, c)] : (T)0;
 #pragma unroll
     for (int c = 0; c < PW; ++c)
       if (c < w) dst[(long long)c * lda] = v[c];
@@ -1031,25 +1039,41 @@ inline cudaError_t launch_panel(T* A, long long lda, int m, int r0, int c0, int 
   // exchange cheaper (fewer keys to poll, less cross-die skew); more rows per
   // CTA make the rank-1 update longer -- on GB300's FP64 pipe sooner than on
   // the FP32 one.
-  // Tall panels beyond 64 CTAs' shared memory spread over every SM instead.
+  // Tall panels beyond 64 CTAs' shared memory spread over every SM instead;
+  // beyond every SM's shared memory the rows go to the global buffer ws.ptile.
   const int rpc_max = (int)((200 * 1024) / (sizeof(T) * PLD)) & ~7;
   int rpc = (R + 63) / 64;
   const int lo_rows = panel_min_rows() > 0 ? panel_min_rows() : (sizeof(T) == 4 ? 256 : 128);
   if (rpc < lo_rows) rpc = lo_rows;
   if (rpc > rpc_max) rpc = (R + num_sms() - 1) / num_sms();
   rpc = (rpc + 7) & ~7;
-  const int G = (R + rpc - 1) / rpc;
-  const size_t smem = sizeof(T) * (size_t)rpc * PLD;
-  if (smem > 200 * 1024 || G > PMAXG) return cudaErrorInvalidValue;  // M beyond the panel limit
-  SL_TRY(smem_attr_once((const void*)panel_kernel<T>, 200 * 1024));
+  int G = (R + rpc - 1) / rpc;
+  size_t smem = sizeof(T) * (size_t)rpc * PLD;
+  const bool global_tile = smem > 200 * 1024 || G > PMAXG;
+  T* gtile = nullptr;
+  if (global_tile) {
+    if constexpr (sizeof(T) != 8) {
+      return cudaErrorInvalidValue;  // M beyond the FP32 panel limit
+    } else {
+      G = std::min(PMAXG, num_sms());
+      rpc = ((R + G - 1) / G + 7) & ~7;
+      G = (R + rpc - 1) / rpc;
+      if (!ws.ptile || ws.ptile_len < (size_t)G * rpc * PW) return cudaErrorInvalidValue;
+      gtile = ws.ptile;
+      smem = 0;
+    }
+  }
+  if (!global_tile) SL_TRY(smem_attr_once((const void*)panel_kernel<T, false>, 200 * 1024));
   // zero the diagonal rows and the G slots used (stale tags must not match)
   cudaError_t e = cudaMemsetAsync(ws.cand, 0, sizeof(unsigned long long) * ((size_t)PX_VALS + (size_t)G * 2 * 2 * PW), s);
   if (e != cudaSuccess) return e;
   long long limit = spin_limit();
   void* args[] = {&A, &lda, &m, &r0, &c0, &w, (void*)&rpc, &ipiv, (void*)&ws.info_col,
-                  (void*)&ws.cand, (void*)&ws.status, (void*)&limit};
+                  (void*)&ws.cand, (void*)&ws.status, (void*)&limit, (void*)&gtile};
   count_launches(1);
-  return cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(PT), args, smem, s);
+  if (global_tile)
+    return cudaLaunchCooperativeKernel((void*)panel_kernel<T, true>, dim3(G), dim3(PT), args, 0, s);
+  return cudaLaunchCooperativeKernel((void*)panel_kernel<T, false>, dim3(G), dim3(PT), args, smem, s);
 }
 
 template <typename T>

@@ -130,6 +130,10 @@ struct LuWork {
   const int* col_end = nullptr;
   const cudaEvent_t* ev_cols = nullptr;
   double* dinv64_step0 = nullptr;
+  // Rows of panels taller than the SMs' shared memory holds (FP64; null: such
+  // panels are rejected): ptile_len doubles.
+  double* ptile = nullptr;
+  size_t ptile_len = 0;
 };
 // Most column chunks a streamed factorization takes.
 constexpr int kMaxColChunks = 16;
@@ -144,8 +148,10 @@ size_t panel_cand_doubles();
 constexpr size_t kPanelCandDoubles = (size_t)4 * 32 + (size_t)8 * 224 + (size_t)224 * 2 * 2 * 32;
 // Ints of a panel's interchange plan (count + 2 x 512 (row, src) pairs).
 constexpr size_t kSwapPlanInts = 1 + 4 * 256 + 15;
-// Largest M the FP64 panel supports on this device (rows held in shared memory).
+// Largest M whose FP64 panel rows fit the SMs' shared memory on this device;
+// taller panels need LuWork::ptile (panel_tile_doubles(m) doubles).
 int panel_max_rows();
+size_t panel_tile_doubles(int m);
 // Smallest row slice per CTA of the cooperative panel (tunable; 0, the
 // default, means 256 rows for FP32 and 128 for FP64).
 int panel_min_rows();

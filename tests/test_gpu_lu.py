@@ -262,3 +262,20 @@ def test_pdgetri_singular_info(sl, orc, ctx):
     info, _, _ = sl.pdgetri(n, A, 1, 1, d, ipiv)
     assert info == 21
     np.testing.assert_array_equal(A, before)  # inverse not computed
+
+
+def test_tall_matrix_beyond_shared_memory_panel(sl, orc, ctx):
+    """M = 200,000 > 152 SMs x 768 rows: the panel's rows no longer fit the
+    SMs' shared memory, and each CTA keeps its rows in a library-owned global
+    buffer instead. pdgetrf_ on a 200000 x 512 matrix (0.8 GB): IPIV identical
+    to the oracle's, the tester's factor residual below 16."""
+    m, n, nb = 200000, 512, 256
+    assert m > 152 * 768
+    A0 = orc.matgen(m, n, 100, kind=1)
+    A = np.asfortranarray(A0.copy())
+    desc = np.array([1, ctx, m, n, nb, nb, 0, 0, m], np.int32)
+    ipiv = np.zeros(m + nb, np.int32)
+    assert sl.pdgetrf(m, n, A, 1, 1, desc, ipiv) == 0
+    bad, ties = compare_ipiv(orc, A0, ipiv[:n], nb)
+    assert bad == 0, ties
+    assert orc.fresid(A, ipiv[:n], A0) < RESID_THRESH
