@@ -639,6 +639,34 @@ def run_gpu(args):
                "d2h_bytes_per_step": 8 * n * n + 4 * n + 8 * n * nrhs,
                "ms_per_step": e2e_s * 1e3, "steps": len(tt),
                "path": "pdgesv_ (Fortran ABI) from pinned host memory"}
+        # the same call on ordinary (pageable) arrays, as a Fortran caller passes them
+        del hA, hB, an, bn
+        pa0 = np.asfortranarray(A)
+        pb0 = np.asfortranarray(B)
+        pa = np.empty_like(pa0, order="F")
+        pb = np.empty_like(pb0, order="F")
+        tp = []
+        for it in range(args.e2e_steps + 1):
+            np.copyto(pa, pa0)
+            np.copyto(pb, pb0)
+            if dist is not None:
+                dist.barrier()
+            t = time.perf_counter()
+            info = sl.pdgesv(n, nrhs, pa, 1, 1, desca, ipiv, pb, 1, 1, descb)
+            dt = time.perf_counter() - t
+            if info != 0:
+                raise RuntimeError(f"pdgesv_ INFO={info}")
+            if it > 0:
+                tp.append(dt)
+        pg_s = float(np.mean(tp))
+        if dist is not None:
+            t = torch.tensor([pg_s], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            pg_s = float(t.item())
+        e2e["pageable"] = {"value": ws * flops_lu(n) / pg_s / 1e12, "unit": "TFLOP/s",
+                           "ms_per_step": pg_s * 1e3, "steps": len(tp),
+                           "path": "pdgesv_ from ordinary (pageable) numpy arrays"}
+        del pa, pb, pa0, pb0
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
