@@ -299,6 +299,13 @@ void sl1x1_set_copy_chunks(int chunks);
  * Returns the hook's previous state: -1 once it has fired (or when it was
  * off), else the growths it was still waiting for. */
 int sl1x1_debug_fail_alloc(int k);
+/* SMs that the factorization's look-ahead trailing update leaves free for
+ * the next panel's kernels: at least min_sms (default 24: the panel kernel's
+ * CTAs must all be resident to make progress) and, when the update is small
+ * enough to finish within about one panel period on fewer SMs, up to max_sms
+ * (default 88). (0, 0) lets the update take every SM. Values are clamped to
+ * 0..120. Changes only the speed. */
+void sl1x1_set_update_reserve(int min_sms, int max_sms);
 /* Test hook for the bounded device waits: the number of polls a panel CTA
  * makes for another CTA's published pivot candidates before it gives up
  * (polls < 0 restores the default, 2^24; 0 makes every wait run out at its

@@ -146,6 +146,8 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_debug_set_spin_limit.restype = None
     L.sl1x1_set_ir_cost_ratio.argtypes = [C.c_double]
     L.sl1x1_set_ir_cost_ratio.restype = None
+    L.sl1x1_set_update_reserve.argtypes = [C.c_int, C.c_int]
+    L.sl1x1_set_update_reserve.restype = None
     L.sl1x1_device_ok.restype = C.c_int
     L.sl1x1_version.restype = C.c_char_p
     L.sl1x1_prof_enable.argtypes = [C.c_int]

@@ -1125,6 +1125,11 @@ int sl1x1_ozgemm_dev(int m, int n, int k, double alpha, const double* dA, long l
   return st ? -20000 - st : 0;
 }
 
+void sl1x1_set_update_reserve(int min_sms, int max_sms) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  sl::set_update_reserve(min_sms, max_sms);
+}
+
 void sl1x1_debug_set_spin_limit(long long polls) {
   std::lock_guard<std::mutex> lk(g_mu);
   sl::set_spin_limit(polls);

@@ -23,7 +23,9 @@
 // with the same swap / triangular-solve / GEMM kernels, so the final factors,
 // pivots and INFO are those of the reference's column-by-column PDGETF2 in
 // exact arithmetic.
+#include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -115,11 +117,32 @@ int f64_update_get() { return g_f64_update; }
 
 // C (m x n) -= A (m x k) * B (k x n) inside the factorization: the sliced
 // tensor-core product when selected and its scratch fits, else FP64 DMMA.
+// With look-ahead, the update of the columns right of the next panel runs
+// beside that panel's kernels (on the auxiliary stream). The panel's
+// cooperative kernel makes progress only once all its CTAs are resident, so
+// the update keeps at least g_res_min SMs free for it; beyond that it takes
+// the SMs it needs to finish within about one panel period (an SM's share of
+// the sliced product being kUpdFlopsPerSm in that time) and leaves up to
+// g_res_max to the panel chain. (0, 0): the update takes every SM.
+static int g_res_min = 24, g_res_max = 88;
+constexpr double kUpdFlopsPerSm = 3.2e8;
+void set_update_reserve(int min_sms, int max_sms) {
+  g_res_min = std::max(0, std::min(min_sms, 120));
+  g_res_max = std::max(g_res_min, std::min(max_sms, 120));
+}
+static int update_ctas(double flops) {
+  if (g_res_max <= 0) return 0;
+  const int S = num_sms();
+  const int want = (int)std::ceil(flops / kUpdFlopsPerSm);
+  return std::max(1, std::max(S - g_res_max, std::min(S - g_res_min, want)));
+}
+
 static cudaError_t lu_update(const OzScratch& sc, int m, int n, int k, double alpha,
                              const double* A, long long lda, const double* B, long long ldb,
-                             double* C, long long ldc, const LuWork& ws, cudaStream_t s) {
+                             double* C, long long ldc, const LuWork& ws, cudaStream_t s,
+                             int max_ctas = 0) {
   if (g_f64_update == 1 && oz_fits(sc, m, n, k))
-    return oz_dgemm(sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, ws.status, s);
+    return oz_dgemm(sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, ws.status, s, max_ctas);
   return dgemm(false, m, n, k, alpha, A, lda, B, ldb, 1.0, C, ldc, s);
 }
 
@@ -478,7 +501,8 @@ cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, 
           if (rest > 0) {
             phase_begin(kPhGemm, s);
             SL_TRY(lu_update(ws.oz, m - jn, rest, jb, -1.0, Ap(jn, j), ldda, Ap(j, jn + jb2), ldda,
-                             Ap(jn, jn + jb2), ldda, ws, s));
+                             Ap(jn, jn + jb2), ldda, ws, s,
+                             update_ctas(2.0 * mr * rest * jb)));
             phase_end(kPhGemm, s, 2.0 * mr * rest * jb, 8.0 * (mr * jb + (double)jb * rest + 2.0 * mr * rest));
           }
         } else {

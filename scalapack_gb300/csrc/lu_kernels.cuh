@@ -41,7 +41,7 @@ inline cudaError_t smem_attr_once(const void* kern, int bytes) {
 }
 }  // namespace
 
-constexpr int PW = 32;       // sub-panel width held in shared memory
+constexpr int PW = 32;       // sub-panel width held in shared memory (<= 64)
 constexpr int PMAXG = 224;   // max CTAs of the panel kernel (warp 7 reads the diagonal row)
 // Exchange area of the panel kernel, in 8-byte tagged words: the diagonal
 // rows [2 parities][2*PW], the candidate keys [2 parities][PMAXG][4] (|x| key
@@ -265,11 +265,12 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
       const int lr = s_lrow;
       if (lr != INT_MAX && lr - lo >= st && lr - lo < nr && (((lr - lo - st) % PT) >> 5) == warp) {
         __syncwarp();
-        if (lane < w) st_value<T>(valw + ((size_t)b * 2 + par) * 2 * PW, lane, tile[tix(lr - lo, lane)], tag);
+        for (int c = lane; c < w; c += 32)
+          st_value<T>(valw + ((size_t)b * 2 + par) * 2 * PW, c, tile[tix(lr - lo, c)], tag);
       }
       if (d - lo >= st && d - lo < nr && (((d - lo - st) % PT) >> 5) == warp) {
         __syncwarp();
-        if (lane < w) st_value<T>(diagw + par * 2 * PW, lane, tile[tix(d - lo, lane)], tag);
+        for (int c = lane; c < w; c += 32) st_value<T>(diagw + par * 2 * PW, c, tile[tix(d - lo, c)], tag);
       }
     }
 
@@ -292,10 +293,12 @@ panel_kernel(T* A, long long lda, int m, int r0, int c0, int w, int rpc, int* ip
           break;
         }
       }
-    } else if (warp == PT / 32 - 1 && lane < w) {
-      T v;
-      if (ld_value<T>(diagw + par * 2 * PW, lane, tag, v, spin_limit)) s_D[lane] = v;
-      else { atomicExch(status, (int)kFlagTimeout); s_fail = 1; }
+    } else if (warp == PT / 32 - 1) {
+      for (int c = lane; c < w; c += 32) {
+        T v;
+        if (ld_value<T>(diagw + par * 2 * PW, c, tag, v, spin_limit)) s_D[c] = v;
+        else { atomicExch(status, (int)kFlagTimeout); s_fail = 1; }
+      }
     }
     warp_ikey(key, row);
     if (lane == 0) { s_wk[warp] = key; s_wr[warp] = row; }

@@ -66,8 +66,8 @@ extern "C" int sl1x1_dgetrf_noalloc(int m, int n, double* dA, long long ldda, in
     if (m > max_rows) {
       std::fprintf(stderr,
                    "sl1x1_dgetrf_noalloc: M=%d exceeds the supported maximum of %d rows "
-                   "(%d SMs x 768 panel rows in shared memory); nothing was launched\n",
-                   m, max_rows, max_rows / 768);
+                   "(the panel's rows held in the %d SMs' shared memory); nothing was launched\n",
+                   m, max_rows, sl::num_sms());
       return -30000;
     }
   }

@@ -826,7 +826,7 @@ unsigned long long* oz_hkeys(const OzScratch& sc) {
 static cudaError_t oz_dgemm_impl(int side_b, unsigned long long keyed_epoch, const OzScratch& sc,
                                  int m, int n, int k, double alpha, const double* A, long long lda,
                                  const double* B, long long ldb, double* C, long long ldc,
-                                 int* status, cudaStream_t s) {
+                                 int* status, cudaStream_t s, int max_ctas = 0) {
   if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
   if (!oz_fits(sc, m, n, k)) return cudaErrorMemoryAllocation;
   if (keyed_epoch && k > OZ_KMAX) return cudaErrorInvalidValue;
@@ -860,7 +860,8 @@ static cudaError_t oz_dgemm_impl(int side_b, unsigned long long keyed_epoch, con
     // a few tiles per CTA: enough to overlap one tile's epilogue with the
     // next one's products, few enough that every SM gets work and SMs free
     // up often
-    const int tpc = std::max(1, std::min(g_oz_tiles_per_cta, tiles / num_sms()));
+    int tpc = std::max(1, std::min(g_oz_tiles_per_cta, tiles / num_sms()));
+    if (max_ctas > 0 && (tiles + tpc - 1) / tpc > max_ctas) tpc = (tiles + max_ctas - 1) / max_ctas;
     const int grid = (tiles + tpc - 1) / tpc;
     ozgemm_kernel<<<grid, OZ_THREADS, oz_smem_bytes(), s>>>(ta, tb, m, n, kpad, m_pad, n_pad, rs,
                                                             cs, alpha, C, ldc, tpc, status, Ak,
@@ -873,8 +874,8 @@ static cudaError_t oz_dgemm_impl(int side_b, unsigned long long keyed_epoch, con
 
 cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, const double* A,
                      long long lda, const double* B, long long ldb, double* C, long long ldc,
-                     int* status, cudaStream_t s) {
-  return oz_dgemm_impl(0, 0ULL, sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, status, s);
+                     int* status, cudaStream_t s, int max_ctas) {
+  return oz_dgemm_impl(0, 0ULL, sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, status, s, max_ctas);
 }
 
 cudaError_t oz_dgemm_keyed(const OzScratch& sc, unsigned long long epoch, int m, int n, int k,

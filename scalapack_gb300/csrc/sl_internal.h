@@ -64,9 +64,11 @@ bool oz_fits(const OzScratch& sc, int m, int n, int k);
 // computed in FP64 arithmetic by the same launches. B may alias C (same
 // pointer and leading dimension): the slices are cut before C is written, and
 // the FP64 route takes whole column blocks per CTA.
+// max_ctas > 0 caps the grid (each CTA then takes more tiles), leaving SMs
+// to concurrent streams.
 cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, const double* A,
                      long long lda, const double* B, long long ldb, double* C, long long ldc,
-                     int* status, cudaStream_t s);
+                     int* status, cudaStream_t s, int max_ctas = 0);
 // The same balanced by the row maxima of B, with the budget tested per
 // column: for A = inv(T) - I of a unit-lower diagonal block T and B the rows
 // it updates (the U12 solve), whose rows carry the pivots' scales.
@@ -160,6 +162,9 @@ void set_panel_min_rows(int rows);
 // up (kSpinLimit by default; a test lowers it to make the waits run out).
 long long spin_limit();
 void set_spin_limit(long long polls);
+// SMs (at least min_sms, at most max_sms) that the look-ahead trailing update
+// leaves to the panel's stream; (0, 0) lets it take every SM.
+void set_update_reserve(int min_sms, int max_sms);
 // Block size used when a caller passes nb <= 0.
 int default_nb();
 // While an instance lives on a thread, phase timers record nothing on it

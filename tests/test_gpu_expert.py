@@ -109,7 +109,9 @@ def test_pdgerfs_matches_oracle(sl, orc, ctx, gpu_required, trans, n, nrhs, nb):
     info, w0, iw0 = sl.pdgerfs(trans, n, nrhs, A, 1, 1, d, AF, 1, 1, d, ipiv, B, 1, 1, db, X, 1, 1,
                                db, ferr, berr)
     assert info == 0 and w0 == 3 * n and iw0 == n
-    assert np.all(berr <= 4 * EPS) and np.all(berr_o <= 4 * EPS)
+    # the oracle refines with the GPU factors too; its stopping point can sit a
+    # hair above 4 eps on these kappa = 1e5 inputs
+    assert np.all(berr <= 4 * EPS) and np.all(berr_o <= 8 * EPS)
     assert np.all(ferr > 0)
     np.testing.assert_allclose(ferr, ferr_o, rtol=0.5)
     scale = np.abs(Xo).max(axis=0)

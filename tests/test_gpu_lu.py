@@ -189,6 +189,32 @@ def test_host_path_chunked_copy_matches_device_path(sl, orc, ctx, m, n, nb):
         assert orc.sresid(A0, B0, X) < RESID_THRESH
 
 
+@pytest.mark.parametrize("n,nb", [(3000, 256), (4096, 128)])
+def test_update_sm_reserve_changes_no_bit(sl, orc, ctx, n, nb):
+    # The look-ahead trailing update leaves SMs to the panel's stream by
+    # capping its grid; each tile's product is the same whichever CTA computes
+    # it, so the factors and pivots are bitwise those of the uncapped update.
+    import torch
+
+    L = sl.lib()
+    rng = np.random.default_rng(n + nb)
+    A0 = np.asfortranarray(rng.uniform(-0.5, 0.5, (n, n)))
+    outs = []
+    try:
+        for lo, hi in ((0, 0), (24, 88), (120, 120), (8, 8)):
+            L.sl1x1_set_update_reserve(lo, hi)
+            dA = torch.from_numpy(np.ascontiguousarray(A0.T)).cuda()
+            dpiv = torch.zeros(n, dtype=torch.int32, device="cuda")
+            assert sl.dgetrf_dev(n, n, dA.data_ptr(), n, dpiv.data_ptr(), nb) == 0
+            outs.append((dA.cpu().numpy(), dpiv.cpu().numpy()))
+    finally:
+        L.sl1x1_set_update_reserve(24, 88)
+    for LU_t, piv in outs[1:]:
+        np.testing.assert_array_equal(piv, outs[0][1])
+        np.testing.assert_array_equal(LU_t, outs[0][0])
+    assert orc.fresid(np.asfortranarray(outs[0][0].T), outs[0][1], A0) < RESID_THRESH
+
+
 def test_config_n16384_nb256_full_size(sl, orc, ctx):
     # The headline case at full size: plain FP64 PDGESV, N=16384, NB=256,
     # NRHS=16, U[-0.5,0.5] from the tester's seeded generator. IPIV against
