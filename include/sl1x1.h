@@ -320,6 +320,10 @@ void sl1x1_debug_set_spin_limit(long long polls);
  * column's pivot exchange but a longer rank-1 update per CTA. Changes only the
  * speed, not the results. */
 void sl1x1_set_panel_rows(int rows);
+/* CTAs (8..224, default 64) that the cooperative panel kernel spreads a tall
+ * panel's rows over, before the minimum slice above applies. Changes only the
+ * speed, not the results. */
+void sl1x1_set_panel_ctas(int ctas);
 /* Pipeline depth of the tcgen05 low-precision update used by the mixed
  * factorization and sl1x1_lowp_update_dev: 2 (default; two CTAs per SM, one's
  * epilogue overlapping the other's main loop) or 3 (one CTA per SM). Changes

@@ -1070,6 +1070,11 @@ void sl1x1_set_copy_chunks(int chunks) {
   g_copy_chunks = chunks < 1 ? 1 : (chunks > sl::kMaxColChunks ? sl::kMaxColChunks : chunks);
 }
 
+void sl1x1_set_panel_ctas(int ctas) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  sl::set_panel_ctas(ctas);
+}
+
 void sl1x1_set_panel_rows(int rows) {
   std::lock_guard<std::mutex> lk(g_mu);
   sl::set_panel_min_rows(rows);

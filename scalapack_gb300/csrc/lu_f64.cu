@@ -52,6 +52,9 @@ void set_spin_limit(long long polls) { g_spin_limit = polls < 0 ? kSpinLimit : p
 
 static int g_panel_min_rows = 0;  // 0: automatic (FP32 256, FP64 128)
 int panel_min_rows() { return g_panel_min_rows; }
+static int g_panel_ctas = 64;  // CTAs a panel's rows are spread over (before the minimum rows)
+int panel_ctas() { return g_panel_ctas; }
+void set_panel_ctas(int g) { g_panel_ctas = g < 8 ? 8 : (g > 224 ? 224 : g); }
 void set_panel_min_rows(int rows) { g_panel_min_rows = rows <= 0 ? 0 : (rows < 8 ? 8 : (rows > 768 ? 768 : rows)); }
 
 SplitKScratch& splitk_scratch() {
@@ -72,40 +75,39 @@ cudaError_t ipiv_shift(const int* src, int* dst, int n, int delta, cudaStream_t 
   return cudaGetLastError();
 }
 
-// Composed row permutation of the n sequential interchanges i <-> ipiv[i]:
-// perm[i] = original row that ends in row i. One CTA, the walk in shared
-// memory (n*4 bytes <= 200 KB) or in global memory otherwise.
-__global__ void perm_compose_kernel(const int* __restrict__ ipiv, int n, int* perm, int use_smem) {
+// Composed row permutation of the n sequential interchanges j <-> ipiv[j]:
+// perm[i] = original row that ends in row i. Thread i walks the interchanges
+// backwards from the last, following the row whose content ends in row i
+// (interchange j moves it from ipiv[j] to j or from j to ipiv[j]); the pivots
+// are compared, never used as addresses, so any IPIV is safe. The walk is the
+// same for every thread of a warp (broadcast reads of one pivot at a time),
+// from shared memory when n*4 bytes fit in 192 KB.
+__global__ void __launch_bounds__(256)
+perm_compose_kernel(const int* __restrict__ ipiv, int n, int* perm, int use_smem) {
   extern __shared__ int sp[];
-  int* p = use_smem ? sp : perm;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = i;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int i = 0; i < n; ++i) {
-      int q = ipiv[i];
-      if (q != i) {
-        int t = p[i];
-        p[i] = p[q];
-        p[q] = t;
-      }
-    }
+  const int* pv = ipiv;
+  if (use_smem) {
+    for (int j = threadIdx.x; j < n; j += blockDim.x) sp[j] = ipiv[j];
+    __syncthreads();
+    pv = sp;
   }
-  __syncthreads();
-  if (use_smem)
-    for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = sp[i];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int q = i;
+  for (int j = n - 1; j >= 0; --j) {
+    const int p = pv[j];
+    q = (q == j) ? p : ((q == p) ? j : q);
+  }
+  if (i < n) perm[i] = q;
 }
 
 cudaError_t perm_compose(const int* dipiv, int n, int* perm, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const size_t smem = sizeof(int) * (size_t)n;
-  const int use_smem = smem <= 200 * 1024 ? 1 : 0;
-  static bool attr = false;
-  if (!attr) {
-    SL_TRY(cudaFuncSetAttribute(perm_compose_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                200 * 1024));
-    attr = true;
-  }
-  perm_compose_kernel<<<1, 1024, use_smem ? smem : 0, s>>>(dipiv, n, perm, use_smem);
+  const int use_smem = smem <= 192 * 1024 ? 1 : 0;
+  static const cudaError_t attr = cudaFuncSetAttribute(
+      perm_compose_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 192 * 1024);
+  SL_TRY(attr);
+  perm_compose_kernel<<<(n + 255) / 256, 256, use_smem ? smem : 0, s>>>(dipiv, n, perm, use_smem);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -559,91 +561,177 @@ tri_inv64_kernel(int n, const double* __restrict__ A, long long lda, double* D) 
   }
 }
 
-// X(k0:k0+kb, c) = inv(T_bb) X(k0:k0+kb, c) for the 128-row block at k0 of
-// the unit-lower L (LOWER, forward) or the upper U (backward), from the
-// inverses of its two 64x64 diagonal blocks and its off-diagonal 64x64 block
-// read from A: one CTA per right-hand side, 128 threads.
+// Balancing keys of the blocked NOTRAN solve's sliced products, once per
+// solve: for column k of the factor, with b = k / 128, ck[k] is the largest
+// exponent key of the unit-lower L's entries in rows [(b+1)*128, n) and
+// ck[npad + k] that of U's entries in rows [0, b*128) -- the rows of the A
+// operand of the product that follows block b's solve (the low 12 bits of
+// oz_key_word; 0: no finite nonzero entry). One warp per column.
+__global__ void __launch_bounds__(256)
+solve_ckeys_kernel(int n, const double* __restrict__ A, long long lda, unsigned* ck, int npad) {
+  const int k = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (k >= n) return;
+  const double* col = A + (long long)k * lda;
+  const int lo = (k / 128) * 128, hi = lo + 128;
+  unsigned kl = 0u, ku = 0u;
+  for (int i = hi + lane; i < n; i += 32) kl = max(kl, (unsigned)oz_key_word(col[i], 0ULL));
+  for (int i = lane; i < lo; i += 32) ku = max(ku, (unsigned)oz_key_word(col[i], 0ULL));
+  kl = __reduce_max_sync(0xffffffffu, kl);
+  ku = __reduce_max_sync(0xffffffffu, ku);
+  if (lane == 0) {
+    ck[k] = kl;
+    ck[npad + k] = ku;
+  }
+}
+
+// One block step of the blocked NOTRAN solve: X(k0:k0+kb, c) =
+// inv(T_bb) X(k0:k0+kb, c) for the 128-row block at k0 of the unit-lower L
+// (LOWER, forward) or the upper U (backward), from the inverses of its two
+// 64x64 diagonal blocks and its off-diagonal 64x64 block, staged in shared
+// memory. CTA c < nrhs takes right-hand side c (threads 0..127 one row each);
+// with ckeys set, the CTAs also publish the balancing keys of the sliced
+// product that follows (A: the factor's columns k0..k0+kb outside the block,
+// B: the solved rows): the h keys from each column's solved values and, in
+// the extra CTA nrhs, the c keys from ck.
+constexpr int kBlkSmem = 3 * 64 * 64 * (int)sizeof(double);
 template <bool LOWER>
-__global__ void __launch_bounds__(128)
-diag_apply128_kernel(int kb, const double* __restrict__ A, long long lda, int k0,
-                     const double* __restrict__ D, double* X, long long ldx) {
+__global__ void __launch_bounds__(256)
+solve_block128_kernel(int kb, const double* __restrict__ A, long long lda, int k0,
+                      const double* __restrict__ D, double* X, long long ldx, int nrhs,
+                      const unsigned* __restrict__ ck, unsigned long long* ckeys,
+                      unsigned long long* hkeys, unsigned long long epoch) {
+  extern __shared__ double blk_smem[];  // D0, D1 and the off-diagonal block O, each [c*64 + r]
   __shared__ double xs[128], ys[128];
   const int c = blockIdx.x, t = threadIdx.x;
+  if (c == nrhs) {  // the c keys of the following product
+    if (t < kb && ck[k0 + t]) atomicMax(ckeys + t, (epoch << 12) | ck[k0 + t]);
+    return;
+  }
   double* x = X + k0 + (long long)c * ldx;
-  xs[t] = (t < kb) ? x[t] : 0.0;
-  __syncthreads();
   const int b0 = k0 / 64;  // first 64-block
   const int w0 = kb < 64 ? kb : 64, w1 = kb - w0;
-  const double* D0 = D + (size_t)b0 * 4096;
-  const double* D1 = D0 + 4096;
+  double* D0s = blk_smem;
+  double* D1s = blk_smem + 4096;
+  double* Os = blk_smem + 2 * 4096;
+  {
+    // every load of the staging is issued before the first store (one
+    // memory round trip): D0 and D1 (D1 follows D0 in memory; only when the
+    // block has a second half), O = L10 (rows 64.., columns 0..) or U01
+    // (rows 0.., columns 64..), [i*64 + r], and this column's right-hand side
+    const double2* Dg = reinterpret_cast<const double2*>(D + (size_t)b0 * 4096);
+    const int nd = (w1 > 0 ? 2 : 1) * 2048;
+    const double xv = (t < kb) ? x[t] : 0.0;
+    double2 rd[16];
+    double ro[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int idx = t + 256 * q;
+      rd[q] = idx < nd ? Dg[idx] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int idx = t + 256 * q;
+      const int r = idx & 63, i = idx >> 6;
+      const bool in = LOWER ? (r < w1 && i < w0) : (r < w0 && i < w1);
+      const long long off = LOWER ? (k0 + 64 + r) + (long long)(k0 + i) * lda
+                                  : (k0 + r) + (long long)(k0 + 64 + i) * lda;
+      ro[q] = in ? A[off] : 0.0;
+    }
+    double2* d = reinterpret_cast<double2*>(blk_smem);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) d[t + 256 * q] = rd[q];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) Os[t + 256 * q] = ro[q];
+    if (t < 128) xs[t] = xv;
+  }
+  __syncthreads();
   if (LOWER) {
     // y0 = inv(L00) x0; x1 -= L10 y0; y1 = inv(L11) x1
     if (t < 64) {
       double acc = 0.0;
-      for (int i = 0; i < 64; ++i) acc = fma(D0[i * 64 + t], xs[i], acc);
+      for (int i = 0; i < 64; ++i) acc = fma(D0s[i * 64 + t], xs[i], acc);
       ys[t] = acc;
     }
     __syncthreads();
-    if (t >= 64 && t - 64 < w1) {
+    if (t >= 64 && t < 128 && t - 64 < w1) {
       double acc = xs[t];
-      for (int i = 0; i < w0; ++i) acc = fma(-A[(k0 + t) + (long long)(k0 + i) * lda], ys[i], acc);
+      for (int i = 0; i < w0; ++i) acc = fma(-Os[i * 64 + (t - 64)], ys[i], acc);
       xs[t] = acc;
     }
     __syncthreads();
-    if (t >= 64 && w1 > 0) {  // (no second 64-block when kb <= 64)
+    if (t >= 64 && t < 128 && w1 > 0) {  // (no second 64-block when kb <= 64)
       const int r = t - 64;
       double acc = 0.0;
-      for (int i = 0; i < 64; ++i) acc = fma(D1[i * 64 + r], xs[64 + i], acc);
+      for (int i = 0; i < 64; ++i) acc = fma(D1s[i * 64 + r], xs[64 + i], acc);
       ys[t] = acc;
     }
   } else {
     // y1 = inv(U11) x1; x0 -= U01 y1; y0 = inv(U00) x0
-    if (t >= 64 && w1 > 0) {
+    if (t >= 64 && t < 128 && w1 > 0) {
       const int r = t - 64;
       double acc = 0.0;
-      for (int i = 0; i < 64; ++i) acc = fma(D1[i * 64 + r], xs[64 + i], acc);
+      for (int i = 0; i < 64; ++i) acc = fma(D1s[i * 64 + r], xs[64 + i], acc);
       ys[t] = acc;
-    } else if (t >= 64) {
+    } else if (t >= 64 && t < 128) {
       ys[t] = 0.0;
     }
     __syncthreads();
     if (t < 64 && w1 > 0) {
       double acc = xs[t];
-      for (int i = 0; i < w1; ++i) acc = fma(-A[(k0 + t) + (long long)(k0 + 64 + i) * lda], ys[64 + i], acc);
+      for (int i = 0; i < w1; ++i) acc = fma(-Os[i * 64 + t], ys[64 + i], acc);
       xs[t] = acc;
     }
     __syncthreads();
     if (t < 64) {
       double acc = 0.0;
-      for (int i = 0; i < 64; ++i) acc = fma(D0[i * 64 + t], xs[i], acc);
+      for (int i = 0; i < 64; ++i) acc = fma(D0s[i * 64 + t], xs[i], acc);
       ys[t] = acc;
     }
   }
   __syncthreads();
-  if (t < kb) x[t] = ys[t];
+  if (t < kb) {
+    x[t] = ys[t];
+    if (hkeys) {
+      const unsigned long long w = oz_key_word(ys[t], epoch);
+      if (w) atomicMax(hkeys + t, w);
+    }
+  }
 }
 
-// Blocked NOTRAN solve with the diagonal-block inverses (ws.dinv_solve, L
-// blocks then U blocks) and the off-diagonal updates on the tensor cores:
-// 128-row blocks, each applied by inverse and then subtracted from the rest.
+// Blocked NOTRAN solve with the diagonal-block inverses (ws.dinv_solve: L
+// blocks, then U blocks, then the column keys) and the off-diagonal updates
+// as sliced products on the tensor cores: 128-row blocks, each applied by
+// inverse and then subtracted from the rest. The products take their
+// balancing keys from the block step (no key pass over the factor per step).
 static cudaError_t tri_solve_inv(bool lower, int n, int nrhs, const double* A, long long lda,
                                  double* X, long long ldx, const LuWork& ws, cudaStream_t s) {
   constexpr int KB = 128;
   const int nblk = (n + KB - 1) / KB;
-  const double* D = ws.dinv_solve + (lower ? 0 : (size_t)((n + 63) / 64) * 4096);
+  const int nb64 = (n + 63) / 64;
+  const double* D = ws.dinv_solve + (lower ? 0 : (size_t)nb64 * 4096);
+  const unsigned* ck = reinterpret_cast<const unsigned*>(ws.dinv_solve + (size_t)2 * nb64 * 4096) +
+                       (lower ? 0 : nb64 * 64);
+  unsigned long long* ckeys = oz_ckeys(ws.oz);
+  unsigned long long* hkeys = oz_hkeys(ws.oz);
   for (int bi = 0; bi < nblk; ++bi) {
     const int b = lower ? bi : nblk - 1 - bi;
     const int k0 = b * KB, kb = (n - k0) < KB ? (n - k0) : KB;
-    if (lower) diag_apply128_kernel<true><<<nrhs, 128, 0, s>>>(kb, A, lda, k0, D, X, ldx);
-    else diag_apply128_kernel<false><<<nrhs, 128, 0, s>>>(kb, A, lda, k0, D, X, ldx);
+    const int rest = lower ? n - k0 - kb : k0;
+    const unsigned long long ep = rest > 0 ? oz_new_epoch() : 0ULL;
+    if (lower)
+      solve_block128_kernel<true><<<nrhs + (rest > 0 ? 1 : 0), 256, kBlkSmem, s>>>(
+          kb, A, lda, k0, D, X, ldx, nrhs, ck, ckeys, rest > 0 ? hkeys : nullptr, ep);
+    else
+      solve_block128_kernel<false><<<nrhs + (rest > 0 ? 1 : 0), 256, kBlkSmem, s>>>(
+          kb, A, lda, k0, D, X, ldx, nrhs, ck, ckeys, rest > 0 ? hkeys : nullptr, ep);
     count_launches(1);
     SL_TRY(cudaGetLastError());
-    if (lower && k0 + kb < n)
-      SL_TRY(oz_dgemm(ws.oz, n - k0 - kb, nrhs, kb, -1.0, A + (k0 + kb) + (long long)k0 * lda, lda,
-                      X + k0, ldx, X + k0 + kb, ldx, ws.status, s));
-    else if (!lower && k0 > 0)
-      SL_TRY(oz_dgemm(ws.oz, k0, nrhs, kb, -1.0, A + (long long)k0 * lda, lda, X + k0, ldx, X, ldx,
-                      ws.status, s));
+    if (rest > 0 && lower)
+      SL_TRY(oz_dgemm_keyed(ws.oz, ep, rest, nrhs, kb, -1.0, A + (k0 + kb) + (long long)k0 * lda, lda,
+                            X + k0, ldx, X + k0 + kb, ldx, ws.status, s));
+    else if (rest > 0)
+      SL_TRY(oz_dgemm_keyed(ws.oz, ep, k0, nrhs, kb, -1.0, A + (long long)k0 * lda, lda, X + k0, ldx,
+                            X, ldx, ws.status, s));
   }
   return cudaSuccess;
 }
@@ -666,11 +754,19 @@ cudaError_t dgetrs_device(char trans, int n, int nrhs, const double* dA, long lo
         tri_inv64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvSmem);
     static const cudaError_t a1 = cudaFuncSetAttribute(
         tri_inv64_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvSmem);
+    static const cudaError_t a2 = cudaFuncSetAttribute(
+        solve_block128_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBlkSmem);
+    static const cudaError_t a3 = cudaFuncSetAttribute(
+        solve_block128_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBlkSmem);
     SL_TRY(a0);
     SL_TRY(a1);
+    SL_TRY(a2);
+    SL_TRY(a3);
     tri_inv64_kernel<true><<<nb64, 256, kInvSmem, s>>>(n, dA, ldda, ws.dinv_solve);
     tri_inv64_kernel<false><<<nb64, 256, kInvSmem, s>>>(n, dA, ldda, ws.dinv_solve + (size_t)nb64 * 4096);
-    count_launches(2);
+    solve_ckeys_kernel<<<(n + 7) / 8, 256, 0, s>>>(
+        n, dA, ldda, reinterpret_cast<unsigned*>(ws.dinv_solve + (size_t)2 * nb64 * 4096), nb64 * 64);
+    count_launches(3);
     SL_TRY(cudaGetLastError());
     SL_TRY(tri_solve_inv(true, n, nrhs, dA, ldda, X, n, ws, s));
     SL_TRY(tri_solve_inv(false, n, nrhs, dA, ldda, X, n, ws, s));

@@ -1045,7 +1045,7 @@ inline cudaError_t launch_panel(T* A, long long lda, int m, int r0, int c0, int 
   // Tall panels beyond 64 CTAs' shared memory spread over every SM instead;
   // beyond every SM's shared memory the rows go to the global buffer ws.ptile.
   const int rpc_max = (int)((200 * 1024) / (sizeof(T) * PLD)) & ~7;
-  int rpc = (R + 63) / 64;
+  int rpc = (R + panel_ctas() - 1) / panel_ctas();
   const int lo_rows = panel_min_rows() > 0 ? panel_min_rows() : (sizeof(T) == 4 ? 256 : 128);
   if (rpc < lo_rows) rpc = lo_rows;
   if (rpc > rpc_max) rpc = (R + num_sms() - 1) / num_sms();

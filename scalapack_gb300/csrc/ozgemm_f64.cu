@@ -616,6 +616,27 @@ oz_split_kernel(const double* __restrict__ A, long long lda, int m, const double
                 __nv_bfloat16* Sa, __nv_bfloat16* Sb, double* rs, double* cs,
                 unsigned long long* kinfo, unsigned long long epoch, int side_b) {
   __shared__ int s_c[OZ_KMAX], s_h[OZ_KMAX], s_d[OZ_KMAX];
+  // A blocks: the CTA's 32 rows x kpad of A, as bits, sA[kk * 33 + row],
+  // loaded once (before the balancing words, so both reads overlap) and read
+  // by the budget test and the slicing
+  extern __shared__ unsigned long long sA[];
+  const int nrb = m_pad / 32;
+  if ((int)blockIdx.x < nrb) {
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i = (int)blockIdx.x * 32 + tx;
+    unsigned long long v[OZ_KMAX / 8];
+#pragma unroll
+    for (int q = 0; q < OZ_KMAX / 8; ++q) {
+      const int kk = ty + 8 * q;
+      v[q] = (i < m && kk < kb) ? (unsigned long long)__double_as_longlong(A[i + (long long)kk * lda])
+                                : 0ULL;
+    }
+#pragma unroll
+    for (int q = 0; q < OZ_KMAX / 8; ++q) {
+      const int kk = ty + 8 * q;
+      if (kk < kpad) sA[kk * 33 + tx] = v[q];
+    }
+  }
   for (int k = threadIdx.x; k < OZ_KMAX; k += 256) {
     int h = OZ_NOEXP, c = OZ_NOEXP;
     if (k < kb) {
@@ -628,9 +649,7 @@ oz_split_kernel(const double* __restrict__ A, long long lda, int m, const double
     s_d[k] = (c == OZ_NOEXP) ? OZ_NOEXP : (side_b ? -h : c);
   }
   __syncthreads();
-  const int nrb = m_pad / 32;
   if ((int)blockIdx.x < nrb) {
-    __shared__ unsigned long long tile[64][33];
     __shared__ int redE[8][33], redF[8][33];
     __shared__ int s_e[32];
     __shared__ int s_bad[32];
@@ -650,8 +669,7 @@ oz_split_kernel(const double* __restrict__ A, long long lda, int m, const double
     int em = OZ_NOEXP, fm = OZ_NOEXP, bad = 0;
     if (i < m)
       for (int kk = ty; kk < kb; kk += 8) {
-        const unsigned long long mag =
-            (unsigned long long)__double_as_longlong(A[i + (long long)kk * lda]) & kMagMask;
+        const unsigned long long mag = sA[kk * 33 + tx] & kMagMask;
         if (mag >= kInfBits) {
           bad = 1;
         } else if (mag != 0ULL && s_d[kk] != OZ_NOEXP) {
@@ -685,19 +703,12 @@ oz_split_kernel(const double* __restrict__ A, long long lda, int m, const double
     const int e = s_e[r];
     const bool zero = s_bad[r] != 0 || e == OZ_NOEXP;
     for (int k0 = 0; k0 < kpad; k0 += 64) {
-      for (int q = ty; q < 64; q += 8) {
-        const int kk = k0 + q;
-        tile[q][tx] = (i < m && kk < kb)
-                          ? (unsigned long long)__double_as_longlong(A[i + (long long)kk * lda])
-                          : 0ULL;
-      }
-      __syncthreads();
       unsigned long long U[8];
       bool neg[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int kk = k0 + g * 8 + q;
-        const unsigned long long bits = tile[g * 8 + q][r];
+        const unsigned long long bits = sA[kk * 33 + r];
         neg[q] = (bits >> 63) != 0ULL;
         const int d = s_d[kk];
         U[q] = (zero || d == OZ_NOEXP) ? 0ULL : oz_fixed(bits & kMagMask, e + d);
@@ -712,7 +723,6 @@ oz_split_kernel(const double* __restrict__ A, long long lda, int m, const double
               *reinterpret_cast<const uint4*>(h);
         }
       }
-      __syncthreads();
     }
     return;
   }
@@ -775,10 +785,15 @@ bool make_slice_map(CUtensorMap* map, const void* ptr, int rows_total, int kpad,
   return r == CUDA_SUCCESS;
 }
 
+// dynamic shared memory of oz_split_kernel: the A rows of one CTA
+inline size_t oz_split_smem(int kpad) { return (size_t)kpad * 33 * sizeof(unsigned long long); }
+
 cudaError_t oz_smem_once() {
   static const cudaError_t e = cudaFuncSetAttribute(
       ozgemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_smem_bytes());
-  return e;
+  static const cudaError_t e2 = cudaFuncSetAttribute(
+      oz_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_split_smem(OZ_KMAX));
+  return e != cudaSuccess ? e : e2;
 }
 
 inline int round_up(int x, int q) { return (x + q - 1) / q * q; }
@@ -849,7 +864,7 @@ static cudaError_t oz_dgemm_impl(int side_b, unsigned long long keyed_epoch, con
       oz_kscale_kernel<<<nab + nbb, 256, 0, s>>>(Ak, lda, m, Bk, ldb, n, kb, nab, kinfo, epoch);
       count_launches(1);
     }
-    oz_split_kernel<<<m_pad / 32 + n_pad / 8, 256, 0, s>>>(Ak, lda, m, Bk, ldb, n, kb, kpad, m_pad,
+    oz_split_kernel<<<m_pad / 32 + n_pad / 8, 256, oz_split_smem(kpad), s>>>(Ak, lda, m, Bk, ldb, n, kb, kpad, m_pad,
                                                           n_pad, sa, sb, rs, cs, kinfo, epoch,
                                                           side_b);
     CUtensorMap ta, tb;

@@ -139,7 +139,11 @@ struct LuWork {
 };
 // Most column chunks a streamed factorization takes.
 constexpr int kMaxColChunks = 16;
-inline size_t kSolveInvDoubles(int n) { return (size_t)2 * (size_t)((n + 63) / 64) * 64 * 64; }
+// 64x64 inverses of the diagonal blocks of L and U, then two 32-bit column
+// keys per column (padded to 64).
+inline size_t kSolveInvDoubles(int n) {
+  return (size_t)2 * (size_t)((n + 63) / 64) * 64 * 64 + (size_t)((n + 63) / 64) * 64;
+}
 // Doubles of the U12 solve's diagonal-block inverses: NB <= 1024 in 64-row blocks.
 constexpr size_t kDinv64Doubles = (size_t)16 * 64 * 64;
 
@@ -157,6 +161,8 @@ size_t panel_tile_doubles(int m);
 // Smallest row slice per CTA of the cooperative panel (tunable; 0, the
 // default, means 256 rows for FP32 and 128 for FP64).
 int panel_min_rows();
+int panel_ctas();
+void set_panel_ctas(int g);
 void set_panel_min_rows(int rows);
 // Polls a panel CTA makes for another CTA's published words before it gives
 // up (kSpinLimit by default; a test lowers it to make the waits run out).
