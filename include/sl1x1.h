@@ -281,8 +281,15 @@ void sl1x1_finalize(void);
 /* Block size NB used by the device entry points when nb <= 0 (default 256). */
 void sl1x1_set_default_nb(int nb);
 /* Look-ahead in the factorizations (default on): the next panel is factored
- * on a second stream while the trailing update runs. Same results either way. */
+ * on a second stream while the trailing update runs. Same pivots (except
+ * where two candidates tie to rounding) and factors equal to rounding either
+ * way: the U12 solve balances its slices by the columns it is given. */
 void sl1x1_set_lookahead(int on);
+/* Split look-ahead step (default on; needs the look-ahead): after each panel,
+ * the panel's stream brings the next panel's columns up to date itself
+ * (interchanges, U12 solve, update) and factors it, while the caller's stream
+ * handles the other columns. Results as for sl1x1_set_lookahead. */
+void sl1x1_set_split_step(int on);
 /* Column chunks of A's host-to-device copy in pdgetrf_ / pdgesv_ (1..16,
  * default 8; 1 = one copy before the factorization): with more than one, A
  * goes over in chunks of whole panels on a copy stream and step 0 of the

@@ -129,6 +129,7 @@ DevState g_dev;
 int g_default_nb = 256;
 double g_ir_cost_ratio = 3.5;  // mixed solver: FP64 cost / low-precision factor time
 bool g_lookahead = true;
+bool g_split_step = true;  // the next panel's columns on the panel's stream
 int g_fail_alloc_in = -1;
 int g_copy_chunks = 8;  // column chunks of A's host-to-device copy (<= 1: one copy)
 
@@ -161,7 +162,7 @@ bool ensure_device() {
   }
   if (cudaMalloc(&g_dev.dsmall, 16 * sizeof(int)) != cudaSuccess) return false;
   if (cudaMalloc(&g_dev.dcand, sl::panel_cand_doubles() * sizeof(double)) != cudaSuccess) return false;
-  if (cudaMalloc(&g_dev.dplan, sl::kSwapPlanInts * sizeof(int)) != cudaSuccess) return false;
+  if (cudaMalloc(&g_dev.dplan, 2 * sl::kSwapPlanInts * sizeof(int)) != cudaSuccess) return false;
   g_dev.ok = true;
   return true;
 }
@@ -191,6 +192,17 @@ void release_all() {
   g_dev = DevState();
 }
 
+// Grows a sliced-product scratch buffer; a new one starts with its balancing
+// words zeroed (the memory may hold anything, including words that look like
+// a later epoch's).
+static cudaError_t grow_oz(unsigned char** p, size_t* cap, size_t need) {
+  const unsigned char* old = *p;
+  cudaError_t e = grow(p, cap, need);
+  if (e == cudaSuccess && *p != old)
+    e = cudaMemset(*p, 0, *cap < (size_t)sl::kOzKinfoBytes ? *cap : (size_t)sl::kOzKinfoBytes);
+  return e;
+}
+
 void ensure_oz(int m, int n, int nb) {
   // panels taller than the SMs' shared memory holds keep their rows in a
   // global buffer (optional: without it such an M is rejected with -30000)
@@ -200,13 +212,14 @@ void ensure_oz(int m, int n, int nb) {
   if (sl::f64_update_get() != 1 || m <= 0 || n <= 0) return;
   if (nb <= 0) nb = g_default_nb;
   const size_t need = sl::oz_scratch_bytes(m, n, nb);
-  const size_t need2 = sl::oz_scratch_bytes(m, nb, 32);  // the panel's 32-column updates
+  // the panel's 32-column updates and the next panel's columns (nb x nb)
+  const size_t need2 = sl::oz_scratch_bytes(m, nb, nb > 32 ? nb : 32);
   cudaError_t e = cudaSuccess;
-  if (need > g_dev.capOz || !g_dev.doz) e = grow(&g_dev.doz, &g_dev.capOz, need);
+  if (need > g_dev.capOz || !g_dev.doz) e = grow_oz(&g_dev.doz, &g_dev.capOz, need);
   if (e == cudaSuccess && (need2 > g_dev.capOz2 || !g_dev.doz2))
-    e = grow(&g_dev.doz2, &g_dev.capOz2, need2);
+    e = grow_oz(&g_dev.doz2, &g_dev.capOz2, need2);
   if (e == cudaSuccess && !g_dev.ddinv64)
-    e = cudaMalloc(&g_dev.ddinv64, 2 * sl::kDinv64Doubles * sizeof(double));
+    e = cudaMalloc(&g_dev.ddinv64, 3 * sl::kDinv64Doubles * sizeof(double));
   if (e != cudaSuccess) cudaGetLastError();  // the DMMA update covers what is missing
 }
 
@@ -226,6 +239,8 @@ sl::LuWork make_work() {
   w.oz_aux.bytes = g_dev.doz2 ? g_dev.capOz2 : 0;
   w.dinv64 = g_dev.ddinv64;
   w.dinv64_step0 = g_dev.ddinv64 ? g_dev.ddinv64 + sl::kDinv64Doubles : nullptr;
+  w.dinv64_alt = (g_dev.ddinv64 && g_split_step) ? g_dev.ddinv64 + 2 * sl::kDinv64Doubles : nullptr;
+  w.swap_plan_alt = g_split_step ? g_dev.dplan + sl::kSwapPlanInts : nullptr;
   w.dinv_solve = g_dev.ddinvs;
   w.dinv_solve_len = g_dev.ddinvs ? g_dev.capDinvs : 0;
   w.ptile = g_dev.dptile;
@@ -1058,6 +1073,11 @@ void sl1x1_set_lookahead(int on) {
   g_lookahead = (on != 0);
 }
 
+void sl1x1_set_split_step(int on) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_split_step = (on != 0);
+}
+
 int sl1x1_debug_fail_alloc(int k) {
   std::lock_guard<std::mutex> lk(g_mu);
   const int prev = g_fail_alloc_in;
@@ -1114,7 +1134,7 @@ int sl1x1_ozgemm_dev(int m, int n, int k, double alpha, const double* dA, long l
   cudaStream_t s = (cudaStream_t)stream;
   const size_t need = sl::oz_scratch_bytes(m, n, k);
   if (need > g_dev.capOz || !g_dev.doz) {
-    cudaError_t e = grow(&g_dev.doz, &g_dev.capOz, need);
+    cudaError_t e = grow_oz(&g_dev.doz, &g_dev.capOz, need);
     if (e != cudaSuccess) return cuda_info(e);
   }
   sl::OzScratch sc;

@@ -469,21 +469,74 @@ cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, 
     SL_TRY(step0_by_chunks(m, n, dA, ldda, dipiv, nb, ws, s, wait_cols));
     panel_on_aux = true;
   }
+  // Split look-ahead step (both buffer sets present, the panel stream's
+  // scratch holding an m x nb x nb product): once panel j is factored, the
+  // panel stream brings the next panel's columns up to date itself (their
+  // interchanges, U12 solve and update) and factors that panel, while the
+  // caller's stream handles every other column -- so only the next panel's
+  // share of the step lies between two panels. cur holds the inverse and
+  // interchange plan of the panel just factored, nxt receives the next one's;
+  // the caller's stream is done with cur's before the panel stream rewrites
+  // them two panels later (it waits for ev_next, recorded after that work).
+  LuWork cur = ws, nxt = ws;
+  const bool split = lookahead && ws.dinv64_alt && ws.swap_plan_alt && g_f64_update == 1 &&
+                     oz_fits(ws.oz_aux, m, nb, nb);
+  if (split) {
+    nxt.dinv64 = ws.dinv64_alt;
+    nxt.swap_plan = ws.swap_plan_alt;
+  }
   for (int j = stream_step0 ? nb : 0; j < mn; j += nb) {
     const int jb = (mn - j) < nb ? (mn - j) : nb;
     if (panel_on_aux) SL_TRY(cudaStreamWaitEvent(s, ws.ev_panel, 0));
     panel_on_aux = false;
-    // ---- PDLASWP on the left and right column blocks ----
-    phase_begin(kPhLaswp, s);
-    SL_TRY(laswp_planned<double>(dA, ldda, j, j + jb, dipiv, ws.swap_plan, 0, j, j + jb, n, s));
-    phase_end(kPhLaswp, s, 0.0, 32.0 * jb * (double)(n - jb));
     const int jn = j + jb;                                   // next panel's first column
     const int jb2 = jn < mn ? ((mn - jn) < nb ? (mn - jn) : nb) : 0;
+    if (split && jb2 > 0) {
+      const double mr = (double)(m - jn);
+      // panel j, and every update of the caller's stream before it
+      SL_TRY(cudaEventRecord(ws.ev_next, s));
+      SL_TRY(cudaStreamWaitEvent(ws.aux, ws.ev_next, 0));
+      LuWork aw = cur;
+      aw.oz = ws.oz_aux;
+      phase_begin(kPhLaswp, ws.aux);
+      SL_TRY(laswp_planned<double>(dA, ldda, j, jn, dipiv, cur.swap_plan, jn, jn + jb2, jn + jb2, jn + jb2, ws.aux));
+      phase_end(kPhLaswp, ws.aux, 0.0, 32.0 * jb * (double)jb2);
+      phase_begin(kPhTrsm, ws.aux);
+      SL_TRY(solve_u12(jb, jb2, Ap(j, j), ldda, Ap(j, jn), ldda, aw, ws.aux));
+      phase_end(kPhTrsm, ws.aux, (double)jb * jb * jb2, 8.0 * (0.5 * jb * jb + 2.0 * jb * jb2));
+      phase_begin(kPhGemm, ws.aux);
+      SL_TRY(lu_update(ws.oz_aux, m - jn, jb2, jb, -1.0, Ap(jn, j), ldda, Ap(j, jn), ldda, Ap(jn, jn),
+                       ldda, ws, ws.aux));
+      phase_end(kPhGemm, ws.aux, 2.0 * mr * jb2 * jb, 8.0 * (mr * jb + (double)jb * jb2 + 2.0 * mr * jb2));
+      SL_TRY(factor_panel(m, dA, ldda, dipiv, jn, jb2, nxt, ws.aux));
+      SL_TRY(cudaEventRecord(ws.ev_panel, ws.aux));
+      panel_on_aux = true;
+      // the other columns on the caller's stream
+      const int c2 = jn + jb2, rest = n - c2;
+      phase_begin(kPhLaswp, s);
+      SL_TRY(laswp_planned<double>(dA, ldda, j, jn, dipiv, cur.swap_plan, 0, j, c2, n, s));
+      phase_end(kPhLaswp, s, 0.0, 32.0 * jb * (double)(n - jb - jb2));
+      if (rest > 0) {
+        phase_begin(kPhTrsm, s);
+        SL_TRY(solve_u12(jb, rest, Ap(j, j), ldda, Ap(j, c2), ldda, cur, s));
+        phase_end(kPhTrsm, s, (double)jb * jb * rest, 8.0 * (0.5 * jb * jb + 2.0 * jb * rest));
+        phase_begin(kPhGemm, s);
+        SL_TRY(lu_update(ws.oz, m - jn, rest, jb, -1.0, Ap(jn, j), ldda, Ap(j, c2), ldda, Ap(jn, c2),
+                         ldda, ws, s, update_ctas(2.0 * mr * rest * jb)));
+        phase_end(kPhGemm, s, 2.0 * mr * rest * jb, 8.0 * (mr * jb + (double)jb * rest + 2.0 * mr * rest));
+      }
+      std::swap(cur, nxt);
+      continue;
+    }
+    // ---- PDLASWP on the left and right column blocks ----
+    phase_begin(kPhLaswp, s);
+    SL_TRY(laswp_planned<double>(dA, ldda, j, j + jb, dipiv, cur.swap_plan, 0, j, j + jb, n, s));
+    phase_end(kPhLaswp, s, 0.0, 32.0 * jb * (double)(n - jb));
     if (jn < n) {
       // ---- PDTRSM: U12 = L11^{-1} A12 ----
       const double nr = (double)(n - jn);
       phase_begin(kPhTrsm, s);
-      SL_TRY(solve_u12(jb, n - jn, Ap(j, j), ldda, Ap(j, jn), ldda, ws, s));
+      SL_TRY(solve_u12(jb, n - jn, Ap(j, j), ldda, Ap(j, jn), ldda, cur, s));
       phase_end(kPhTrsm, s, (double)jb * jb * nr, 8.0 * (0.5 * jb * jb + 2.0 * jb * nr));
       // ---- PDGEMM: A22 -= L21 * U12 ----
       if (jn < m) {

@@ -115,7 +115,7 @@ constexpr int GROUP_M = 8;       // tile raster: 8 row tiles sweep the columns t
 // B), c keys [256] (columns of A), the FP64-route flag. Each word is
 // (epoch << 12) | (exponent + OZ_EBIAS), so a pass ignores what earlier passes
 // left (epochs only grow) and nothing has to be cleared between passes.
-constexpr int OZ_KINFO_BYTES = 8192;
+constexpr int OZ_KINFO_BYTES = kOzKinfoBytes;
 constexpr int OZ_KI_H = 0, OZ_KI_C = OZ_KMAX, OZ_KI_FLAG = 2 * OZ_KMAX;
 constexpr int OZ_EBIAS = kOzEbias;
 constexpr int OZ_BUDGET = 8;     // bits above the FP64 GEMM's row (column) bound

@@ -136,11 +136,23 @@ struct LuWork {
   // panels are rejected): ptile_len doubles.
   double* ptile = nullptr;
   size_t ptile_len = 0;
+  // Second inverse block (kDinv64Doubles) and interchange plan
+  // (kSwapPlanInts) for the split look-ahead step, in which the next panel's
+  // columns are brought up to date on the panel's stream (with oz_aux, which
+  // then holds an m x nb x nb product) while the caller's stream handles the
+  // other columns: consecutive panels alternate between the two sets. Null:
+  // the next panel's columns go first on the caller's stream.
+  double* dinv64_alt = nullptr;
+  int* swap_plan_alt = nullptr;
 };
 // Most column chunks a streamed factorization takes.
 constexpr int kMaxColChunks = 16;
 // 64x64 inverses of the diagonal blocks of L and U, then two 32-bit column
 // keys per column (padded to 64).
+// Bytes of balancing words at the start of a sliced-product scratch buffer.
+// They are epoch-tagged atomicMax words, so a buffer must start with them
+// zeroed (a stale word of a larger epoch would never be replaced).
+constexpr int kOzKinfoBytes = 8192;
 inline size_t kSolveInvDoubles(int n) {
   return (size_t)2 * (size_t)((n + 63) / 64) * 64 * 64 + (size_t)((n + 63) / 64) * 64;
 }

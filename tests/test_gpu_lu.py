@@ -305,3 +305,26 @@ def test_tall_matrix_beyond_shared_memory_panel(sl, orc, ctx):
     bad, ties = compare_ipiv(orc, A0, ipiv[:n], nb)
     assert bad == 0, ties
     assert orc.fresid(A, ipiv[:n], A0) < RESID_THRESH
+
+
+@pytest.mark.parametrize("n,nb", [(200, 32), (1000, 64)])
+def test_scratch_on_reused_dirty_memory(sl, orc, ctx, n, nb):
+    # The sliced products keep epoch-tagged balancing words at the start of
+    # their scratch buffers; a buffer allocated over memory that held other
+    # data (here: all bits set, freed back to the driver) must start clean,
+    # or the words of later products would never replace the stale ones.
+    import torch
+
+    L = sl.lib()
+    L.sl1x1_finalize()
+    junk = torch.full((1 << 27,), -1, dtype=torch.int64, device="cuda")  # 1 GiB of 0xff
+    torch.cuda.synchronize()
+    del junk
+    torch.cuda.empty_cache()
+    rng = np.random.default_rng(n + 3)
+    A0 = np.asfortranarray(rng.uniform(-1, 1, (n, n)))
+    dA = torch.from_numpy(np.ascontiguousarray(A0.T)).cuda()
+    dpiv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    assert sl.dgetrf_dev(n, n, dA.data_ptr(), n, dpiv.data_ptr(), nb) == 0
+    LU = np.asfortranarray(dA.cpu().numpy().T)
+    assert orc.fresid(LU, dpiv.cpu().numpy(), A0) < RESID_THRESH
