@@ -209,59 +209,66 @@ constexpr int kFullInvMax = 256;
 // c: x = e_c, then for q = c, c+1, ... x_q is final and every row i > q loses
 // L(i,q) x_q -- forward substitution in the order of a strip solve, with x_q
 // passed by a shuffle from the lane that owns row q (lane l owns rows l, l+32,
-// ..., in registers). The CTA's 8 warps stage L 32 columns at a time in
-// shared memory (rows from the chunk's first column down), so the 32 steps of
-// a chunk read shared memory only and no block barrier sits inside them.
-// With a plan to make (plan != null), one extra block computes the panel's
-// interchange plan (laswp_plan_block) in the same launch: both only read the
-// finished panel.
-constexpr int kInvColsSmem = 32 * 257 * (int)sizeof(double);
-__global__ void __launch_bounds__(256)
+// ..., in registers). Column c costs about (jb-c)^2/2 FMAs on the FP64 pipe,
+// so warp pairs take columns p and jb-1-p (equal work per pair) and a CTA of
+// kInvColsWarps warps holds kInvColsWarps/2 pairs: the work spreads evenly
+// over jb/kInvColsWarps CTAs. L is read from global memory (L2) two columns
+// ahead of its use, no shared memory and no block barrier. With a plan to
+// make (plan != null), one extra block computes the panel's interchange plan
+// (laswp_plan_block) in the same launch: both only read the finished panel.
+constexpr int kInvColsWarps = 4;
+__host__ __device__ inline int inv_cols_blocks(int jb) {
+  const int pairs = (jb + 1) / 2;
+  return (pairs + kInvColsWarps / 2 - 1) / (kInvColsWarps / 2);
+}
+__global__ void __launch_bounds__(32 * kInvColsWarps)
 unit_lower_inv_cols_kernel(int jb, const double* __restrict__ L, long long ldl, double* X,
                            int ldx, int k1, int k2, const int* __restrict__ ipiv, int* plan) {
-  if (plan != nullptr && (int)blockIdx.x == (jb + 7) / 8) {
+  if (plan != nullptr && (int)blockIdx.x == inv_cols_blocks(jb)) {
     laswp_plan_block(k1, k2, ipiv, plan);
     return;
   }
-  extern __shared__ double inv_ls[];  // Ls[l * 257 + i] = L(i, 32 tq + l)
-  const int lane = threadIdx.x & 31;
-  const int c = (int)blockIdx.x * 8 + (threadIdx.x >> 5);
-  const int cmin = (int)blockIdx.x * 8;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int p = (int)blockIdx.x * (kInvColsWarps / 2) + (warp >> 1);
+  const int c = (warp & 1) ? jb - 1 - p : p;
+  // the middle column of an odd jb has no partner; pairs past the end none
+  if (p >= (jb + 1) / 2 || ((warp & 1) && c == p)) return;
   double xr[8];
 #pragma unroll
   for (int t = 0; t < 8; ++t) xr[t] = (lane + 32 * t == c) ? 1.0 : 0.0;
-#pragma unroll
-  for (int tq = 0; tq < 8; ++tq) {
-    const int q0 = 32 * tq;
-    if (q0 >= jb) break;
-    if (q0 + 31 < cmin) continue;  // no column of this CTA starts before the chunk ends
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < 32 * 256; idx += 256) {
-      const int l = idx >> 8, i = idx & 255;
-      if (q0 + l < jb && i > q0 + l && i < jb) inv_ls[l * 257 + i] = L[i + (long long)(q0 + l) * ldl];
-    }
-    __syncthreads();
-    if (c < jb && q0 + 31 >= c) {
-      for (int l = 0; l < 32; ++l) {
-        const int q = q0 + l;
-        if (q >= jb) break;
-        const double xq = __shfl_sync(0xffffffffu, xr[tq], l);
-        if (q < c) continue;
-        const double* Lq = inv_ls + l * 257;
-#pragma unroll
-        for (int t = tq; t < 8; ++t) {
-          const int i = lane + 32 * t;
-          if (i > q && i < jb) xr[t] = fma(-Lq[i], xq, xr[t]);
-        }
-      }
-    }
-  }
-  if (c < jb) {
+  // L(lane + 32 t, q) for t >= q / 32, rows > q and < jb (0 elsewhere)
+  auto load_col = [&](int q, int tq, double* v) {
 #pragma unroll
     for (int t = 0; t < 8; ++t) {
       const int i = lane + 32 * t;
-      if (i < jb) X[i + (long long)c * ldx] = (i > c) ? xr[t] : 0.0;
+      v[t] = (t >= tq && q < jb && i > q && i < jb) ? __ldg(L + i + (long long)q * ldl) : 0.0;
     }
+  };
+  double v0[8], v1[8];
+  load_col(c, c >> 5, v0);
+  load_col(c + 1, (c + 1) >> 5, v1);
+#pragma unroll
+  for (int tq = 0; tq < 8; ++tq) {
+    if (32 * tq + 31 < c || 32 * tq >= jb) continue;
+    for (int l = (c > 32 * tq ? c - 32 * tq : 0); l < 32; ++l) {
+      const int q = 32 * tq + l;
+      if (q >= jb) break;
+      double v2[8];
+      load_col(q + 2, (q + 2) >> 5, v2);  // two columns ahead
+      const double xq = __shfl_sync(0xffffffffu, xr[tq], l);
+#pragma unroll
+      for (int t = tq; t < 8; ++t) xr[t] = fma(-v0[t], xq, xr[t]);
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        v0[t] = v1[t];
+        v1[t] = v2[t];
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    const int i = lane + 32 * t;
+    if (i < jb) X[i + (long long)c * ldx] = (i > c) ? xr[t] : 0.0;
   }
 }
 
@@ -342,12 +349,9 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
   if (g_f64_update == 1 && ws.dinv64 && npiv == jb && jb <= kFullInvMax) {
     // inv(L11) - I whole (jb x jb, leading dimension jb), and the interchange
     // plan in the same launch
-    static const cudaError_t attr = cudaFuncSetAttribute(
-        unit_lower_inv_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvColsSmem);
-    SL_TRY(attr);
     if (want_plan && npiv <= 0) SL_TRY(cudaMemsetAsync(ws.swap_plan, 0, sizeof(int), s));
     const bool fused = want_plan && npiv > 0;
-    unit_lower_inv_cols_kernel<<<(jb + 7) / 8 + (fused ? 1 : 0), 256, kInvColsSmem, s>>>(
+    unit_lower_inv_cols_kernel<<<inv_cols_blocks(jb) + (fused ? 1 : 0), 32 * kInvColsWarps, 0, s>>>(
         jb, Ap(j, j), ldda, ws.dinv64, jb, j, j + npiv, dipiv, fused ? ws.swap_plan : nullptr);
     count_launches(1);
     SL_TRY(cudaGetLastError());
