@@ -313,6 +313,10 @@ int sl1x1_debug_fail_alloc(int k);
  * (default 88). (0, 0) lets the update take every SM. Values are clamped to
  * 0..120. Changes only the speed. */
 void sl1x1_set_update_reserve(int min_sms, int max_sms);
+/* The estimate behind that rule: sliced-product flops one SM takes within a
+ * panel period (default 3.2e8; larger values leave the panel more SMs; <= 1e6
+ * restores the default). Changes only the speed. */
+void sl1x1_set_update_share(double flops_per_sm);
 /* Test hook for the bounded device waits: the number of polls a panel CTA
  * makes for another CTA's published pivot candidates before it gives up
  * (polls < 0 restores the default, 2^24; 0 makes every wait run out at its

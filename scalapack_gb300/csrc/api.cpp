@@ -1155,6 +1155,11 @@ void sl1x1_set_update_reserve(int min_sms, int max_sms) {
   sl::set_update_reserve(min_sms, max_sms);
 }
 
+void sl1x1_set_update_share(double flops_per_sm) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  sl::set_update_share(flops_per_sm);
+}
+
 void sl1x1_debug_set_spin_limit(long long polls) {
   std::lock_guard<std::mutex> lk(g_mu);
   sl::set_spin_limit(polls);

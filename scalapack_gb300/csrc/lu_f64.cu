@@ -124,18 +124,21 @@ int f64_update_get() { return g_f64_update; }
 // cooperative kernel makes progress only once all its CTAs are resident, so
 // the update keeps at least g_res_min SMs free for it; beyond that it takes
 // the SMs it needs to finish within about one panel period (an SM's share of
-// the sliced product being kUpdFlopsPerSm in that time) and leaves up to
+// the sliced product being g_upd_flops_per_sm in that time) and leaves up to
 // g_res_max to the panel chain. (0, 0): the update takes every SM.
 static int g_res_min = 24, g_res_max = 88;
-constexpr double kUpdFlopsPerSm = 3.2e8;
+static double g_upd_flops_per_sm = 3.2e8;
 void set_update_reserve(int min_sms, int max_sms) {
   g_res_min = std::max(0, std::min(min_sms, 120));
   g_res_max = std::max(g_res_min, std::min(max_sms, 120));
 }
+void set_update_share(double flops_per_sm) {
+  g_upd_flops_per_sm = flops_per_sm > 1e6 ? flops_per_sm : 3.2e8;
+}
 static int update_ctas(double flops) {
   if (g_res_max <= 0) return 0;
   const int S = num_sms();
-  const int want = (int)std::ceil(flops / kUpdFlopsPerSm);
+  const int want = (int)std::ceil(flops / g_upd_flops_per_sm);
   return std::max(1, std::max(S - g_res_max, std::min(S - g_res_min, want)));
 }
 

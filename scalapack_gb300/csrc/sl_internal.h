@@ -183,6 +183,9 @@ void set_spin_limit(long long polls);
 // SMs (at least min_sms, at most max_sms) that the look-ahead trailing update
 // leaves to the panel's stream; (0, 0) lets it take every SM.
 void set_update_reserve(int min_sms, int max_sms);
+// Sliced-product flops an SM takes in about one panel period (the rule's
+// estimate; larger values leave the panel more SMs).
+void set_update_share(double flops_per_sm);
 // Block size used when a caller passes nb <= 0.
 int default_nb();
 // While an instance lives on a thread, phase timers record nothing on it
