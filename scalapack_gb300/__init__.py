@@ -367,7 +367,7 @@ def pdlaqge(m, n, a, ia, ja, desca, r, c, rowcnd, colcnd, amax) -> str:
 
 # ------------------------------------------------------------ phase timers
 PHASES = ["panel", "laswp", "trsm", "gemm", "solve", "mixed_gemm", "mixed_panel", "refine",
-          "batched", "residual", "precond"]
+          "batched", "residual", "precond", "panel_kernel", "panel_update", "panel_inverse"]
 
 
 def prof_enable(on: bool = True):

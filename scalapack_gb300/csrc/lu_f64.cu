@@ -311,9 +311,14 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
   for (int c = 0; c < jb; c += PW) {
     const int w = (jb - c) < PW ? (jb - c) : PW;
     const int r0 = j + c;
-    SL_TRY(launch_panel<double>(dA, ldda, m, r0, r0, w, dipiv, ws, s));
     const int kw = (m - r0) < w ? (m - r0) : w;
-    for (int k = 0; k < kw; ++k) pflops += 2.0 * (double)(m - r0 - k - 1) * (w - k - 1) + (m - r0 - k - 1);
+    double kflops = 0.0;
+    for (int k = 0; k < kw; ++k) kflops += 2.0 * (double)(m - r0 - k - 1) * (w - k - 1) + (m - r0 - k - 1);
+    pflops += kflops;
+    phase_begin(kPhPanelKernel, s);
+    SL_TRY(launch_panel<double>(dA, ldda, m, r0, r0, w, dipiv, ws, s));
+    phase_end(kPhPanelKernel, s, kflops, 16.0 * (double)(m - r0) * w);
+    phase_begin(kPhPanelUpdate, s);
     SL_TRY(laswp<double>(dA, ldda, r0, r0 + kw, dipiv, j, r0, r0 + w, j + jb, s));
     if (c + w < jb) {
       // The strip solve also publishes the balancing keys of the product that
@@ -343,7 +348,9 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
         pflops += 2.0 * (double)(m - r0 - kw) * (jb - c - w) * kw;
       }
     }
+    phase_end(kPhPanelUpdate, s, 0.0, 0.0);
   }
+  phase_begin(kPhPanelInverse, s);
   // the panel's interchanges in composite form, for the row interchanges of
   // the other columns (computed here, on the panel's stream)
   const int npiv = (m - j) < jb ? (m - j) : jb;
@@ -369,6 +376,7 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
     unit_lower_inv64_kernel<<<(jb + 63) / 64, 256, kInvSmem, s>>>(jb, Ap(j, j), ldda, ws.dinv64);
     count_launches(1);
   }
+  phase_end(kPhPanelInverse, s, (double)jb * jb * jb / 3.0, 16.0 * (double)jb * jb);
   phase_end(kPhPanel, s, pflops, 16.0 * (double)(m - j) * jb);
   return cudaSuccess;
 }

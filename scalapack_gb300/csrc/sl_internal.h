@@ -30,7 +30,13 @@ enum Phase {
   kPhBatched = 8,    // batched solver
   kPhResidual = 9,   // FP64 residuals and matrix-vector products of the refinement
   kPhPrecond = 10,   // low-precision solves applied during the refinement
-  kNumPhases = 11
+  // parts of kPhPanel (timed inside it): the cooperative sub-panel kernels,
+  // the in-panel interchanges, strip solves and sliced products, and the
+  // inverse of L11 with the interchange plan
+  kPhPanelKernel = 11,
+  kPhPanelUpdate = 12,
+  kPhPanelInverse = 13,
+  kNumPhases = 14
 };
 void count_launches(int n);
 void phase_begin(int phase, cudaStream_t s);
