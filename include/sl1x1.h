@@ -335,6 +335,12 @@ void sl1x1_set_panel_rows(int rows);
  * panel's rows over, before the minimum slice above applies. Changes only the
  * speed, not the results. */
 void sl1x1_set_panel_ctas(int ctas);
+/* 32-column sub-panels per in-panel block of the FP64 panel factorization
+ * (1..8, default 2): inside a block only the next sub-panel's columns are
+ * updated after each sub-panel, the columns beyond the block once at its end.
+ * Same pivots except where candidates tie to rounding; factors equal to
+ * rounding. */
+void sl1x1_set_panel_ib(int subpanels);
 /* Pipeline depth of the tcgen05 low-precision update used by the mixed
  * factorization and sl1x1_lowp_update_dev: 2 (default; two CTAs per SM, one's
  * epilogue overlapping the other's main loop) or 3 (one CTA per SM). Changes

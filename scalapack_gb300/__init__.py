@@ -130,6 +130,8 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_set_default_nb.argtypes = [C.c_int]
     L.sl1x1_set_panel_rows.argtypes = [C.c_int]
     L.sl1x1_set_panel_ctas.argtypes = [C.c_int]
+    L.sl1x1_set_panel_ib.argtypes = [C.c_int]
+    L.sl1x1_set_panel_ib.restype = None
     L.sl1x1_set_panel_ctas.restype = None
     L.sl1x1_set_lowp_stages.argtypes = [C.c_int]
     L.sl1x1_set_f64_update.argtypes = [C.c_int]

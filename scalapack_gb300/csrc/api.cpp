@@ -1090,6 +1090,11 @@ void sl1x1_set_copy_chunks(int chunks) {
   g_copy_chunks = chunks < 1 ? 1 : (chunks > sl::kMaxColChunks ? sl::kMaxColChunks : chunks);
 }
 
+void sl1x1_set_panel_ib(int subpanels) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  sl::set_panel_ib(subpanels);
+}
+
 void sl1x1_set_panel_ctas(int ctas) {
   std::lock_guard<std::mutex> lk(g_mu);
   sl::set_panel_ctas(ctas);

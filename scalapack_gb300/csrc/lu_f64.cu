@@ -53,6 +53,8 @@ void set_spin_limit(long long polls) { g_spin_limit = polls < 0 ? kSpinLimit : p
 static int g_panel_min_rows = 0;  // 0: automatic (FP32 256, FP64 128)
 int panel_min_rows() { return g_panel_min_rows; }
 static int g_panel_ctas = 64;  // CTAs a panel's rows are spread over (before the minimum rows)
+static int g_panel_ib = 2;     // sub-panels per in-panel block (factor_panel)
+void set_panel_ib(int ib) { g_panel_ib = ib < 1 ? 1 : (ib > 8 ? 8 : ib); }
 int panel_ctas() { return g_panel_ctas; }
 void set_panel_ctas(int g) { g_panel_ctas = g < 8 ? 8 : (g > 224 ? 224 : g); }
 void set_panel_min_rows(int rows) { g_panel_min_rows = rows <= 0 ? 0 : (rows < 8 ? 8 : (rows > 768 ? 768 : rows)); }
@@ -308,7 +310,14 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
   const OzScratch& sc = (ws.aux && s == ws.aux) ? ws.oz_aux : ws.oz;
   phase_begin(kPhPanel, s);
   double pflops = 0.0;
-  for (int c = 0; c < jb; c += PW) {
+  // Sub-panels are grouped in blocks of g_panel_ib: inside a block only the
+  // next sub-panel's columns are brought up to date after each sub-panel
+  // (left-looking, with every pivot row of the block so far), and the
+  // columns beyond the block once at its end, with the block's rows -- fewer,
+  // deeper in-panel products than one per sub-panel over all the remaining
+  // columns.
+  int blk_r0 = j;  // first row (= column) of the current block
+  for (int c = 0, q = 0; c < jb; c += PW, ++q) {
     const int w = (jb - c) < PW ? (jb - c) : PW;
     const int r0 = j + c;
     const int kw = (m - r0) < w ? (m - r0) : w;
@@ -321,32 +330,40 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
     phase_begin(kPhPanelUpdate, s);
     SL_TRY(laswp<double>(dA, ldda, r0, r0 + kw, dipiv, j, r0, r0 + w, j + jb, s));
     if (c + w < jb) {
+      const bool block_end = (q + 1) % g_panel_ib == 0 || kw < w;
+      // columns brought up to date now: the next sub-panel's, or at the end
+      // of a block every remaining one; rows: the block's pivot rows (U, by
+      // the strip solve) and every row below them (the product)
+      const int ncols = block_end ? jb - c - w : ((jb - c - w) < PW ? (jb - c - w) : PW);
+      const int kb = r0 + kw - blk_r0;
+      const int rl = r0 + kw;  // first row below the block's pivot rows
       // The strip solve also publishes the balancing keys of the product that
       // follows it: the row maxima of its own output (U) and, in extra blocks
-      // of the same launch, the column maxima of the sub-panel's L.
-      const bool keyed = r0 + kw < m && g_f64_update == 1 && oz_fits(sc, m - r0 - kw, jb - c - w, kw);
+      // of the same launch, the column maxima of the block's L.
+      const bool keyed = rl < m && g_f64_update == 1 && oz_fits(sc, m - rl, ncols, kb);
       OzKeyJob kj;
       if (keyed) {
         kj.epoch = oz_new_epoch();
         kj.ckeys = oz_ckeys(sc);
         kj.hkeys = oz_hkeys(sc);
-        kj.L = Ap(r0 + kw, r0);
+        kj.L = Ap(rl, blk_r0);
         kj.ldl = ldda;
-        kj.lrows = m - r0 - kw;
-        kj.lcols = kw;
+        kj.lrows = m - rl;
+        kj.lcols = kb;
       }
-      SL_TRY((trsm_strip<double, false, false, true>(kw, jb - c - w, Ap(r0, r0), ldda,
-                                                      Ap(r0, r0 + w), ldda, s, kj)));
-      pflops += (double)kw * kw * (jb - c - w);
+      SL_TRY((trsm_strip<double, false, false, true>(kb, ncols, Ap(blk_r0, blk_r0), ldda,
+                                                      Ap(blk_r0, r0 + w), ldda, s, kj)));
+      pflops += (double)kb * kb * ncols;
       if (keyed) {
-        SL_TRY(oz_dgemm_keyed(sc, kj.epoch, m - r0 - kw, jb - c - w, kw, -1.0, Ap(r0 + kw, r0),
-                              ldda, Ap(r0, r0 + w), ldda, Ap(r0 + kw, r0 + w), ldda, ws.status, s));
-        pflops += 2.0 * (double)(m - r0 - kw) * (jb - c - w) * kw;
-      } else if (r0 + kw < m) {
-        SL_TRY(lu_update(sc, m - r0 - kw, jb - c - w, kw, -1.0, Ap(r0 + kw, r0), ldda,
-                         Ap(r0, r0 + w), ldda, Ap(r0 + kw, r0 + w), ldda, ws, s));
-        pflops += 2.0 * (double)(m - r0 - kw) * (jb - c - w) * kw;
+        SL_TRY(oz_dgemm_keyed(sc, kj.epoch, m - rl, ncols, kb, -1.0, Ap(rl, blk_r0), ldda,
+                              Ap(blk_r0, r0 + w), ldda, Ap(rl, r0 + w), ldda, ws.status, s));
+        pflops += 2.0 * (double)(m - rl) * ncols * kb;
+      } else if (rl < m) {
+        SL_TRY(lu_update(sc, m - rl, ncols, kb, -1.0, Ap(rl, blk_r0), ldda, Ap(blk_r0, r0 + w), ldda,
+                         Ap(rl, r0 + w), ldda, ws, s));
+        pflops += 2.0 * (double)(m - rl) * ncols * kb;
       }
+      if (block_end) blk_r0 = r0 + w;
     }
     phase_end(kPhPanelUpdate, s, 0.0, 0.0);
   }

@@ -180,6 +180,7 @@ size_t panel_tile_doubles(int m);
 // default, means 256 rows for FP32 and 128 for FP64).
 int panel_min_rows();
 int panel_ctas();
+void set_panel_ib(int ib);
 void set_panel_ctas(int g);
 void set_panel_min_rows(int rows);
 // Polls a panel CTA makes for another CTA's published words before it gives
