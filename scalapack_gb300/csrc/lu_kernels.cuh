@@ -480,46 +480,54 @@ laswp_kernel(T* A, long long lda, int k1, int k2, const int* __restrict__ ipiv, 
 
 // Plan of the interchanges k1..k2-1 (k2-k1 <= LSW_MAXP) in composite form:
 // plan[0] = number of pairs, then (row, src) pairs for every touched row whose
-// content changes (row receives the original content of src). One thread
-// replays the swaps on row labels with a hash table over the touched rows, so
-// the cost is a few shared-memory operations per interchange. Computed once
-// per panel, on the panel's stream; laswp_apply_kernel then only moves data.
-constexpr int LSW_HASH = 1024;
+// content changes (row receives the original content of src). The touched
+// rows are k1..k2-1, then each row outside them in the order the interchanges
+// first reach it; every thread walks the interchanges backwards for its rows
+// (interchange i moves the content followed from ipiv[k1+i] to k1+i or the
+// other way), so the cost is npiv shared-memory reads per row, in parallel.
+// The pairs come out in the order of a sequential replay. Computed once per
+// panel, on the panel's stream; laswp_apply_kernel then only moves data.
 static __device__ __noinline__ void laswp_plan_block(int k1, int k2, const int* __restrict__ ipiv,
                                                     int* plan) {
-  __shared__ int s_row[2 * LSW_MAXP], s_src[2 * LSW_MAXP], s_tab[LSW_HASH], s_piv[LSW_MAXP];
-  const int npiv = k2 - k1;
-  for (int i = threadIdx.x; i < LSW_HASH; i += blockDim.x) s_tab[i] = -1;
-  for (int i = threadIdx.x; i < npiv; i += blockDim.x) {
-    s_row[i] = k1 + i;
-    s_src[i] = k1 + i;
-    s_piv[i] = ipiv[k1 + i];  // staged: the replay below reads shared memory only
+  __shared__ int s_piv[LSW_MAXP], s_first[LSW_MAXP], s_rank[LSW_MAXP];
+  __shared__ int s_row[2 * LSW_MAXP], s_src[2 * LSW_MAXP];
+  __shared__ int s_cnt;
+  const int npiv = k2 - k1, tid = threadIdx.x, nt = blockDim.x;
+  for (int i = tid; i < npiv; i += nt) s_piv[i] = ipiv[k1 + i];
+  __syncthreads();
+  // interchange i reaches an outside row for the first time
+  for (int i = tid; i < npiv; i += nt) {
+    const int p = s_piv[i];
+    bool first = p < k1 || p >= k2;
+    for (int i2 = 0; first && i2 < i; ++i2) first = s_piv[i2] != p;
+    s_first[i] = first ? 1 : 0;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int cnt = npiv;
+  if (tid == 0) {
+    int c = 0;
     for (int i = 0; i < npiv; ++i) {
-      const int p = s_piv[i];
-      if (p == k1 + i) continue;
-      int e;
-      if (p >= k1 && p < k2) {
-        e = p - k1;
-      } else {
-        int h = p & (LSW_HASH - 1);
-        while (s_tab[h] >= 0 && s_row[s_tab[h]] != p) h = (h + 1) & (LSW_HASH - 1);
-        if (s_tab[h] < 0) {  // first time this row is touched
-          e = cnt++;
-          s_row[e] = p;
-          s_src[e] = p;
-          s_tab[h] = e;
-        } else {
-          e = s_tab[h];
-        }
-      }
-      const int t = s_src[i];
-      s_src[i] = s_src[e];
-      s_src[e] = t;
+      s_rank[i] = c;
+      c += s_first[i];
     }
+    s_cnt = npiv + c;
+  }
+  __syncthreads();
+  for (int i = tid; i < npiv; i += nt) {
+    s_row[i] = k1 + i;
+    if (s_first[i]) s_row[npiv + s_rank[i]] = s_piv[i];
+  }
+  __syncthreads();
+  const int cnt = s_cnt;
+  for (int e = tid; e < cnt; e += nt) {
+    int q = s_row[e];
+    for (int i = npiv - 1; i >= 0; --i) {
+      const int p = s_piv[i];
+      q = (q == k1 + i) ? p : ((q == p) ? k1 + i : q);
+    }
+    s_src[e] = q;
+  }
+  __syncthreads();
+  if (tid == 0) {
     int np = 0;
     for (int e = 0; e < cnt; ++e)
       if (s_src[e] != s_row[e]) {
