@@ -153,6 +153,8 @@ def lib(build_if_missing: bool = False):
     L.sl1x1_set_update_reserve.argtypes = [C.c_int, C.c_int]
     L.sl1x1_set_split_step.argtypes = [C.c_int]
     L.sl1x1_set_update_share.argtypes = [C.c_double]
+    L.sl1x1_set_inpanel_cap.argtypes = [C.c_int]
+    L.sl1x1_set_inpanel_cap.restype = None
     L.sl1x1_set_update_share.restype = None
     L.sl1x1_set_split_step.restype = None
     L.sl1x1_set_update_reserve.restype = None

@@ -1160,6 +1160,11 @@ void sl1x1_set_update_reserve(int min_sms, int max_sms) {
   sl::set_update_reserve(min_sms, max_sms);
 }
 
+void sl1x1_set_inpanel_cap(int on) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  sl::set_inpanel_cap(on);
+}
+
 void sl1x1_set_update_share(double flops_per_sm) {
   std::lock_guard<std::mutex> lk(g_mu);
   sl::set_update_share(flops_per_sm);

@@ -129,6 +129,12 @@ int f64_update_get() { return g_f64_update; }
 // the sliced product being g_upd_flops_per_sm in that time) and leaves up to
 // g_res_max to the panel chain. (0, 0): the update takes every SM.
 static int g_res_min = 24, g_res_max = 88;
+static int g_inpanel_cap = 1;
+static int g_next_cap = 1;
+void set_inpanel_cap(int on) {
+  g_inpanel_cap = on ? 1 : 0;
+  g_next_cap = on >= 2 ? 0 : 1;
+}
 static double g_upd_flops_per_sm = 3.2e8;
 void set_update_reserve(int min_sms, int max_sms) {
   g_res_min = std::max(0, std::min(min_sms, 120));
@@ -356,7 +362,8 @@ static cudaError_t factor_panel(int m, double* dA, long long ldda, int* dipiv, i
       pflops += (double)kb * kb * ncols;
       if (keyed) {
         SL_TRY(oz_dgemm_keyed(sc, kj.epoch, m - rl, ncols, kb, -1.0, Ap(rl, blk_r0), ldda,
-                              Ap(blk_r0, r0 + w), ldda, Ap(rl, r0 + w), ldda, ws.status, s));
+                              Ap(blk_r0, r0 + w), ldda, Ap(rl, r0 + w), ldda, ws.status, s,
+                              ws.aux && s == ws.aux ? ws.inpanel_ctas : 0));
         pflops += 2.0 * (double)(m - rl) * ncols * kb;
       } else if (rl < m) {
         SL_TRY(lu_update(sc, m - rl, ncols, kb, -1.0, Ap(rl, blk_r0), ldda, Ap(blk_r0, r0 + w), ldda,
@@ -536,10 +543,16 @@ cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, 
       phase_begin(kPhTrsm, ws.aux);
       SL_TRY(solve_u12(jb, jb2, Ap(j, j), ldda, Ap(j, jn), ldda, aw, ws.aux));
       phase_end(kPhTrsm, ws.aux, (double)jb * jb * jb2, 8.0 * (0.5 * jb * jb + 2.0 * jb * jb2));
+      // the next panel's update and in-panel products run on the SMs the
+      // update of the other columns (beside them) leaves
+      const int rest_cols = n - jn - jb2;
+      const int upd = rest_cols > 0 ? update_ctas(2.0 * mr * rest_cols * jb) : 0;
+      const int free_sms = (g_inpanel_cap && upd > 0) ? num_sms() - upd : 0;
       phase_begin(kPhGemm, ws.aux);
       SL_TRY(lu_update(ws.oz_aux, m - jn, jb2, jb, -1.0, Ap(jn, j), ldda, Ap(j, jn), ldda, Ap(jn, jn),
-                       ldda, ws, ws.aux));
+                       ldda, ws, ws.aux, g_next_cap ? free_sms : 0));
       phase_end(kPhGemm, ws.aux, 2.0 * mr * jb2 * jb, 8.0 * (mr * jb + (double)jb * jb2 + 2.0 * mr * jb2));
+      nxt.inpanel_ctas = free_sms;
       SL_TRY(factor_panel(m, dA, ldda, dipiv, jn, jb2, nxt, ws.aux));
       SL_TRY(cudaEventRecord(ws.ev_panel, ws.aux));
       panel_on_aux = true;

@@ -895,8 +895,9 @@ cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, con
 
 cudaError_t oz_dgemm_keyed(const OzScratch& sc, unsigned long long epoch, int m, int n, int k,
                            double alpha, const double* A, long long lda, const double* B,
-                           long long ldb, double* C, long long ldc, int* status, cudaStream_t s) {
-  return oz_dgemm_impl(0, epoch, sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, status, s);
+                           long long ldb, double* C, long long ldc, int* status, cudaStream_t s,
+                           int max_ctas) {
+  return oz_dgemm_impl(0, epoch, sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, status, s, max_ctas);
 }
 
 cudaError_t oz_dgemm_bside(const OzScratch& sc, int m, int n, int k, double alpha,

@@ -86,7 +86,8 @@ cudaError_t oz_dgemm_bside(const OzScratch& sc, int m, int n, int k, double alph
 // oz_hkeys(sc) by the kernels that produced A and B: one launch fewer.
 cudaError_t oz_dgemm_keyed(const OzScratch& sc, unsigned long long epoch, int m, int n, int k,
                            double alpha, const double* A, long long lda, const double* B,
-                           long long ldb, double* C, long long ldc, int* status, cudaStream_t s);
+                           long long ldb, double* C, long long ldc, int* status, cudaStream_t s,
+                           int max_ctas = 0);
 unsigned long long oz_new_epoch();
 unsigned long long* oz_ckeys(const OzScratch& sc);
 unsigned long long* oz_hkeys(const OzScratch& sc);
@@ -150,6 +151,9 @@ struct LuWork {
   // the next panel's columns go first on the caller's stream.
   double* dinv64_alt = nullptr;
   int* swap_plan_alt = nullptr;
+  // Grid cap of the in-panel products on the panel's stream (0: none): the
+  // SMs the trailing update beside them leaves free.
+  int inpanel_ctas = 0;
 };
 // Most column chunks a streamed factorization takes.
 constexpr int kMaxColChunks = 16;
@@ -193,6 +197,8 @@ void set_update_reserve(int min_sms, int max_sms);
 // Sliced-product flops an SM takes in about one panel period (the rule's
 // estimate; larger values leave the panel more SMs).
 void set_update_share(double flops_per_sm);
+// Split step: the in-panel products keep to the SMs the update leaves.
+void set_inpanel_cap(int on);
 // Block size used when a caller passes nb <= 0.
 int default_nb();
 // While an instance lives on a thread, phase timers record nothing on it
