@@ -317,11 +317,12 @@ void sl1x1_set_update_reserve(int min_sms, int max_sms);
  * panel period (default 3.2e8; larger values leave the panel more SMs; <= 1e6
  * restores the default). Changes only the speed. */
 void sl1x1_set_update_share(double flops_per_sm);
-/* In the split look-ahead step, the next panel's update and its in-panel
- * sliced products cap their grids at the SMs the trailing update beside them
- * leaves (1, the default; each CTA then loops over more tiles); 2 caps only
- * the in-panel products, 0 neither. Changes only the speed. */
-void sl1x1_set_inpanel_cap(int on);
+/* Grid caps of the split look-ahead step, a bit mask (default 7): 1 the
+ * next panel's in-panel sliced products and 2 its update keep to the SMs the
+ * trailing update beside them leaves (each CTA then loops over more tiles);
+ * 4 the caller's stream's U12 solve and row interchanges keep to the
+ * update's own SMs. Changes only the speed. */
+void sl1x1_set_inpanel_cap(int mask);
 /* Test hook for the bounded device waits: the number of polls a panel CTA
  * makes for another CTA's published pivot candidates before it gives up
  * (polls < 0 restores the default, 2^24; 0 makes every wait run out at its

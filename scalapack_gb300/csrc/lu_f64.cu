@@ -129,12 +129,11 @@ int f64_update_get() { return g_f64_update; }
 // the sliced product being g_upd_flops_per_sm in that time) and leaves up to
 // g_res_max to the panel chain. (0, 0): the update takes every SM.
 static int g_res_min = 24, g_res_max = 88;
-static int g_inpanel_cap = 1;
-static int g_next_cap = 1;
-void set_inpanel_cap(int on) {
-  g_inpanel_cap = on ? 1 : 0;
-  g_next_cap = on >= 2 ? 0 : 1;
-}
+// Grid caps in the split step (bit mask): 1 the in-panel products and 2 the
+// next panel's update keep to the SMs the trailing update leaves; 4 the
+// caller's stream's U12 solve and interchanges keep to the update's SMs.
+static int g_cap_mask = 7;
+void set_inpanel_cap(int mask) { g_cap_mask = mask & 7; }
 static double g_upd_flops_per_sm = 3.2e8;
 void set_update_reserve(int min_sms, int max_sms) {
   g_res_min = std::max(0, std::min(min_sms, 120));
@@ -291,9 +290,10 @@ unit_lower_inv_cols_kernel(int jb, const double* __restrict__ L, long long ldl, 
 // balanced by the rows of A12, which carry the pivots' scales. Otherwise the
 // FP64 strip solve.
 static cudaError_t solve_u12(int jb, int nr, const double* L11, long long ldl, double* A12,
-                             long long lda, const LuWork& ws, cudaStream_t s) {
+                             long long lda, const LuWork& ws, cudaStream_t s, int max_ctas = 0) {
   if (g_f64_update == 1 && ws.dinv64 && jb <= kFullInvMax && oz_fits(ws.oz, jb, nr, jb))
-    return oz_dgemm_bside(ws.oz, jb, nr, jb, 1.0, ws.dinv64, jb, A12, lda, A12, lda, ws.status, s);
+    return oz_dgemm_bside(ws.oz, jb, nr, jb, 1.0, ws.dinv64, jb, A12, lda, A12, lda, ws.status, s,
+                          max_ctas);
   if (!(g_f64_update == 1 && ws.dinv64 && jb <= 1024 && oz_fits(ws.oz, jb, nr, 64)))
     return trsm_strip<double, false, false, true>(jb, nr, L11, ldl, A12, lda, s);
   for (int r0 = 0; r0 < jb; r0 += 64) {
@@ -547,23 +547,24 @@ cudaError_t dgetrf_device(int m, int n, double* dA, long long ldda, int* dipiv, 
       // update of the other columns (beside them) leaves
       const int rest_cols = n - jn - jb2;
       const int upd = rest_cols > 0 ? update_ctas(2.0 * mr * rest_cols * jb) : 0;
-      const int free_sms = (g_inpanel_cap && upd > 0) ? num_sms() - upd : 0;
+      const int free_sms = upd > 0 ? num_sms() - upd : 0;
       phase_begin(kPhGemm, ws.aux);
       SL_TRY(lu_update(ws.oz_aux, m - jn, jb2, jb, -1.0, Ap(jn, j), ldda, Ap(j, jn), ldda, Ap(jn, jn),
-                       ldda, ws, ws.aux, g_next_cap ? free_sms : 0));
+                       ldda, ws, ws.aux, (g_cap_mask & 2) ? free_sms : 0));
       phase_end(kPhGemm, ws.aux, 2.0 * mr * jb2 * jb, 8.0 * (mr * jb + (double)jb * jb2 + 2.0 * mr * jb2));
-      nxt.inpanel_ctas = free_sms;
+      nxt.inpanel_ctas = (g_cap_mask & 1) ? free_sms : 0;
       SL_TRY(factor_panel(m, dA, ldda, dipiv, jn, jb2, nxt, ws.aux));
       SL_TRY(cudaEventRecord(ws.ev_panel, ws.aux));
       panel_on_aux = true;
       // the other columns on the caller's stream
       const int c2 = jn + jb2, rest = n - c2;
+      const int main_cap = (g_cap_mask & 4) ? upd : 0;
       phase_begin(kPhLaswp, s);
-      SL_TRY(laswp_planned<double>(dA, ldda, j, jn, dipiv, cur.swap_plan, 0, j, c2, n, s));
+      SL_TRY(laswp_planned<double>(dA, ldda, j, jn, dipiv, cur.swap_plan, 0, j, c2, n, s, main_cap));
       phase_end(kPhLaswp, s, 0.0, 32.0 * jb * (double)(n - jb - jb2));
       if (rest > 0) {
         phase_begin(kPhTrsm, s);
-        SL_TRY(solve_u12(jb, rest, Ap(j, j), ldda, Ap(j, c2), ldda, cur, s));
+        SL_TRY(solve_u12(jb, rest, Ap(j, j), ldda, Ap(j, c2), ldda, cur, s, main_cap));
         phase_end(kPhTrsm, s, (double)jb * jb * rest, 8.0 * (0.5 * jb * jb + 2.0 * jb * rest));
         phase_begin(kPhGemm, s);
         SL_TRY(lu_update(ws.oz, m - jn, rest, jb, -1.0, Ap(jn, j), ldda, Ap(j, c2), ldda, Ap(jn, c2),

@@ -1119,12 +1119,12 @@ inline cudaError_t laswp_plan(int k1, int k2, const int* ipiv, int* plan, cudaSt
 template <typename T>
 inline cudaError_t laswp_planned(T* A, long long lda, int k1, int k2, const int* ipiv,
                                  const int* plan, int cb1, int ce1, int cb2, int ce2,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, int max_ctas = 0) {
   const long long ncols = (long long)(ce1 - cb1) + (ce2 - cb2);
   if (ncols <= 0 || k2 <= k1) return cudaSuccess;
   if (!plan || k2 - k1 > LSW_MAXP) return laswp<T>(A, lda, k1, k2, ipiv, cb1, ce1, cb2, ce2, s);
   const long long want = (ncols + 7) / 8;
-  const long long cap = 4LL * num_sms();
+  const long long cap = max_ctas > 0 ? (long long)max_ctas : 4LL * num_sms();
   laswp_apply_kernel<T><<<(unsigned)(want < cap ? want : cap), 256, 0, s>>>(A, lda, plan, cb1, ce1,
                                                                             cb2, ce2);
   count_launches(1);

@@ -902,8 +902,8 @@ cudaError_t oz_dgemm_keyed(const OzScratch& sc, unsigned long long epoch, int m,
 
 cudaError_t oz_dgemm_bside(const OzScratch& sc, int m, int n, int k, double alpha,
                            const double* A, long long lda, const double* B, long long ldb,
-                           double* C, long long ldc, int* status, cudaStream_t s) {
-  return oz_dgemm_impl(1, 0ULL, sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, status, s);
+                           double* C, long long ldc, int* status, cudaStream_t s, int max_ctas) {
+  return oz_dgemm_impl(1, 0ULL, sc, m, n, k, alpha, A, lda, B, ldb, C, ldc, status, s, max_ctas);
 }
 
 }  // namespace sl

@@ -80,7 +80,7 @@ cudaError_t oz_dgemm(const OzScratch& sc, int m, int n, int k, double alpha, con
 // it updates (the U12 solve), whose rows carry the pivots' scales.
 cudaError_t oz_dgemm_bside(const OzScratch& sc, int m, int n, int k, double alpha,
                            const double* A, long long lda, const double* B, long long ldb,
-                           double* C, long long ldc, int* status, cudaStream_t s);
+                           double* C, long long ldc, int* status, cudaStream_t s, int max_ctas = 0);
 // The same (side A) with the balancing keys of its single pass (k <= 256)
 // already published with `epoch` (from oz_new_epoch) into oz_ckeys(sc) and
 // oz_hkeys(sc) by the kernels that produced A and B: one launch fewer.
