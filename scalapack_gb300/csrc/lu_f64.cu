@@ -843,8 +843,9 @@ cudaError_t dgetrs_device(char trans, int n, int nrhs, const double* dA, long lo
   phase_begin(kPhSolve, s);
   SL_TRY(perm_compose(dipiv, n, ws.perm, s));
   double* X = ws.bswap;  // n x nrhs, ld = n
+  // any NRHS whose products fit the scratch (PDGETRI solves with NRHS = N)
   const bool inv_path = g_f64_update == 1 && ws.dinv_solve && ws.dinv_solve_len >= kSolveInvDoubles(n) &&
-                        nrhs <= 64 && oz_fits(ws.oz, n, nrhs, 128);
+                        oz_fits(ws.oz, n, nrhs, 128);
   if (notran && inv_path) {
     SL_TRY((permute_rows<double, double>(dB, lddb, X, n, ws.perm, n, nrhs, 0, s)));
     const int nb64 = (n + 63) / 64;
