@@ -56,6 +56,22 @@ def measured_peaks():
                 "source": "fallback"}
 
 
+def phase_table(phases, steps, hbm_gbs):
+    """Per-step phase figures from the library's phase timers: launches, device
+    ms, algorithmic TFLOP/s and GB/s, and the GB/s as a fraction of the
+    measured HBM copy bandwidth (the roofline of the memory-bound phases)."""
+    out = {}
+    for k, (launches, ms, flops, nbytes) in phases.items():
+        if launches <= 0:
+            continue
+        gbs = (nbytes / (ms * 1e-3) / 1e9) if ms > 0 and nbytes > 0 else None
+        out[k] = {"launches": launches, "ms_per_step": ms / steps,
+                  "tflops": (flops / (ms * 1e-3) / 1e12) if ms > 0 and flops > 0 else None,
+                  "gbs": gbs,
+                  "hbm_frac": (gbs / hbm_gbs) if (gbs and hbm_gbs) else None}
+    return out
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -598,10 +614,7 @@ def run_gpu(args):
                                    "(sl1x1_dmma_peak_tflops); MEASURED_PEAKS.json has no FP64 figure",
                     "launches": g_launch, "avg_launch_ms": g_ms / max(1, g_launch),
                     "algorithmic_bytes_per_launch": g_bytes / max(1, g_launch)}
-    phase_summary = {k: {"launches": v[0], "ms_per_step": v[1] / args.steps,
-                         "tflops": (v[2] / (v[1] * 1e-3) / 1e12) if v[1] > 0 and v[2] > 0 else None,
-                         "gbs": (v[3] / (v[1] * 1e-3) / 1e9) if v[1] > 0 and v[3] > 0 else None}
-                     for k, v in phases.items() if v[0] > 0}
+    phase_summary = phase_table(phases, args.steps, measured_peaks().get("hbm_gbs"))
 
     # end to end through the Fortran-ABI entry point with pinned host buffers
     e2e = None

@@ -32,3 +32,15 @@ def test_reference_arm_json_line():
     e = d["e2e"]
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+
+
+def test_phase_table_fractions():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    ph = {"laswp": (10, 5.0, 0.0, 4.0e9), "gemm": (4, 20.0, 8.0e12, 1.0e9), "solve": (0, 0.0, 0.0, 0.0)}
+    t = bench.phase_table(ph, 2, 8000.0)
+    assert set(t) == {"laswp", "gemm"}
+    assert t["laswp"]["ms_per_step"] == 2.5 and t["laswp"]["tflops"] is None
+    assert abs(t["laswp"]["gbs"] - 800.0) < 1e-9 and abs(t["laswp"]["hbm_frac"] - 0.1) < 1e-12
+    assert abs(t["gemm"]["tflops"] - 400.0) < 1e-9
