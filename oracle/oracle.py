@@ -100,6 +100,8 @@ def lib():
     L.orc_pdlange.restype = C.c_double
     L.orc_pdgecon.argtypes = [C.c_char, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double]
     L.orc_pdgecon.restype = C.c_double
+    L.orc_pdgetri.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int]
+    L.orc_pdgetri.restype = C.c_int
     L.orc_pdgerfs.argtypes = [C.c_char, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
                               C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                               C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
@@ -304,6 +306,16 @@ def pdlange(norm, A):
 def pdgecon(norm, LU, anorm):
     LU = np.asfortranarray(LU, dtype=np.float64)
     return lib().orc_pdgecon(norm.encode(), LU.shape[0], _p(LU), max(LU.shape[0], 1), 1, 1, anorm)
+
+
+def pdgetri(LU, ipiv_rel, nb=64):
+    """PDGETRI on a 1x1 grid from the factors L, U and 0-based relative pivots (as
+    pdgetrf leaves them, minus one): (INFO, inv(A) or the unchanged LU)."""
+    X = np.asfortranarray(np.array(LU, dtype=np.float64))
+    piv = np.ascontiguousarray(ipiv_rel, dtype=np.int32)
+    n = X.shape[0]
+    info = lib().orc_pdgetri(n, _p(X), max(n, 1), 1, 1, _p(piv), nb)
+    return info, X
 
 
 def pdgerfs(trans, A, AF, ipiv, B, X):

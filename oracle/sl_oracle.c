@@ -952,3 +952,102 @@ int orc_pdgesvx(char fact, char trans, int n, int nrhs, double* A, int lda, int 
   }
   return 0;
 }
+
+/* ------------------------------------------------------------------------- */
+/* PDGETRI on a 1x1 grid                                                      */
+/* ------------------------------------------------------------------------- */
+/* PDTRTI2, upper non-unit (SRC/pdtrti2.f:194-211), on the n x n block T (ld
+ * ldt): column j's diagonal is inverted, then its entries above the diagonal
+ * become -inv(T(j,j)) times the already-inverted leading block applied to
+ * them (DTRMV 'Upper', in place, rows in ascending order). */
+static void orc_trti2_upper(int n, double* T, int ldt) {
+  for (int j = 0; j < n; ++j) {
+    A_AT(T, ldt, j, j) = 1.0 / A_AT(T, ldt, j, j);
+    const double ajj = -A_AT(T, ldt, j, j);
+    for (int i = 0; i < j; ++i) {
+      double s = 0.0;
+      for (int k = i; k < j; ++k) s += A_AT(T, ldt, i, k) * A_AT(T, ldt, k, j);
+      A_AT(T, ldt, i, j) = s;
+    }
+    for (int i = 0; i < j; ++i) A_AT(T, ldt, i, j) *= ajj;
+  }
+}
+
+/* PDGETRI (SRC/pdgetri.f:299-372) with PDTRTRI (SRC/pdtrtri.f:226-302) on a
+ * 1x1 grid: A (n x n at (ia, ja), ld lda) holds L\U and ipiv_rel the 0-based
+ * pivot rows relative to IA. Returns INFO: the first zero U(i,i) (1-based;
+ * A untouched) or 0 with inv(A) in place. Blocked by nb as the reference:
+ * inv(U) block column by block column (TRMM with the inverted leading block,
+ * TRSM by the diagonal block, PDTRTI2 on it), then inv(A) L = inv(U) from the
+ * last block column back (the block column of L copied out and zeroed, one
+ * GEMM with the columns already done, a unit-lower TRSM from the right), then
+ * the pivots applied to the columns backwards (PDLAPIV 'Backward', 'Columns'). */
+int orc_pdgetri(int n, double* A, int lda, int ia, int ja, const int* ipiv_rel, int nb) {
+  if (n <= 0) return 0;
+  double* S = A + (ia - 1) + (size_t)(ja - 1) * lda;
+  for (int i = 0; i < n; ++i)
+    if (A_AT(S, lda, i, i) == 0.0) return i + 1;
+  if (nb < 1) nb = 1;
+  /* inv(U) */
+  for (int j = 0; j < n; j += nb) {
+    const int jb = (n - j) < nb ? (n - j) : nb;
+    if (j > 0) {
+      /* B = A(0:j, j:j+jb) := triu(A(0:j, 0:j)) B (TRMM 'Left', 'Upper'): row by row ascending */
+      for (int c = 0; c < jb; ++c)
+        for (int i = 0; i < j; ++i) {
+          double s = 0.0;
+          for (int k = i; k < j; ++k) s += A_AT(S, lda, i, k) * A_AT(S, lda, k, j + c);
+          A_AT(S, lda, i, j + c) = s;
+        }
+      /* B := -B inv(U_jj) (TRSM 'Right', 'Upper', non-unit): columns ascending */
+      for (int c = 0; c < jb; ++c) {
+        for (int k = 0; k < c; ++k) {
+          const double u = A_AT(S, lda, j + k, j + c);
+          for (int i = 0; i < j; ++i) A_AT(S, lda, i, j + c) -= A_AT(S, lda, i, j + k) * u;
+        }
+        const double d = A_AT(S, lda, j + c, j + c);
+        for (int i = 0; i < j; ++i) A_AT(S, lda, i, j + c) /= d;
+      }
+      for (int c = 0; c < jb; ++c)
+        for (int i = 0; i < j; ++i) A_AT(S, lda, i, j + c) = -A_AT(S, lda, i, j + c);
+    }
+    orc_trti2_upper(jb, &A_AT(S, lda, j, j), lda);
+  }
+  /* inv(A) L = inv(U), block columns from the last one back */
+  double* W = (double*)malloc(sizeof(double) * (size_t)n * (size_t)nb);
+  const int nn = ((n - 1) / nb) * nb;
+  for (int j = nn; j >= 0; j -= nb) {
+    const int jb = (n - j) < nb ? (n - j) : nb;
+    /* W(r, c) = L(r, j + c) for rows r > j + c (W is n x jb, row index global), then zeroed in A */
+    for (int c = 0; c < jb; ++c)
+      for (int r = 0; r < n; ++r) {
+        if (r > j + c) {
+          A_AT(W, n, r, c) = A_AT(S, lda, r, j + c);
+          A_AT(S, lda, r, j + c) = 0.0;
+        } else {
+          A_AT(W, n, r, c) = 0.0;
+        }
+      }
+    if (j + jb < n)
+      orc_dgemm('N', 'N', n, jb, n - j - jb, -1.0, &A_AT(S, lda, 0, j + jb), lda, &A_AT(W, n, j + jb, 0),
+                n, 1.0, &A_AT(S, lda, 0, j), lda);
+    /* X(:, j:j+jb) := X inv(L_jj) (TRSM 'Right', 'Lower', unit): columns descending */
+    for (int c = jb - 1; c >= 0; --c)
+      for (int k = c + 1; k < jb; ++k) {
+        const double l = A_AT(W, n, j + k, c);
+        for (int i = 0; i < n; ++i) A_AT(S, lda, i, j + c) -= A_AT(S, lda, i, j + k) * l;
+      }
+  }
+  free(W);
+  /* the row interchanges of the factorization, applied to the columns backwards */
+  for (int j = n - 1; j >= 0; --j) {
+    const int p = ipiv_rel[j];
+    if (p != j)
+      for (int i = 0; i < n; ++i) {
+        const double t = A_AT(S, lda, i, j);
+        A_AT(S, lda, i, j) = A_AT(S, lda, i, p);
+        A_AT(S, lda, i, p) = t;
+      }
+  }
+  return 0;
+}
