@@ -268,11 +268,16 @@ def test_pdgetri_inverse(sl, orc, ctx, n, nb):
     d = np.array([1, ctx, n, n, nb, nb, 0, 0, n], np.int32)
     ipiv = np.zeros(n + nb, dtype=np.int32)
     assert sl.pdgetrf(n, n, A, 1, 1, d, ipiv) == 0
+    LU = np.asfortranarray(A.copy())
     info, _, _ = sl.pdgetri(n, A, 1, 1, d, ipiv)
     assert info == 0
     R = A0 @ A - np.eye(n)
     eps = 2.0 ** -53
     assert np.abs(R).sum(1).max() / (np.abs(A0).sum(1).max() * np.abs(A).sum(1).max() * n * eps) < 16
+    # the oracle's restatement of the reference's algorithm on the same factors
+    info_o, Xo = orc.pdgetri(LU, ipiv[:n] - 1, nb)
+    assert info_o == 0
+    assert np.abs(A - Xo).max() <= 1e-8 * np.abs(Xo).max()
 
 
 def test_pdgetri_singular_info(sl, orc, ctx):
