@@ -17,6 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIBNAME = "libsl1x1gpu.so"
+ILP64_NAME = "libsl1x1gpu_ilp64.so"  # the same entry points with 8-byte INTEGERs
 SOURCES = ["api.cpp", "expert_api.cpp", "redist.cpp", "prof.cpp", "dgemm_f64.cu", "lu_f64.cu", "noalloc.cu", "mixed_gemm.cu", "ozgemm_f64.cu", "mixed.cu", "batched.cu", "aux.cu", "refine.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -30,6 +31,10 @@ def nvcc_path() -> str:
 
 def lib_path() -> str:
     return os.path.join(LIBDIR, LIBNAME)
+
+
+def ilp64_path() -> str:
+    return os.path.join(LIBDIR, ILP64_NAME)
 
 
 def _stale(out: str, deps) -> bool:
@@ -69,12 +74,27 @@ def build(force: bool = False, verbose: bool = False) -> str:
         raise RuntimeError(f"nvcc failed:\n{msg}")
     so = lib_path()
     if force or _stale(so, objs):
-        cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-o", so, *objs, "-lpthread"]
+        # -Bsymbolic: the library's calls to its own entry points stay inside it
+        # even when the ILP64 library's same-named symbols come first
+        cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-Xlinker", "-Bsymbolic", "-o", so, *objs,
+               "-lpthread"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))
+    # the ILP64 (8-byte INTEGER) entry points: host code that loads this library
+    src64 = os.path.join(CSRC, "ilp64.cpp")
+    so64 = ilp64_path()
+    hdr64 = os.path.join(os.path.dirname(HERE), "include", "sl1x1_ilp64.h")
+    if force or _stale(so64, [src64, hdr64]):
+        cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+        cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-fPIC", "-shared", "-o", so64, src64, "-ldl"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+        if r.returncode != 0:
+            raise RuntimeError("ILP64 build failed:\n" + r.stdout.decode(errors="replace"))
     return so
 
 
