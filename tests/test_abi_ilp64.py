@@ -153,3 +153,33 @@ def test_pdgesv_through_both_abis_bitwise(L64, sl, orc, gpu_required):
     np.testing.assert_array_equal(A64, A32)
     np.testing.assert_array_equal(B64, B32)
     assert orc.sresid(A0, B0, B64) < 16.0
+
+
+def test_workspace_queries_match_the_32_bit_library(L64, sl):
+    # LWORK = LIWORK = -1: WORK(1) and IWORK(1) report the minimal sizes, no device work
+    ctx = sl.blacs_gridinit(1, 1)
+    n, nb = 500, 64
+    A = np.asfortranarray(np.eye(n))
+    d32 = np.array([1, ctx, n, n, nb, nb, 0, 0, n], np.int32)
+    d64 = np.array(d32, np.int64)
+    rc32, info32, w32, iw32 = sl.pdgecon("1", n, A, 1, 1, d32, 1.0, lwork=-1, liwork=-1)
+    work = np.zeros(4)
+    iwork = np.zeros(4, np.int64)
+    rc, info = C.c_double(), I64(5)
+    L64.pdgecon_(b"1", ref(n), p(A), ref(1), ref(1), p(d64), C.byref(C.c_double(1.0)), C.byref(rc),
+                 p(work), ref(-1), p(iwork), ref(-1), C.byref(info), C.c_size_t(1))
+    assert info.value == info32 == 0
+    assert work[0] == w32 and iwork[0] == iw32 > 0
+    ipiv32 = np.arange(1, n + nb + 1, dtype=np.int32)
+    info32, w32, iw32 = sl.pdgetri(n, A, 1, 1, d32, ipiv32, lwork=-1, liwork=-1)
+    ipiv64 = np.arange(1, n + nb + 1, dtype=np.int64)
+    work[:] = 0
+    iwork[:] = 0
+    L64.pdgetri_(ref(n), p(A), ref(1), ref(1), p(d64), p(ipiv64), p(work), ref(-1), p(iwork), ref(-1),
+                 C.byref(info))
+    assert info.value == info32 == 0
+    assert work[0] == w32 and iwork[0] == iw32 > 0
+    # argument errors: the 32-bit codes
+    L64.pdgetri_(ref(-3), p(A), ref(1), ref(1), p(d64), p(ipiv64), p(work), ref(10), p(iwork), ref(10),
+                 C.byref(info))
+    assert info.value == sl.pdgetri(-3, A, 1, 1, d32, ipiv32, lwork=10, liwork=10)[0] == -1
